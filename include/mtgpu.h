@@ -1,0 +1,155 @@
+/*
+ * libmtgpu — GB300-native (sm_103a) solve stage of the MTCalc 3-D
+ * magnetotelluric modeller: the COCR solver for complex-symmetric systems with
+ * the folded preconditioner, on the 2x2-block SLAE format of the reference
+ * (kiselev2013/MTCalc_with_DFP_COCR).
+ *
+ * Plain C ABI: plain pointers and sizes, no exceptions, every call returns an
+ * int status.  Reference citations are paths inside the reference repository.
+ *
+ * Status codes.  The solver codes are the reference's RCI codes
+ * (Code/COCR_FP/rci.h:23-42); library failures use values below -100.
+ */
+#ifndef MTGPU_H
+#define MTGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MTGPU_OK 0                 /* REQ_OK: converged                         */
+#define MTGPU_X0_NULL (-1)         /* REQ_X0_NULL: the initial guess solves A x = b */
+#define MTGPU_DIV_BY_ZERO (-2)     /* REQ_DIV_BY_ZERO: (a, w) = 0 breakdown     */
+#define MTGPU_MAXITER (-3)         /* REQ_MAXITER: iteration limit reached      */
+#define MTGPU_ERR_ARG (-101)       /* invalid argument                           */
+#define MTGPU_ERR_CUDA (-102)      /* a CUDA call failed (see mtgpu_last_error) */
+#define MTGPU_ERR_IO (-103)        /* a file could not be read or written        */
+#define MTGPU_ERR_UNSUPPORTED (-104)
+#define MTGPU_ERR_TIMEOUT (-105)   /* a bounded device wait gave up              */
+
+/* Text of the last library error of the calling process. */
+const char *mtgpu_last_error(void);
+
+/* Number of kernels this library has launched in this process (graph
+ * launches count every kernel node they contain). */
+unsigned long long mtgpu_kernel_launches(void);
+
+/* ------------------------------------------------------------------------
+ * Drop-in solver: replaces PCOCR::PCOCR_2x2_Folded
+ * (Code/COCR_FP/pcocr.h:27-31, Code/COCR_FP/pcocr.cpp:40-126).
+ *
+ * Same arguments, meaning and ownership, all host pointers, 0-based arrays:
+ *   n          2 * number of edges (real length of pr and x)
+ *   ig, jg, idi, ijg, di, gg   lower-triangle 2x2-block SLAE
+ *   pr         right-hand side, x initial guess in / solution out
+ *   eps, maxiter   stop at smoothed relative residual < eps (rci.cpp:66-75)
+ *   y_omp      the reference's OpenMP scratch; unused here (may be NULL)
+ *   kpar ... is_node_bound   mesh data of the folded preconditioner
+ * Returns MTGPU_OK / MTGPU_X0_NULL / MTGPU_DIV_BY_ZERO / MTGPU_MAXITER as the
+ * reference does, or an MTGPU_ERR_* code.  Like the reference it writes the
+ * `kit` file ("r=%e\teps=%e\tkit=%d\ttime=%lf sec") in the current directory
+ * (Code/COCR_FP/base_solver.cpp:181-200).
+ * ---------------------------------------------------------------------- */
+int mtgpu_pcocr_2x2_folded(int n, int *ig, int *jg, int *idi, int *ijg, double *di,
+                           double *gg, double *pr, double *x, double eps, int maxiter,
+                           double *y_omp, int kpar, int n_edges_c, int n_nodes_c,
+                           double (*xyz)[3], int *nvkat, int (*nver)[14], double *sigma3d,
+                           int (*edges)[2], int *ig_t, int *jg_t, double *gg_t,
+                           int *is_node_bound);
+
+typedef struct {
+    int iterations;            /* the reference's `iter` at exit              */
+    double residual_rel;       /* smoothed relative residual of the stop test */
+    double true_residual_rel;  /* ||b - A x|| / ||b|| of the returned x (FP64) */
+    double setup_seconds;      /* upload, format conversion, preconditioner   */
+    double solve_seconds;      /* COCR iterations                             */
+    int status;
+} mtgpu_solve_stats;
+
+typedef struct {
+    /* 0: stop where the reference stops (MRS-smoothed residual < eps).
+     * 1: after that, keep iterating until the true residual ||b-Ax||/||b||
+     *    is below eps as well (checked on the GPU in FP64). */
+    int stop_on_true_residual;
+    /* iterations per CUDA-graph launch between host status checks (0: 16) */
+    int iterations_per_launch;
+} mtgpu_solve_opts;
+
+/* Same as mtgpu_pcocr_2x2_folded with options and statistics and without
+ * writing `kit`.  opts and stats may be NULL. */
+int mtgpu_pcocr_2x2_folded_ex(int n, const int *ig, const int *jg, const int *idi,
+                              const int *ijg, const double *di, const double *gg,
+                              const double *pr, double *x, double eps, int maxiter,
+                              int kpar, int n_edges_c, int n_nodes_c, const double *xyz,
+                              const int *nvkat, const int *nver14, const double *sigma3d,
+                              const int *edges2, const int *ig_t, const int *jg_t,
+                              const double *gg_t, const int *is_node_bound,
+                              const mtgpu_solve_opts *opts, mtgpu_solve_stats *stats);
+
+/* y = A x on host buffers; replaces Block_2x2_solver::Mult_MV_block_2x2
+ * (Code/COCR_FP/block_2x2_solver.cpp:73-173).  x, y: 2*nb doubles. */
+int mtgpu_mult_mv_block_2x2(int nb, const int *ig, const int *jg, const int *idi,
+                            const int *ijg, const double *di, const double *gg,
+                            const double *x, double *y);
+
+/* Folded preconditioner on host buffers: BuildGMatrix + BuildDiagComplex +
+ * ApplyPreconditionerComplex (Code/COCR_FP/FoldedPreconditioner.cpp:68-259,
+ * 473-574, 578-630).  y = D_A x + G^T D_S G x.  When diag_a (2*nb doubles)
+ * and diag_gagt (2*m doubles, m returned in *m_out) are not NULL they receive
+ * 1/diag(A) and 1/diag(G A G^T). */
+int mtgpu_folded_apply(int nb, const int *ig, const int *jg, const int *idi,
+                       const int *ijg, const double *di, const double *gg,
+                       int kpar, int n_nodes_c, const int *nvkat, const int *nver14,
+                       const double *sigma3d, const int *edges2, const int *ig_t,
+                       const int *jg_t, const double *gg_t, const int *is_node_bound,
+                       const double *x, double *y, int *m_out, double *diag_a,
+                       double *diag_gagt);
+
+/* ------------------------------------------------------------------------
+ * Device-resident solver context: the matrix (SELL-32 full storage) and the
+ * folded preconditioner live in GPU memory; right-hand sides and solutions
+ * are device pointers.  This is the GB300-native form of the drop-in above
+ * (the drop-in is create + solve + destroy around host copies).
+ * ---------------------------------------------------------------------- */
+typedef struct mtgpu_cocr_s mtgpu_cocr;
+
+/* Build a context.  `on_device` = 1: the SLAE arrays are device pointers;
+ * 0: host pointers (copied).  The mesh arrays are always host pointers.
+ * stream: a cudaStream_t (NULL = legacy default stream). */
+int mtgpu_cocr_create(int nb, int nnz_lower, const int *ig, const int *jg, const int *idi,
+                      const int *ijg, const double *di, const double *gg, int on_device,
+                      int kpar, int n_nodes_c, const int *nvkat, const int *nver14,
+                      const double *sigma3d, const int *edges2, const int *ig_t,
+                      const int *jg_t, const double *gg_t, const int *is_node_bound,
+                      void *stream, mtgpu_cocr **out);
+
+/* Solve A x = b with x (device, 2*nb doubles) as initial guess. */
+int mtgpu_cocr_solve(mtgpu_cocr *ctx, const double *d_b, double *d_x, double eps,
+                     int maxiter, const mtgpu_solve_opts *opts, mtgpu_solve_stats *stats);
+
+/* y = A x and y = M^{-1} x on device vectors (2*nb doubles). */
+int mtgpu_cocr_spmv(mtgpu_cocr *ctx, const double *d_x, double *d_y);
+int mtgpu_cocr_precond(mtgpu_cocr *ctx, const double *d_x, double *d_y);
+
+/* Sizes of the device matrix: stored complex and real entries (without
+ * padding) and the number of preconditioner nodes m. */
+int mtgpu_cocr_info(const mtgpu_cocr *ctx, long long *nnz_complex, long long *nnz_real,
+                    int *m_nodes);
+
+void mtgpu_cocr_destroy(mtgpu_cocr *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+/* Internal: mesh arrays of the folded preconditioner bundled together. */
+typedef struct {
+    int kpar, n_edges_c, n_nodes_c;
+    const int *nvkat, *nver14;
+    const double *sigma3d;
+    const int *edges2, *ig_t, *jg_t;
+    const double *gg_t;
+    const int *is_node_bound;
+} mtgpu_mesh_desc;
+
+#endif

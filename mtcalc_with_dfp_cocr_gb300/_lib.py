@@ -1,0 +1,106 @@
+"""ctypes binding of libmtgpu (include/mtgpu.h).
+
+The library is loaded from the package's in-tree _build/ directory.  There
+is no fallback: if the shared object is missing or fails to load, every call
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libmtgpu.so")
+
+_i = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_d = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_vp = C.c_void_p
+
+MTGPU_OK = 0
+MTGPU_X0_NULL = -1
+MTGPU_DIV_BY_ZERO = -2
+MTGPU_MAXITER = -3
+MTGPU_ERR_ARG = -101
+MTGPU_ERR_CUDA = -102
+MTGPU_ERR_IO = -103
+MTGPU_ERR_UNSUPPORTED = -104
+MTGPU_ERR_TIMEOUT = -105
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("residual_rel", C.c_double),
+                ("true_residual_rel", C.c_double), ("setup_seconds", C.c_double),
+                ("solve_seconds", C.c_double), ("status", C.c_int)]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("stop_on_true_residual", C.c_int), ("iterations_per_launch", C.c_int)]
+
+
+class MtgpuError(RuntimeError):
+    pass
+
+
+# (name, restype, argtypes) of every exported entry point
+SIGNATURES = {
+    "mtgpu_last_error": (C.c_char_p, []),
+    "mtgpu_kernel_launches": (C.c_ulonglong, []),
+    "mtgpu_pcocr_2x2_folded": (C.c_int, [
+        C.c_int, _i, _i, _i, _i, _d, _d, _d, _d, C.c_double, C.c_int, _vp,
+        C.c_int, C.c_int, C.c_int, _d, _i, _i, _d, _i, _i, _i, _d, _i]),
+    "mtgpu_pcocr_2x2_folded_ex": (C.c_int, [
+        C.c_int, _i, _i, _i, _i, _d, _d, _d, _d, C.c_double, C.c_int,
+        C.c_int, C.c_int, C.c_int, _d, _i, _i, _d, _i, _i, _i, _d, _i,
+        C.POINTER(SolveOpts), C.POINTER(SolveStats)]),
+    "mtgpu_mult_mv_block_2x2": (C.c_int, [C.c_int, _i, _i, _i, _i, _d, _d, _d, _d]),
+    "mtgpu_folded_apply": (C.c_int, [
+        C.c_int, _i, _i, _i, _i, _d, _d, C.c_int, C.c_int, _i, _i, _d, _i, _i, _i, _d, _i,
+        _d, _d, C.POINTER(C.c_int), _vp, _vp]),
+    "mtgpu_cocr_create": (C.c_int, [
+        C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int,
+        C.c_int, C.c_int, _i, _i, _d, _i, _i, _i, _d, _i, _vp, C.POINTER(_vp)]),
+    "mtgpu_cocr_solve": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int,
+                                   C.POINTER(SolveOpts), C.POINTER(SolveStats)]),
+    "mtgpu_cocr_spmv": (C.c_int, [_vp, _vp, _vp]),
+    "mtgpu_cocr_precond": (C.c_int, [_vp, _vp, _vp]),
+    "mtgpu_cocr_info": (C.c_int, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
+                                  C.POINTER(C.c_int)]),
+    "mtgpu_cocr_destroy": (None, [_vp]),
+}
+
+_lib = None
+
+
+def lib():
+    """Load libmtgpu; raises if it is not built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise MtgpuError(f"libmtgpu is not built ({LIB_PATH} missing); "
+                             "run __graft_entry__.build() or python -m "
+                             "mtcalc_with_dfp_cocr_gb300.build")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    s = lib().mtgpu_last_error()
+    return s.decode() if s else ""
+
+
+def check(rc: int, what: str) -> int:
+    """Raise on library errors (codes below -100); solver codes pass through."""
+    if rc <= -100:
+        raise MtgpuError(f"{what} failed ({rc}): {last_error()}")
+    return rc
+
+
+def kernel_launches() -> int:
+    return int(lib().mtgpu_kernel_launches())

@@ -1,0 +1,418 @@
+// extern "C" entry points of libmtgpu (declared in include/mtgpu.h).
+#include "mtgpu_internal.cuh"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+namespace mtgpu {
+
+static std::mutex g_err_mu;
+static std::string g_err = "";
+static std::atomic<unsigned long long> g_launches{0};
+
+void set_last_error(cudaError_t e, const char *what, const char *file, int line)
+{
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_err = std::string(cudaGetErrorName(e)) + ": " + cudaGetErrorString(e) + " in " + what +
+            " (" + file + ":" + std::to_string(line) + ")";
+}
+
+void set_last_message(const char *msg)
+{
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_err = msg;
+}
+
+void note_launches(unsigned long long k) { g_launches += k; }
+
+}  // namespace mtgpu
+
+using namespace mtgpu;
+
+struct mtgpu_cocr_s {
+    CocrSolver S;
+    bool own_stream = false;
+};
+
+namespace {
+
+double now_s()
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+
+template <class T>
+int upload(T **d, const T *h, size_t count, cudaStream_t st)
+{
+    int rc = dev_alloc(d, count);
+    if (rc) return rc;
+    if (count) MTGPU_TRY(cudaMemcpyAsync(*d, h, count * sizeof(T), cudaMemcpyHostToDevice, st));
+    return MTGPU_OK;
+}
+
+struct LowerDev {
+    int *ig = nullptr, *jg = nullptr, *idi = nullptr, *ijg = nullptr;
+    double *di = nullptr, *gg = nullptr;
+    ~LowerDev()
+    {
+        dev_free(ig); dev_free(jg); dev_free(idi); dev_free(ijg); dev_free(di); dev_free(gg);
+    }
+};
+
+int upload_lower(int nb, const int *ig, const int *jg, const int *idi, const int *ijg,
+                 const double *di, const double *gg, LowerDev &L, cudaStream_t st)
+{
+    const int nnz = ig[nb];
+    int rc;
+    if ((rc = upload(&L.ig, ig, nb + 1, st)) || (rc = upload(&L.jg, jg, nnz, st)) ||
+        (rc = upload(&L.idi, idi, nb + 1, st)) || (rc = upload(&L.ijg, ijg, nnz + 1, st)) ||
+        (rc = upload(&L.di, di, (size_t)idi[nb], st)) ||
+        (rc = upload(&L.gg, gg, (size_t)ijg[nnz], st)))
+        return rc;
+    return MTGPU_OK;
+}
+
+int validate_lower(int nb, const int *ig, const int *jg, const int *idi, const int *ijg)
+{
+    MTGPU_CHECK_ARG(nb > 0, "n must be a positive even number");
+    MTGPU_CHECK_ARG(ig && jg && idi && ijg, "null SLAE pointer");
+    MTGPU_CHECK_ARG(ig[0] == 0 && idi[0] == 0, "ig/idi must be 0-based offsets");
+    for (int i = 0; i < nb; i++) {
+        MTGPU_CHECK_ARG(ig[i + 1] >= ig[i], "ig is not monotone");
+        const int ds = idi[i + 1] - idi[i];
+        MTGPU_CHECK_ARG(ds == 1 || ds == 2, "diagonal block size must be 1 or 2");
+        for (int q = ig[i]; q < ig[i + 1]; q++) {
+            MTGPU_CHECK_ARG(jg[q] >= 0 && jg[q] < i, "jg must hold lower-triangle columns");
+            const int s = ijg[q + 1] - ijg[q];
+            MTGPU_CHECK_ARG(s == 1 || s == 2, "off-diagonal block size must be 1 or 2");
+        }
+    }
+    return MTGPU_OK;
+}
+
+int validate_mesh(const mtgpu_mesh_desc &m)
+{
+    MTGPU_CHECK_ARG(m.kpar >= 0 && m.n_edges_c > 0 && m.n_nodes_c > 0, "bad mesh sizes");
+    MTGPU_CHECK_ARG(m.nvkat && m.nver14 && m.sigma3d && m.edges2 && m.is_node_bound,
+                    "null mesh pointer");
+    for (int e = 0; e < m.n_edges_c; e++)
+        for (int k = 0; k < 2; k++) {
+            const int v = m.edges2[2 * e + k];
+            MTGPU_CHECK_ARG(v >= 0, "negative node in edges");
+            if (v >= m.n_nodes_c) MTGPU_CHECK_ARG(m.ig_t && m.jg_t && m.gg_t,
+                                                  "edge node beyond n_nodes_c without T-matrix");
+        }
+    for (int c = 0; c < m.kpar; c++)
+        for (int j = 0; j < 8; j++) MTGPU_CHECK_ARG(m.nver14[(size_t)c * 14 + j] >= 0, "bad nver");
+    return MTGPU_OK;
+}
+
+int make_stream(mtgpu_cocr_s *c, void *stream)
+{
+    if (stream) {
+        c->S.st = (cudaStream_t)stream;
+        c->own_stream = false;
+    } else {
+        MTGPU_TRY(cudaStreamCreateWithFlags(&c->S.st, cudaStreamNonBlocking));
+        c->own_stream = true;
+    }
+    return MTGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *mtgpu_last_error(void)
+{
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    static thread_local std::string copy;
+    copy = g_err;
+    return copy.c_str();
+}
+
+unsigned long long mtgpu_kernel_launches(void) { return g_launches.load(); }
+
+int mtgpu_cocr_create(int nb, int nnz_lower, const int *ig, const int *jg, const int *idi,
+                      const int *ijg, const double *di, const double *gg, int on_device,
+                      int kpar, int n_nodes_c, const int *nvkat, const int *nver14,
+                      const double *sigma3d, const int *edges2, const int *ig_t,
+                      const int *jg_t, const double *gg_t, const int *is_node_bound,
+                      void *stream, mtgpu_cocr **out)
+{
+    MTGPU_CHECK_ARG(out != nullptr, "out is null");
+    *out = nullptr;
+    MTGPU_CHECK_ARG(nb > 0, "nb must be positive");
+    if (!on_device) {
+        int rc = validate_lower(nb, ig, jg, idi, ijg);
+        if (rc) return rc;
+        nnz_lower = ig[nb];
+    }
+    mtgpu_mesh_desc mesh{kpar, nb, n_nodes_c, nvkat, nver14, sigma3d, edges2, ig_t, jg_t,
+                         gg_t, is_node_bound};
+    int rc = validate_mesh(mesh);
+    if (rc) return rc;
+    auto *c = new mtgpu_cocr_s();
+    if ((rc = make_stream(c, stream))) {
+        delete c;
+        return rc;
+    }
+    CocrSolver &S = c->S;
+    S.nb = nb;
+    MTGPU_TRY(cudaStreamSynchronize(cudaStreamLegacy));
+    {
+        LowerDev L;
+        if (!on_device) {
+            if ((rc = upload_lower(nb, ig, jg, idi, ijg, di, gg, L, S.st))) goto fail;
+            rc = sell_from_block2x2_device(nb, L.ig, L.jg, L.idi, L.ijg, L.di, L.gg, nnz_lower,
+                                           S.A, S.st);
+        } else {
+            rc = sell_from_block2x2_device(nb, ig, jg, idi, ijg, di, gg, nnz_lower, S.A, S.st);
+        }
+        note_launches(5);
+        if (rc) goto fail;
+    }
+    if ((rc = folded_build_g(mesh, S.P, S.st))) goto fail;
+    if ((rc = folded_build_diag(S.A, S.P, S.st))) goto fail;
+    note_launches(2);
+    if ((rc = cocr_alloc(S))) goto fail;
+    {
+        cudaError_t e = cudaStreamSynchronize(S.st);
+        if (e != cudaSuccess) {
+            set_last_error(e, "mtgpu_cocr_create", __FILE__, __LINE__);
+            rc = MTGPU_ERR_CUDA;
+            goto fail;
+        }
+    }
+    *out = c;
+    return MTGPU_OK;
+fail:
+    mtgpu_cocr_destroy(c);
+    return rc;
+}
+
+void mtgpu_cocr_destroy(mtgpu_cocr *c)
+{
+    if (!c) return;
+    if (c->S.st) cudaStreamSynchronize(c->S.st);
+    c->S.release();
+    if (c->own_stream && c->S.st) cudaStreamDestroy(c->S.st);
+    delete c;
+}
+
+int mtgpu_cocr_solve(mtgpu_cocr *c, const double *d_b, double *d_x, double eps, int maxiter,
+                     const mtgpu_solve_opts *opts, mtgpu_solve_stats *stats)
+{
+    MTGPU_CHECK_ARG(c && d_b && d_x, "null argument");
+    MTGPU_CHECK_ARG(((uintptr_t)d_b % 16) == 0 && ((uintptr_t)d_x % 16) == 0,
+                    "vectors must be 16-byte aligned");
+    MTGPU_TRY(cudaStreamSynchronize(cudaStreamLegacy));
+    const double t0 = now_s();
+    int rc = cocr_solve(c->S, (const double2 *)d_b, (double2 *)d_x, eps, maxiter,
+                        opts ? opts->stop_on_true_residual : 0,
+                        opts ? opts->iterations_per_launch : 0, stats);
+    if (stats) stats->solve_seconds = now_s() - t0;
+    return rc;
+}
+
+int mtgpu_cocr_spmv(mtgpu_cocr *c, const double *d_x, double *d_y)
+{
+    MTGPU_CHECK_ARG(c && d_x && d_y, "null argument");
+    MTGPU_TRY(cudaStreamSynchronize(cudaStreamLegacy));
+    sell_spmv(c->S.A, (const double2 *)d_x, (double2 *)d_y, c->S.st);
+    note_launches(1);
+    MTGPU_TRY(cudaGetLastError());
+    MTGPU_TRY(cudaStreamSynchronize(c->S.st));
+    return MTGPU_OK;
+}
+
+int mtgpu_cocr_precond(mtgpu_cocr *c, const double *d_x, double *d_y)
+{
+    MTGPU_CHECK_ARG(c && d_x && d_y, "null argument");
+    MTGPU_TRY(cudaStreamSynchronize(cudaStreamLegacy));
+    folded_apply(c->S.P, (const double2 *)d_x, (double2 *)d_y, c->S.st);
+    note_launches(2);
+    MTGPU_TRY(cudaGetLastError());
+    MTGPU_TRY(cudaStreamSynchronize(c->S.st));
+    return MTGPU_OK;
+}
+
+int mtgpu_cocr_info(const mtgpu_cocr *c, long long *nnz_complex, long long *nnz_real,
+                    int *m_nodes)
+{
+    MTGPU_CHECK_ARG(c != nullptr, "null context");
+    if (nnz_complex) *nnz_complex = c->S.A.nnz_c;
+    if (nnz_real) *nnz_real = c->S.A.nnz_r;
+    if (m_nodes) *m_nodes = c->S.P.m;
+    return MTGPU_OK;
+}
+
+int mtgpu_pcocr_2x2_folded_ex(int n, const int *ig, const int *jg, const int *idi,
+                              const int *ijg, const double *di, const double *gg,
+                              const double *pr, double *x, double eps, int maxiter,
+                              int kpar, int n_edges_c, int n_nodes_c, const double *xyz,
+                              const int *nvkat, const int *nver14, const double *sigma3d,
+                              const int *edges2, const int *ig_t, const int *jg_t,
+                              const double *gg_t, const int *is_node_bound,
+                              const mtgpu_solve_opts *opts, mtgpu_solve_stats *stats)
+{
+    (void)xyz;
+    MTGPU_CHECK_ARG(n > 0 && n % 2 == 0, "n must be a positive even number");
+    MTGPU_CHECK_ARG(pr && x, "null vector");
+    const int nb = n / 2;
+    MTGPU_CHECK_ARG(n_edges_c == nb, "n_edges_c must equal n/2 (all edges are unknowns)");
+    const double t0 = now_s();
+    mtgpu_cocr *c = nullptr;
+    int rc = mtgpu_cocr_create(nb, 0, ig, jg, idi, ijg, di, gg, 0, kpar, n_nodes_c, nvkat,
+                               nver14, sigma3d, edges2, ig_t, jg_t, gg_t, is_node_bound,
+                               nullptr, &c);
+    if (rc) return rc;
+    double *d_b = nullptr, *d_x = nullptr;
+    mtgpu_solve_stats st{};
+    if ((rc = dev_alloc(&d_b, n)) || (rc = dev_alloc(&d_x, n))) goto out;
+    {
+        cudaError_t e = cudaMemcpyAsync(d_b, pr, sizeof(double) * n, cudaMemcpyHostToDevice, c->S.st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_x, x, sizeof(double) * n, cudaMemcpyHostToDevice, c->S.st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->S.st);
+        if (e != cudaSuccess) {
+            set_last_error(e, "upload of pr/x", __FILE__, __LINE__);
+            rc = MTGPU_ERR_CUDA;
+            goto out;
+        }
+    }
+    {
+        const double t1 = now_s();
+        st.setup_seconds = t1 - t0;
+        rc = cocr_solve(c->S, (const double2 *)d_b, (double2 *)d_x, eps, maxiter,
+                        opts ? opts->stop_on_true_residual : 0,
+                        opts ? opts->iterations_per_launch : 0, &st);
+        if (rc < -100) goto out;
+        cudaError_t e = cudaMemcpyAsync(x, d_x, sizeof(double) * n, cudaMemcpyDeviceToHost, c->S.st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->S.st);
+        if (e != cudaSuccess) {
+            set_last_error(e, "download of x", __FILE__, __LINE__);
+            rc = MTGPU_ERR_CUDA;
+            goto out;
+        }
+        st.solve_seconds = now_s() - t1;
+    }
+    if (stats) *stats = st;
+out:
+    dev_free(d_b);
+    dev_free(d_x);
+    mtgpu_cocr_destroy(c);
+    return rc;
+}
+
+int mtgpu_pcocr_2x2_folded(int n, int *ig, int *jg, int *idi, int *ijg, double *di,
+                           double *gg, double *pr, double *x, double eps, int maxiter,
+                           double *y_omp, int kpar, int n_edges_c, int n_nodes_c,
+                           double (*xyz)[3], int *nvkat, int (*nver)[14], double *sigma3d,
+                           int (*edges)[2], int *ig_t, int *jg_t, double *gg_t,
+                           int *is_node_bound)
+{
+    (void)y_omp;
+    const double t0 = now_s();
+    mtgpu_solve_stats st{};
+    st.residual_rel = 1.0;
+    const int rc = mtgpu_pcocr_2x2_folded_ex(
+        n, ig, jg, idi, ijg, di, gg, pr, x, eps, maxiter, kpar, n_edges_c, n_nodes_c,
+        (const double *)xyz, nvkat, (const int *)nver, sigma3d, (const int *)edges, ig_t, jg_t,
+        gg_t, is_node_bound, nullptr, &st);
+    if (rc < -100) return rc;
+    const double secs = now_s() - t0;
+    // the reference's `kit` line, base_solver.cpp:181-200
+    FILE *fp = fopen("kit", "w");
+    if (!fp) {
+        set_last_message("cannot open file kit");
+        return MTGPU_ERR_IO;
+    }
+    fprintf(fp, "r=%e\teps=%e\tkit=%d\t", st.residual_rel, eps, st.iterations);
+    fprintf(fp, "time=%lf sec\n", secs);
+    fclose(fp);
+    return rc;
+}
+
+int mtgpu_mult_mv_block_2x2(int nb, const int *ig, const int *jg, const int *idi,
+                            const int *ijg, const double *di, const double *gg,
+                            const double *x, double *y)
+{
+    int rc = validate_lower(nb, ig, jg, idi, ijg);
+    if (rc) return rc;
+    MTGPU_CHECK_ARG(x && y, "null vector");
+    cudaStream_t st;
+    MTGPU_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    SellMatrix A;
+    double2 *dx = nullptr, *dy = nullptr;
+    {
+        LowerDev L;
+        if (!(rc = upload_lower(nb, ig, jg, idi, ijg, di, gg, L, st)))
+            rc = sell_from_block2x2_device(nb, L.ig, L.jg, L.idi, L.ijg, L.di, L.gg, ig[nb], A, st);
+        note_launches(5);
+    }
+    if (!rc && !(rc = upload(&dx, (const double2 *)x, nb, st)) && !(rc = dev_alloc(&dy, nb))) {
+        sell_spmv(A, dx, dy, st);
+        note_launches(1);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(y, dy, sizeof(double2) * nb, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            set_last_error(e, "mtgpu_mult_mv_block_2x2", __FILE__, __LINE__);
+            rc = MTGPU_ERR_CUDA;
+        }
+    }
+    cudaStreamSynchronize(st);
+    dev_free(dx);
+    dev_free(dy);
+    A.release();
+    cudaStreamDestroy(st);
+    return rc;
+}
+
+int mtgpu_folded_apply(int nb, const int *ig, const int *jg, const int *idi, const int *ijg,
+                       const double *di, const double *gg, int kpar, int n_nodes_c,
+                       const int *nvkat, const int *nver14, const double *sigma3d,
+                       const int *edges2, const int *ig_t, const int *jg_t, const double *gg_t,
+                       const int *is_node_bound, const double *x, double *y, int *m_out,
+                       double *diag_a, double *diag_gagt)
+{
+    MTGPU_CHECK_ARG(x && y, "null vector");
+    mtgpu_cocr *c = nullptr;
+    int rc = mtgpu_cocr_create(nb, 0, ig, jg, idi, ijg, di, gg, 0, kpar, n_nodes_c, nvkat,
+                               nver14, sigma3d, edges2, ig_t, jg_t, gg_t, is_node_bound,
+                               nullptr, &c);
+    if (rc) return rc;
+    double2 *dx = nullptr, *dy = nullptr;
+    cudaStream_t st = c->S.st;
+    if (!(rc = upload(&dx, (const double2 *)x, nb, st)) && !(rc = dev_alloc(&dy, nb))) {
+        folded_apply(c->S.P, dx, dy, st);
+        note_launches(2);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(y, dy, sizeof(double2) * nb, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess && diag_a)
+            e = cudaMemcpyAsync(diag_a, c->S.P.d_da, sizeof(double2) * nb, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess && diag_gagt && c->S.P.m > 0)
+            e = cudaMemcpyAsync(diag_gagt, c->S.P.d_ds, sizeof(double2) * c->S.P.m,
+                                cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            set_last_error(e, "mtgpu_folded_apply", __FILE__, __LINE__);
+            rc = MTGPU_ERR_CUDA;
+        }
+    }
+    if (m_out) *m_out = c->S.P.m;
+    cudaStreamSynchronize(st);
+    dev_free(dx);
+    dev_free(dy);
+    mtgpu_cocr_destroy(c);
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,147 @@
+// Internal declarations shared by the libmtgpu translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <algorithm>
+#include <vector>
+
+#include "../../include/mtgpu.h"
+
+namespace mtgpu {
+
+// --------------------------------------------------------------- errors
+#define MTGPU_TRY(expr)                                                        \
+    do {                                                                       \
+        cudaError_t e_ = (expr);                                               \
+        if (e_ != cudaSuccess) {                                               \
+            ::mtgpu::set_last_error(e_, #expr, __FILE__, __LINE__);           \
+            return MTGPU_ERR_CUDA;                                             \
+        }                                                                      \
+    } while (0)
+
+#define MTGPU_CHECK_ARG(cond, msg)                                             \
+    do {                                                                       \
+        if (!(cond)) {                                                         \
+            ::mtgpu::set_last_message(msg);                                    \
+            return MTGPU_ERR_ARG;                                              \
+        }                                                                      \
+    } while (0)
+
+void set_last_error(cudaError_t e, const char *what, const char *file, int line);
+void set_last_message(const char *msg);
+
+constexpr int kSlice = 32;          // SELL slice height = one warp of rows
+constexpr int kThreads = 256;       // default block size for row/edge kernels
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// ------------------------------------------------ device matrix (SELL-32)
+// Full (both triangles) complex-symmetric matrix in sliced ELL with slice
+// height 32.  Every row is split into complex slots (diagonal and parallel
+// edge pairs: 16-byte values) and real slots (perpendicular pairs: 8-byte
+// values).  Slot k of row (32*s + l) lives at sptr[s] + 32*k + l, so a warp
+// reading one slot of its 32 rows touches one contiguous segment.
+struct SellMatrix {
+    int nb = 0;                 // rows (edges)
+    int nslices = 0;
+    long long nnz_c = 0, nnz_r = 0;          // stored entries without padding
+    long long len_c = 0, len_r = 0;          // stored slots with padding
+    int *d_wc = nullptr, *d_wr = nullptr;    // slice widths [nslices]
+    long long *d_pc = nullptr, *d_pr = nullptr;  // slice offsets [nslices+1]
+    int *d_col_c = nullptr, *d_col_r = nullptr;
+    double2 *d_val_c = nullptr;
+    double *d_val_r = nullptr;
+    int *d_diag_slot = nullptr;   // complex slot index of the diagonal, per row
+    void release();
+};
+
+// Builds the SELL matrix from the reference lower 2x2-block storage that is
+// already resident on the device (0-based arrays).
+int sell_from_block2x2_device(int nb, const int *d_ig, const int *d_jg, const int *d_idi,
+                              const int *d_ijg, const double *d_di, const double *d_gg,
+                              int nnz_lower, SellMatrix &A, cudaStream_t st);
+
+// y = A x  (x, y complex interleaved, device)
+void sell_spmv(const SellMatrix &A, const double2 *x, double2 *y, cudaStream_t st);
+// y = b - A x
+void sell_residual(const SellMatrix &A, const double2 *b, const double2 *x, double2 *y,
+                   cudaStream_t st);
+
+// ------------------------------------------------ folded preconditioner
+struct Folded {
+    int n = 0, m = 0;                  // edges, interior conductive nodes
+    int *d_gp = nullptr, *d_gj = nullptr;   double *d_gv = nullptr;   // G   (CSR, m rows)
+    int *d_tp = nullptr, *d_tj = nullptr;   double *d_tv = nullptr;   // G^T (CSR, n rows)
+    double2 *d_da = nullptr;           // 1/diag(A)
+    double2 *d_ds = nullptr;           // 1/diag(G A G^T)
+    double2 *d_h = nullptr;            // node work vector
+    void release();
+};
+
+// Host construction of G and G^T (FoldedPreconditioner.cpp:68-259 semantics),
+// uploaded to the device.
+int folded_build_g(const mtgpu_mesh_desc &mesh, Folded &P, cudaStream_t st);
+// D_A and D_S from the device matrix.
+int folded_build_diag(const SellMatrix &A, Folded &P, cudaStream_t st);
+// y = D_A x + G^T D_S G x
+void folded_apply(const Folded &P, const double2 *x, double2 *y, cudaStream_t st);
+
+// ------------------------------------------------ COCR solver state
+struct Ctl;   // device control block (cocr.cu)
+struct CocrSolver {
+    SellMatrix A;
+    Folded P;
+    cudaStream_t st = nullptr;
+    int nb = 0;
+    int grid = 0;                 // blocks of the reduction kernels
+    double2 *r = nullptr, *p = nullptr, *s = nullptr, *z = nullptr, *a = nullptr,
+            *w = nullptr, *sm = nullptr;
+    double *partials = nullptr;
+    Ctl *ctl = nullptr;           // device
+    Ctl *hctl = nullptr;          // pinned host mirror
+    cudaGraphExec_t graph = nullptr;
+    const void *graph_x = nullptr;
+    int graph_iters = 0;
+    void release();
+};
+int cocr_alloc(CocrSolver &S);
+int cocr_solve(CocrSolver &S, const double2 *b, double2 *x, double eps, int maxiter,
+               int stop_true, int iters_per_launch, mtgpu_solve_stats *stats);
+void note_launches(unsigned long long k);
+
+// ------------------------------------------------ small device helpers
+__host__ __device__ inline double2 cmul(double2 a, double2 b)
+{
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ inline double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__host__ __device__ inline double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+// a / b with scaling against overflow (Smith's algorithm)
+__host__ __device__ inline double2 cdiv(double2 a, double2 b)
+{
+    if (fabs(b.x) >= fabs(b.y)) {
+        const double r = b.y / b.x, d = b.x + b.y * r;
+        return make_double2((a.x + a.y * r) / d, (a.y - a.x * r) / d);
+    }
+    const double r = b.x / b.y, d = b.x * r + b.y;
+    return make_double2((a.x * r + a.y) / d, (a.y * r - a.x) / d);
+}
+
+// device allocation helpers (record the failing call)
+template <class T>
+int dev_alloc(T **p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) count = 1;
+    MTGPU_TRY(cudaMalloc((void **)p, count * sizeof(T)));
+    return MTGPU_OK;
+}
+template <class T>
+void dev_free(T *&p)
+{
+    if (p) cudaFree((void *)p);
+    p = nullptr;
+}
+
+}  // namespace mtgpu

@@ -1,0 +1,51 @@
+#!/usr/bin/env bash
+# Builds the reference's own CPU programs for the solve stage from their
+# sources where they lie (read-only), into oracle/_ref/.  Nothing is copied
+# and no reference file is edited: Windows-only names come from the
+# force-included shims in oracle/ref_shim/.
+#
+# Test infrastructure only.  The binaries are the pinning oracle for
+# tests/golden/make_golden.py; the product never links or runs them.
+#
+#   COCR_FP      Code/COCR_FP/*.cpp      the reference solver (PCOCR_2x2_Folded)
+#   BuildMatrix  Code/BuildMatrix/*.cpp  the reference SLAE assembly
+#   Harm1D       Code/Harm1D/*.cpp       the reference 1-D normal field
+#
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+set -euo pipefail
+REF="${1:-/root/reference}"
+HERE="$(cd "$(dirname "$0")" && pwd)"
+OUT="$HERE/_ref"
+SHIM="$HERE/ref_shim"
+mkdir -p "$OUT"
+
+if [ ! -d "$REF/Code/COCR_FP" ]; then
+    echo "build_ref: no reference sources at $REF; nothing to build" >&2
+    exit 0
+fi
+
+CXX="${CXX:-g++}"
+# `intn` is a typo for `int n` in COCR_FP/rci.h:63 and COCR_FP/T_Mapping.h:40;
+# the macro restores the declaration without touching the file.
+COMMON=(-O2 -fopenmp -fpermissive -w -std=gnu++14 -D'intn=int n'
+        -include "$SHIM/msvc_compat.h" -I "$SHIM/include")
+
+build_prog() {
+    local name="$1"; shift
+    local src="$REF/Code/$name"
+    local objdir="$OUT/obj_$name"
+    mkdir -p "$objdir"
+    local objs=()
+    for f in "$src"/*.cpp; do
+        local o="$objdir/$(basename "${f%.cpp}").o"
+        "$CXX" "${COMMON[@]}" "$@" -I "$src" -c "$f" -o "$o" &
+        objs+=("$o")
+    done
+    wait
+    "$CXX" -fopenmp -o "$OUT/$name" "${objs[@]}"
+    echo "build_ref: $OUT/$name"
+}
+
+build_prog COCR_FP
+build_prog BuildMatrix -include "$SHIM/llp64.h"
+build_prog Harm1D -include "$SHIM/llp64.h"
