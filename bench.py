@@ -1,0 +1,386 @@
+"""Benchmark: time per solve to true relative residual 1e-8 on the
+96x96x64-cell survey mesh (1.8M edges, 0.1 Hz, both polarisations).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+GPU arm (default).  A step solves every system of the workload on the GPU
+from the device-resident assembly: per frequency the COCR context is built on
+the device (A = K + i omega M, folded preconditioner set-up), then each
+polarisation is solved with the reference's stop rule and, in addition, until
+the true residual ||b - A x|| / ||b|| < 1e-8.  `value` is seconds per solve
+(lower is better) from CUDA events on the solver's stream; the matrix
+(~0.9 GB) is larger than L2, so no flush is needed between iterations.
+`e2e` is the same metric through the reference-facing C ABI
+(mtgpu_pcocr_2x2_folded_ex) with the SLAE in host memory: upload, set-up,
+solve and download of x every step.  `roofline` is the SpMV kernel
+(the dominant kernel) against the measured HBM copy bandwidth.
+
+Reference arm (--impl reference).  The reference's CPU algorithm (the
+oracle restatement of COCR_FP, all host threads) on a bounded sample of the
+same workload: preconditioner set-up plus a fixed number of iterations,
+extrapolated to the reference's own iteration count for the system (pinned
+by running the reference programs, tests/golden/c2_summary.json).
+
+Multi-GPU: systems are independent (replicas over the survey's systems);
+every rank solves its own copy of the workload and `value` is the
+whole-job seconds per solve (total time / total solves).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time/solve to rel-res 1e-8: batched mixed vs plain FP64 GPU; SpMV HBM GB/s"
+UNIT = "s/solve"
+WORKLOAD = "c2"
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ref_iterations():
+    """The reference's own iteration counts for the workload's systems, or
+    None when they have not been pinned."""
+    p = os.path.join(ROOT, "tests", "golden", "c2_summary.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return {(s["nu"], s["alfa"]): s["iterations"] for s in d["systems"]}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [t.strip() for t in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": smax or None, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_inputs(w):
+    from mtcalc_with_dfp_cocr_gb300 import normal1d
+    tops = [l.top for l in w.mesh.layers]
+    sig = [l.sigma for l in w.mesh.layers]
+    tables = {}
+    for nu in sorted(set(f for f, _ in w.systems)):
+        tables[nu] = normal1d.solve_1d(nu, tops, sig)
+    return tables
+
+
+# ------------------------------------------------------------------- GPU arm
+def gpu_arm(args):
+    import torch
+    world, rank, local = dist_init()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from mtcalc_with_dfp_cocr_gb300 import _lib, assembly, slae_io, solver, workloads
+    from mtcalc_with_dfp_cocr_gb300 import build as B
+    B.build()
+
+    w = workloads.make(WORKLOAD)
+    systems = w.systems
+    S = len(systems)
+    tables = make_inputs(w)
+    nb = w.mesh.nb
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    A = assembly.Assembly(w.mesh)
+    z1d = tables[systems[0][0]][0]
+    rhs = torch.empty(S, 2 * nb, dtype=torch.float64, device="cuda")
+    A.rhs([f for f, _ in systems], [a for _, a in systems], z1d,
+          np.stack([tables[f][1] for f, _ in systems]),
+          np.stack([tables[f][2] for f, _ in systems]), rhs)
+    x = torch.zeros_like(rhs)
+    freqs = sorted(set(f for f, _ in systems))
+    eps, maxiter = 1e-8, 20000
+    iters = {}
+
+    def step():
+        for nu in freqs:
+            ctx = A.cocr(nu, stream)
+            for k, (f, a) in enumerate(systems):
+                if f != nu:
+                    continue
+                x[k].zero_()
+                code, st = ctx.solve(rhs[k], x[k], eps=eps, maxiter=maxiter,
+                                     stop_on_true_residual=True)
+                if code != 0:
+                    raise RuntimeError(f"solve failed with code {code}")
+                iters[(f, a)] = (st.iterations, st.true_residual_rel)
+            ctx.close()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    launches0 = _lib.kernel_launches()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        barrier()
+    ms = ev0.elapsed_time(ev1)
+    launches = _lib.kernel_launches() - launches0
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = (ms / 1e3) / (args.steps * S * world)
+
+    # ---- roofline of the SpMV kernel
+    ctx = A.cocr(freqs[0], stream)
+    nc, nr, m = ctx.info()
+    xs = torch.randn(2 * nb, dtype=torch.float64, device="cuda")
+    ys = torch.empty_like(xs)
+    ctx.spmv_timed(xs, ys, 5)
+    reps = 50
+    spmv_ms = ctx.spmv_timed(xs, ys, reps) / reps
+    ctx.close()
+    nslices = (nb + 31) // 32
+    spmv_bytes = nc * (16 + 4) + nr * (8 + 4) + 16 * nb + 16 * nb + nslices * (8 + 8 + 4 + 4)
+    peak, peak_kind = load_peaks()
+    achieved = spmv_bytes / (spmv_ms * 1e-3) / 1e9
+
+    # ---- e2e through the reference-facing C ABI with host buffers
+    mesh_h = slae_io.mesh_to_solve_mesh(w.mesh)
+    host = {}
+    for k, (f, a) in enumerate(systems):
+        t = tables[f]
+        host[k] = A.block2x2(f, a, t[0], t[1], t[2], eps=eps, maxiter=maxiter)
+    h2d = d2h = 0
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        for k in range(S):
+            s = host[k]
+            code, xh, st = solver.pcocr_2x2_folded(s, mesh_h, stop_on_true_residual=True)
+            if code != 0:
+                raise RuntimeError(f"e2e solve failed with code {code}")
+            h2d += (s.ig.nbytes + s.jg.nbytes + s.idi.nbytes + s.ijg.nbytes + s.di.nbytes +
+                    s.gg.nbytes + s.pr.nbytes + xh.nbytes)
+            d2h += xh.nbytes
+    e2e_s = (time.perf_counter() - t0) / (e2e_steps * S)
+    A.close()
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 (complex128)",
+        "data": "synthetic (seeded layered earth + 20 random blocks, reference file formats)",
+        "config": {"workload": "c2: 96x96x64 cells, 1,812,736 edges, 0.1 Hz x 2 polarisations, "
+                               "plain FP64 COCR + folded preconditioner, stop: reference MRS "
+                               "rule and true rel-res < 1e-8",
+                   "systems_per_step": S, "nb": nb, "l2_flush": "none: matrix 0.9 GB > L2",
+                   "iterations": {f"{f}Hz/{'XY'[1 - a]}": v[0] for (f, a), v in iters.items()},
+                   "true_rel_res": {f"{f}Hz/{'XY'[1 - a]}": v[1] for (f, a), v in iters.items()},
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": "k_spmv (SELL-32 FP64 complex SpMV)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": f"{peak_kind} hbm_gbs",
+                     "bytes_per_launch": spmv_bytes, "ms_per_launch": spmv_ms,
+                     "traffic": None},
+        "e2e": {"value": e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d // e2e_steps,
+                "d2h_bytes_per_step": d2h // e2e_steps},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_sample(host[0], mesh_h, systems[0],
+                                         fallback_iterations=iters[systems[0]][0])
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+# --------------------------------------------------------------- CPU baseline
+def cpu_sample(slae, mesh, key, target_seconds=12.0, fallback_iterations=None):
+    """The oracle restatement of COCR_FP with all host threads: set-up plus
+    a bounded number of iterations, extrapolated to the reference's
+    iteration count for this system."""
+    from oracle import pyoracle as O
+    cores = os.cpu_count() or 1
+    _, _, s1 = O.pcocr(slae, mesh, nthreads=cores, iter_limit=3)
+    per_guess = max(s1.seconds / 6.0, 1e-3)
+    n2 = int(min(2000, max(20, target_seconds / per_guess)))
+    _, _, s2 = O.pcocr(slae, mesh, nthreads=cores, iter_limit=n2)
+    per_iter = (s2.seconds - s1.seconds) / (n2 - 3)
+    setup = max(0.0, s1.seconds - 3 * per_iter)
+    pinned = ref_iterations()
+    n_ref = pinned[key] if pinned else fallback_iterations
+    return {"value": setup + per_iter * n_ref, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"oracle COCR_FP restatement, {cores} threads: set-up + {n2} iterations "
+                      f"on the {key[0]} Hz / {'XY'[1 - key[1]]} system "
+                      f"({s2.seconds:.1f} s), extrapolated to " +
+                      (f"the reference's {n_ref} iterations" if pinned else
+                       f"{n_ref} iterations (the GPU solve's count; reference count not pinned)"),
+            "seconds_per_iteration": per_iter, "setup_seconds": setup}
+
+
+def reference_arm(args):
+    world, rank, local = dist_init()
+    if rank != 0:
+        return
+    from mtcalc_with_dfp_cocr_gb300 import slae_io, workloads
+    from oracle import pyoracle as O
+    w = workloads.make(WORKLOAD)
+    tables = make_inputs(w)
+    nu, alfa = w.systems[0]
+    t = tables[nu]
+    slae = O.assemble(w.mesh, nu, alfa, t[0], t[1], t[2], eps=1e-8, maxiter=20000)
+    mesh = slae_io.mesh_to_solve_mesh(w.mesh)
+    vals, base = [], None
+    for i in range(args.warmup + args.steps):
+        b = cpu_sample(slae, mesh, (nu, alfa), target_seconds=6.0)
+        if i >= args.warmup:
+            vals.append(b["value"])
+            base = b
+    v = statistics.median(vals)
+    base["value"] = v
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64 (complex128)",
+           "data": "synthetic (seeded layered earth + 20 random blocks)",
+           "config": {"workload": "c2: 96x96x64 cells, 1,812,736 edges, 0.1 Hz, COCR_FP "
+                                  "algorithm on the host cores"},
+           "impl": "reference", "cpu_baseline": base,
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def profile_run(args):
+    """A short fixed run for ncu: the device assembly, one COCR context,
+    10 SpMV launches and 30 COCR iterations (ends with the iteration-limit
+    code, which is expected here)."""
+    import torch
+    from mtcalc_with_dfp_cocr_gb300 import assembly, workloads
+    from mtcalc_with_dfp_cocr_gb300 import build as B
+    B.build()
+    torch.cuda.set_device(0)
+    w = workloads.make(args.workload)
+    tables = make_inputs(w)
+    nu, alfa = w.systems[0]
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    A = assembly.Assembly(w.mesh)
+    rhs = torch.empty(1, 2 * w.mesh.nb, dtype=torch.float64, device="cuda")
+    t = tables[nu]
+    A.rhs([nu], [alfa], t[0], t[1][None], t[2][None], rhs)
+    ctx = A.cocr(nu, stream)
+    xs = torch.randn(2 * w.mesh.nb, dtype=torch.float64, device="cuda")
+    ys = torch.empty_like(xs)
+    ms = ctx.spmv_timed(xs, ys, 10)
+    x = torch.zeros_like(rhs[0])
+    code, st = ctx.solve(rhs[0], x, eps=1e-8, maxiter=30)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": args.workload, "spmv_ms": ms / 10, "code": code,
+                      "iterations": st.iterations}))
+    ctx.close()
+    A.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="short fixed run for ncu captures (see profile_run)")
+    ap.add_argument("--workload", default=None, help="workload of --profile (default c3)")
+    args = ap.parse_args()
+    if args.profile:
+        args.workload = args.workload or "c3"
+        profile_run(args)
+        return
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

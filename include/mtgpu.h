@@ -131,12 +131,73 @@ int mtgpu_cocr_solve(mtgpu_cocr *ctx, const double *d_b, double *d_x, double eps
 int mtgpu_cocr_spmv(mtgpu_cocr *ctx, const double *d_x, double *d_y);
 int mtgpu_cocr_precond(mtgpu_cocr *ctx, const double *d_x, double *d_y);
 
+/* Time `reps` back-to-back SpMV launches y = A x on the context's stream
+ * with CUDA events; *ms receives the total device time.  For measurement. */
+int mtgpu_cocr_spmv_timed(mtgpu_cocr *ctx, const double *d_x, double *d_y, int reps, float *ms);
+
 /* Sizes of the device matrix: stored complex and real entries (without
  * padding) and the number of preconditioner nodes m. */
 int mtgpu_cocr_info(const mtgpu_cocr *ctx, long long *nnz_complex, long long *nnz_real,
                     int *m_nodes);
 
 void mtgpu_cocr_destroy(mtgpu_cocr *ctx);
+
+/* ------------------------------------------------------------------------
+ * Device assembly: replaces BuildMatrix (Code/BuildMatrix/HarmVect3d.cpp:74-138:
+ * T_Portrait::Gen_Portrait/Gen_idi_ijg, VecBlockSLAE::AsmBlockSLAE,
+ * Bound_cond_vec_harm::SetHomogenDirichletCond).  The matrix is held on the
+ * GPU in the frequency-independent form A(omega) = K + i omega M (K = sum
+ * B/mu, M = sum sigma C over the cells, Dirichlet rows/columns applied), so
+ * one assembly serves every frequency and polarisation of a survey.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+    int kuzlov, kpar, nb, n_materials;
+    const double *xyz;        /* [kuzlov][3]                                   */
+    const int *nver;          /* [kpar][nver_stride], 8 nodes used (0-based)   */
+    int nver_stride;          /* 14 in nver.dat                                */
+    const int *ed;            /* [kpar][ed_stride], 12 edges used (0-based)    */
+    int ed_stride;            /* 25 in edges.dat                               */
+    const int *edges;         /* [nb][2] node pairs (0-based)                  */
+    const int *nvkat;         /* [kpar] material (0-based)                     */
+    const double *mu;         /* [n_materials] mu3d * MU_0                     */
+    const double *mu0;        /* may be NULL; must equal mu                    */
+    const double *sigma;      /* [n_materials] sigma3d                         */
+    const double *sigma0;     /* [n_materials] normal-field conductivity       */
+    const double *dpr, *dpr0; /* may be NULL; must be 0 (no displacement term) */
+    int n_bound;              /* boundary nodes (l13d.dat, 0-based)            */
+    const int *bound_nodes;
+} mtgpu_fem_mesh;
+
+typedef struct mtgpu_assembly_s mtgpu_assembly;
+
+int mtgpu_assembly_create(const mtgpu_fem_mesh *mesh, mtgpu_assembly **out);
+
+/* Sizes of the assembled system: full-storage complex/real entries, and the
+ * lower-triangle block format (nnz_lower = ig[nb], gg_len = ijg[nnz_lower]). */
+int mtgpu_assembly_info(const mtgpu_assembly *a, long long *nnz_complex, long long *nnz_real,
+                        int *nnz_lower, long long *gg_len);
+
+/* The SLAE of one frequency nu [Hz] and polarisation alfa (1: x, 0: y) in the
+ * reference's 0-based lower-triangle block format, into host arrays sized by
+ * mtgpu_assembly_info: ig[nb+1], jg[nnz_lower], idi[nb+1], ijg[nnz_lower+1],
+ * di[2 nb], gg[gg_len], pr[2 nb].  z1d/usin/ucos: the 1-D normal field table
+ * (Harm1D's usin.dat/ucos.dat) of that frequency. */
+int mtgpu_assembly_block2x2(mtgpu_assembly *a, double nu, int alfa, int n1d, const double *z1d,
+                            const double *usin, const double *ucos, int *ig, int *jg, int *idi,
+                            int *ijg, double *di, double *gg, double *pr);
+
+/* Right-hand sides of S systems into device memory d_rhs[S][2 nb]
+ * (re/im interleaved).  usin/ucos: host [S][n1d] tables on the shared z1d. */
+int mtgpu_assembly_rhs(mtgpu_assembly *a, int S, const double *nu, const int *alfa, int n1d,
+                       const double *z1d, const double *usin, const double *ucos,
+                       double *d_rhs);
+
+/* COCR context for A(2 pi nu) built from the device assembly: no matrix
+ * crosses PCIe.  stream: a cudaStream_t or NULL. */
+int mtgpu_cocr_create_from_assembly(mtgpu_assembly *a, double nu, void *stream,
+                                    mtgpu_cocr **out);
+
+void mtgpu_assembly_destroy(mtgpu_assembly *a);
 
 #ifdef __cplusplus
 }
@@ -150,6 +211,7 @@ typedef struct {
     const int *edges2, *ig_t, *jg_t;
     const double *gg_t;
     const int *is_node_bound;
+    int nver_stride;          /* 14 for the reference arrays */
 } mtgpu_mesh_desc;
 
 #endif

@@ -39,6 +39,15 @@ class SolveOpts(C.Structure):
     _fields_ = [("stop_on_true_residual", C.c_int), ("iterations_per_launch", C.c_int)]
 
 
+class FemMesh(C.Structure):
+    _fields_ = [("kuzlov", C.c_int), ("kpar", C.c_int), ("nb", C.c_int), ("n_materials", C.c_int),
+                ("xyz", C.c_void_p), ("nver", C.c_void_p), ("nver_stride", C.c_int),
+                ("ed", C.c_void_p), ("ed_stride", C.c_int), ("edges", C.c_void_p),
+                ("nvkat", C.c_void_p), ("mu", C.c_void_p), ("mu0", C.c_void_p),
+                ("sigma", C.c_void_p), ("sigma0", C.c_void_p), ("dpr", C.c_void_p),
+                ("dpr0", C.c_void_p), ("n_bound", C.c_int), ("bound_nodes", C.c_void_p)]
+
+
 class MtgpuError(RuntimeError):
     pass
 
@@ -64,10 +73,19 @@ SIGNATURES = {
     "mtgpu_cocr_solve": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int,
                                    C.POINTER(SolveOpts), C.POINTER(SolveStats)]),
     "mtgpu_cocr_spmv": (C.c_int, [_vp, _vp, _vp]),
+    "mtgpu_cocr_spmv_timed": (C.c_int, [_vp, _vp, _vp, C.c_int, C.POINTER(C.c_float)]),
     "mtgpu_cocr_precond": (C.c_int, [_vp, _vp, _vp]),
     "mtgpu_cocr_info": (C.c_int, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
                                   C.POINTER(C.c_int)]),
     "mtgpu_cocr_destroy": (None, [_vp]),
+    "mtgpu_assembly_create": (C.c_int, [C.POINTER(FemMesh), C.POINTER(_vp)]),
+    "mtgpu_assembly_info": (C.c_int, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
+                                      C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),
+    "mtgpu_assembly_block2x2": (C.c_int, [_vp, C.c_double, C.c_int, C.c_int, _d, _d, _d,
+                                          _i, _i, _i, _i, _d, _d, _d]),
+    "mtgpu_assembly_rhs": (C.c_int, [_vp, C.c_int, _d, _i, C.c_int, _d, _d, _d, _vp]),
+    "mtgpu_cocr_create_from_assembly": (C.c_int, [_vp, C.c_double, _vp, C.POINTER(_vp)]),
+    "mtgpu_assembly_destroy": (None, [_vp]),
 }
 
 _lib = None

@@ -1,0 +1,48 @@
+// Device assembly: parametric matrix A(omega) = K + i omega M on a SELL-32
+// pattern, per-system right-hand sides, and conversion to the reference's
+// lower-triangle block format.
+#pragma once
+#include "mtgpu_internal.cuh"
+
+namespace mtgpu {
+
+struct ParamMatrix {
+    int nb = 0, kpar = 0, kuzlov = 0, n_materials = 0;
+    int ed_stride = 12, nver_stride = 8;
+    int nslices = 0;
+    long long nnz_c = 0, nnz_r = 0, len_c = 0, len_r = 0;
+    // pattern (same layout as SellMatrix)
+    int *d_wc = nullptr, *d_wr = nullptr;
+    long long *d_pc = nullptr, *d_pr = nullptr;
+    int *d_nc = nullptr, *d_nr = nullptr;
+    int *d_col_c = nullptr, *d_col_r = nullptr;
+    // values: K on complex and real slots, M on complex slots
+    double *d_kc = nullptr, *d_mc = nullptr, *d_kr = nullptr;
+    // mesh on the device
+    int *d_ec_ptr = nullptr, *d_ec_cell = nullptr;    // edge -> (cell << 4 | local edge)
+    double *d_xyz = nullptr;
+    int *d_nver = nullptr, *d_ed = nullptr, *d_edges = nullptr, *d_nvkat = nullptr;
+    double *d_mu = nullptr, *d_sig = nullptr, *d_sig0 = nullptr;
+    unsigned char *d_bedge = nullptr;                  // Dirichlet edges
+    void release();
+};
+
+struct Block2x2Dev {
+    int nb = 0, nnz = 0;
+    long long gg_len = 0;
+    int *ig = nullptr, *jg = nullptr, *idi = nullptr, *ijg = nullptr;
+    double *di = nullptr, *gg = nullptr;
+    void release();
+};
+
+int param_assemble(const mtgpu_fem_mesh &m, ParamMatrix &P, cudaStream_t st);
+// rhs[k] for S systems (omega, alfa, 1-D tables usin/ucos [S][n1d] on z1d);
+// layout: interleaved ? rhs[e * S + k] : rhs[k * rhs_stride + e]
+int param_rhs(const ParamMatrix &P, int S, const double *d_omega, const int *d_alfa, int n1d,
+              const double *d_z1d, const double *d_usin, const double *d_ucos, double2 *d_rhs,
+              long long rhs_stride, int interleaved, cudaStream_t st);
+int param_to_sell(const ParamMatrix &P, double omega, SellMatrix &A, cudaStream_t st);
+int param_to_block2x2(const ParamMatrix &P, double omega, Block2x2Dev &B, cudaStream_t st);
+int exclusive_scan_host(const int *d_in, int n, int *d_out, long long *total, cudaStream_t st);
+
+}  // namespace mtgpu

@@ -30,22 +30,20 @@ void set_last_message(const char *msg)
 
 void note_launches(unsigned long long k) { g_launches += k; }
 
-}  // namespace mtgpu
-
-using namespace mtgpu;
-
-struct mtgpu_cocr_s {
-    CocrSolver S;
-    bool own_stream = false;
-};
-
-namespace {
-
-double now_s()
+double now_seconds()
 {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
         .count();
 }
+
+}  // namespace mtgpu
+
+using namespace mtgpu;
+
+
+namespace {
+
+double now_s() { return now_seconds(); }
 
 template <class T>
 int upload(T **d, const T *h, size_t count, cudaStream_t st)
@@ -109,11 +107,13 @@ int validate_mesh(const mtgpu_mesh_desc &m)
                                                   "edge node beyond n_nodes_c without T-matrix");
         }
     for (int c = 0; c < m.kpar; c++)
-        for (int j = 0; j < 8; j++) MTGPU_CHECK_ARG(m.nver14[(size_t)c * 14 + j] >= 0, "bad nver");
+        for (int j = 0; j < 8; j++) MTGPU_CHECK_ARG(m.nver14[(size_t)c * m.nver_stride + j] >= 0, "bad nver");
     return MTGPU_OK;
 }
 
-int make_stream(mtgpu_cocr_s *c, void *stream)
+}  // namespace
+
+int mtgpu::make_stream(mtgpu_cocr_s *c, void *stream)
 {
     if (stream) {
         c->S.st = (cudaStream_t)stream;
@@ -124,8 +124,6 @@ int make_stream(mtgpu_cocr_s *c, void *stream)
     }
     return MTGPU_OK;
 }
-
-}  // namespace
 
 extern "C" {
 
@@ -155,7 +153,7 @@ int mtgpu_cocr_create(int nb, int nnz_lower, const int *ig, const int *jg, const
         nnz_lower = ig[nb];
     }
     mtgpu_mesh_desc mesh{kpar, nb, n_nodes_c, nvkat, nver14, sigma3d, edges2, ig_t, jg_t,
-                         gg_t, is_node_bound};
+                         gg_t, is_node_bound, 14};
     int rc = validate_mesh(mesh);
     if (rc) return rc;
     auto *c = new mtgpu_cocr_s();
@@ -229,6 +227,26 @@ int mtgpu_cocr_spmv(mtgpu_cocr *c, const double *d_x, double *d_y)
     note_launches(1);
     MTGPU_TRY(cudaGetLastError());
     MTGPU_TRY(cudaStreamSynchronize(c->S.st));
+    return MTGPU_OK;
+}
+
+int mtgpu_cocr_spmv_timed(mtgpu_cocr *c, const double *d_x, double *d_y, int reps, float *ms)
+{
+    MTGPU_CHECK_ARG(c && d_x && d_y && ms && reps > 0, "bad argument");
+    MTGPU_TRY(cudaStreamSynchronize(cudaStreamLegacy));
+    cudaEvent_t e0, e1;
+    MTGPU_TRY(cudaEventCreate(&e0));
+    MTGPU_TRY(cudaEventCreate(&e1));
+    MTGPU_TRY(cudaEventRecord(e0, c->S.st));
+    for (int k = 0; k < reps; k++)
+        sell_spmv(c->S.A, (const double2 *)d_x, (double2 *)d_y, c->S.st);
+    note_launches((unsigned long long)reps);
+    MTGPU_TRY(cudaEventRecord(e1, c->S.st));
+    MTGPU_TRY(cudaEventSynchronize(e1));
+    MTGPU_TRY(cudaEventElapsedTime(ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    MTGPU_TRY(cudaGetLastError());
     return MTGPU_OK;
 }
 

@@ -1,0 +1,178 @@
+// extern "C" entry points of the device assembly (include/mtgpu.h).
+#include "assemble.cuh"
+
+#include <cmath>
+
+using namespace mtgpu;
+
+struct mtgpu_assembly_s {
+    ParamMatrix P;
+    cudaStream_t st = nullptr;
+    // host copies of what the folded preconditioner set-up reads
+    std::vector<int> nver, nvkat, edges, bound;
+    std::vector<double> sigflag;
+    std::vector<int> ig_t;
+    int nver_stride = 14;
+};
+
+namespace {
+constexpr double kTwoPi = 2.0 * 3.1415926535897932384626433832795;   // BuildMatrix/stdafx.h:32
+
+template <class T>
+int upload_vec(T **d, const T *h, size_t n, cudaStream_t st)
+{
+    int rc = dev_alloc(d, n);
+    if (rc) return rc;
+    if (n) MTGPU_TRY(cudaMemcpyAsync(*d, h, n * sizeof(T), cudaMemcpyHostToDevice, st));
+    return MTGPU_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int mtgpu_assembly_create(const mtgpu_fem_mesh *mesh, mtgpu_assembly **out)
+{
+    MTGPU_CHECK_ARG(mesh && out, "null argument");
+    *out = nullptr;
+    auto *a = new mtgpu_assembly_s();
+    cudaError_t e = cudaStreamCreateWithFlags(&a->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete a;
+        set_last_error(e, "cudaStreamCreateWithFlags", __FILE__, __LINE__);
+        return MTGPU_ERR_CUDA;
+    }
+    int rc = param_assemble(*mesh, a->P, a->st);
+    if (rc) {
+        mtgpu_assembly_destroy(a);
+        return rc;
+    }
+    const mtgpu_fem_mesh &m = *mesh;
+    a->nver_stride = m.nver_stride;
+    a->nver.assign(m.nver, m.nver + (size_t)m.kpar * m.nver_stride);
+    a->nvkat.assign(m.nvkat, m.nvkat + m.kpar);
+    a->edges.assign(m.edges, m.edges + (size_t)2 * m.nb);
+    a->bound.assign(m.kuzlov, 0);
+    for (int i = 0; i < m.n_bound; i++) a->bound[m.bound_nodes[i]] = 1;
+    a->sigflag.resize(m.n_materials);
+    for (int i = 0; i < m.n_materials; i++) a->sigflag[i] = m.sigma[i] == 0.0 ? 0.0 : 1.0;
+    a->ig_t.assign(m.kuzlov + 1, 0);
+    *out = a;
+    return MTGPU_OK;
+}
+
+void mtgpu_assembly_destroy(mtgpu_assembly *a)
+{
+    if (!a) return;
+    if (a->st) cudaStreamSynchronize(a->st);
+    a->P.release();
+    if (a->st) cudaStreamDestroy(a->st);
+    delete a;
+}
+
+int mtgpu_assembly_info(const mtgpu_assembly *a, long long *nnz_complex, long long *nnz_real,
+                        int *nnz_lower, long long *gg_len)
+{
+    MTGPU_CHECK_ARG(a != nullptr, "null assembly");
+    const ParamMatrix &P = a->P;
+    if (nnz_complex) *nnz_complex = P.nnz_c;
+    if (nnz_real) *nnz_real = P.nnz_r;
+    // the pattern is symmetric with every diagonal present
+    if (nnz_lower) *nnz_lower = (int)((P.nnz_c - P.nb) / 2 + P.nnz_r / 2);
+    if (gg_len) *gg_len = (P.nnz_c - P.nb) + P.nnz_r / 2;
+    return MTGPU_OK;
+}
+
+int mtgpu_assembly_rhs(mtgpu_assembly *a, int S, const double *nu, const int *alfa, int n1d,
+                       const double *z1d, const double *usin, const double *ucos, double *d_rhs)
+{
+    MTGPU_CHECK_ARG(a && nu && alfa && z1d && usin && ucos && d_rhs, "null argument");
+    MTGPU_CHECK_ARG(S > 0 && n1d >= 2, "bad sizes");
+    for (int i = 0; i + 1 < n1d; i++) MTGPU_CHECK_ARG(z1d[i] <= z1d[i + 1], "z1d must ascend");
+    std::vector<double> om(S);
+    for (int k = 0; k < S; k++) om[k] = kTwoPi * nu[k];
+    double *d_om = nullptr, *d_z = nullptr, *d_us = nullptr, *d_uc = nullptr;
+    int *d_al = nullptr;
+    int rc;
+    MTGPU_TRY(cudaStreamSynchronize(cudaStreamLegacy));
+    if (!(rc = upload_vec(&d_om, om.data(), S, a->st)) && !(rc = upload_vec(&d_al, alfa, S, a->st)) &&
+        !(rc = upload_vec(&d_z, z1d, n1d, a->st)) &&
+        !(rc = upload_vec(&d_us, usin, (size_t)S * n1d, a->st)) &&
+        !(rc = upload_vec(&d_uc, ucos, (size_t)S * n1d, a->st))) {
+        rc = param_rhs(a->P, S, d_om, d_al, n1d, d_z, d_us, d_uc, (double2 *)d_rhs, a->P.nb, 0, a->st);
+        cudaError_t e = cudaStreamSynchronize(a->st);
+        if (!rc && e != cudaSuccess) {
+            set_last_error(e, "mtgpu_assembly_rhs", __FILE__, __LINE__);
+            rc = MTGPU_ERR_CUDA;
+        }
+    }
+    dev_free(d_om); dev_free(d_al); dev_free(d_z); dev_free(d_us); dev_free(d_uc);
+    return rc;
+}
+
+int mtgpu_assembly_block2x2(mtgpu_assembly *a, double nu, int alfa, int n1d, const double *z1d,
+                            const double *usin, const double *ucos, int *ig, int *jg, int *idi,
+                            int *ijg, double *di, double *gg, double *pr)
+{
+    MTGPU_CHECK_ARG(a && ig && jg && idi && ijg && di && gg && pr, "null argument");
+    const int nb = a->P.nb;
+    Block2x2Dev B;
+    int rc = param_to_block2x2(a->P, kTwoPi * nu, B, a->st);
+    double *d_rhs = nullptr;
+    if (!rc) rc = dev_alloc(&d_rhs, (size_t)2 * nb);
+    if (!rc) rc = mtgpu_assembly_rhs(a, 1, &nu, &alfa, n1d, z1d, usin, ucos, d_rhs);
+    if (!rc) {
+        cudaError_t e = cudaSuccess;
+        auto cp = [&](void *dst, const void *src, size_t bytes) {
+            if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, a->st);
+        };
+        cp(ig, B.ig, sizeof(int) * (nb + 1));
+        cp(jg, B.jg, sizeof(int) * B.nnz);
+        cp(idi, B.idi, sizeof(int) * (nb + 1));
+        cp(ijg, B.ijg, sizeof(int) * (B.nnz + 1));
+        cp(di, B.di, sizeof(double) * 2 * nb);
+        cp(gg, B.gg, sizeof(double) * B.gg_len);
+        cp(pr, d_rhs, sizeof(double) * 2 * nb);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(a->st);
+        if (e != cudaSuccess) {
+            set_last_error(e, "mtgpu_assembly_block2x2", __FILE__, __LINE__);
+            rc = MTGPU_ERR_CUDA;
+        }
+    }
+    dev_free(d_rhs);
+    B.release();
+    return rc;
+}
+
+int mtgpu_cocr_create_from_assembly(mtgpu_assembly *a, double nu, void *stream, mtgpu_cocr **out)
+{
+    MTGPU_CHECK_ARG(a && out, "null argument");
+    *out = nullptr;
+    auto *c = new mtgpu_cocr_s();
+    int rc = make_stream(c, stream);
+    if (rc) {
+        delete c;
+        return rc;
+    }
+    CocrSolver &S = c->S;
+    S.nb = a->P.nb;
+    mtgpu_mesh_desc mesh{a->P.kpar, a->P.nb, a->P.kuzlov, a->nvkat.data(), a->nver.data(),
+                         a->sigflag.data(), a->edges.data(), a->ig_t.data(), a->ig_t.data(),
+                         nullptr, a->bound.data(), a->nver_stride};
+    if (!(rc = param_to_sell(a->P, kTwoPi * nu, S.A, S.st)) && !(rc = folded_build_g(mesh, S.P, S.st)) &&
+        !(rc = folded_build_diag(S.A, S.P, S.st)) && !(rc = cocr_alloc(S))) {
+        note_launches(2);
+        cudaError_t e = cudaStreamSynchronize(S.st);
+        if (e != cudaSuccess) {
+            set_last_error(e, "mtgpu_cocr_create_from_assembly", __FILE__, __LINE__);
+            rc = MTGPU_ERR_CUDA;
+        }
+    }
+    if (rc) {
+        mtgpu_cocr_destroy(c);
+        return rc;
+    }
+    *out = c;
+    return MTGPU_OK;
+}
+
+}  // extern "C"

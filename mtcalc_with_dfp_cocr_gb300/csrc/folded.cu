@@ -9,6 +9,8 @@
 // here serves the set-up stages and the stand-alone entry point.
 #include "mtgpu_internal.cuh"
 
+#include <climits>
+
 namespace mtgpu {
 
 void Folded::release()
@@ -28,7 +30,7 @@ int folded_build_g(const mtgpu_mesh_desc &mesh, Folded &P, cudaStream_t st)
     for (int c = 0; c < mesh.kpar; c++) {
         if (!(mesh.sigma3d[mesh.nvkat[c]] > 0.0)) continue;
         for (int j = 0; j < 8; j++) {
-            const int v = mesh.nver14[(size_t)c * 14 + j];
+            const int v = mesh.nver14[(size_t)c * mesh.nver_stride + j];
             if (v >= 0 && v < nn && !mesh.is_node_bound[v]) in_sigma[v] = 1;
         }
     }
@@ -113,11 +115,17 @@ __global__ void k_diag_a(int nb, const long long *pc, const int *col_c, const do
     da[i] = cdiv(make_double2(1.0, 0.0), d);
 }
 
-// D_S[v] = 1 / sum_{k,c in row v of G} g_k g_c A[k][c]
-__global__ void k_diag_s(int m, const int *gp, const int *gj, const double *gv, const int *wc,
-                         const int *wr, const long long *pc, const long long *pr,
-                         const int *col_c, const double2 *val_c, const int *col_r,
-                         const double *val_r, double2 *ds)
+// D_S[v] = 1 / sum_{k,c in row v of G} g_k g_c A[k][c].
+// Re diag(G A G^T) is a cancellation (the curl-curl part annihilates
+// gradients) and in the air it is not small next to the tiny imaginary
+// part, so D_S there depends on the summation order.  This kernel therefore
+// adds in the reference's order — row k of A by increasing column, complex
+// and real entries merged (FoldedPreconditioner.cpp:518-556 over the rows
+// of From2x2ToCSR2x2_2) — with unfused multiply and add.
+__global__ void k_diag_s(int m, const int *gp, const int *gj, const double *gv,
+                         const int *nc_row, const int *nr_row, const long long *pc,
+                         const long long *pr, const int *col_c, const double2 *val_c,
+                         const int *col_r, const double *val_r, double2 *ds)
 {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= m) return;
@@ -126,26 +134,32 @@ __global__ void k_diag_s(int m, const int *gp, const int *gj, const double *gv, 
     for (int j = b; j < e; j++) {
         const int k = gj[j];
         const double gk = gv[j];
-        const int s = k / kSlice;
+        const int nc = nc_row[k], nr = nr_row[k];
         double tr = 0.0, ti = 0.0;
-        for (int q = 0; q < wc[s]; q++) {
-            const long long t = slot(pc, k, q);
-            const int c = col_c[t];
+        int qc = 0, qr = 0;
+        while (qc < nc || qr < nr) {
+            const int cc = qc < nc ? col_c[slot(pc, k, qc)] : INT_MAX;
+            const int cr = qr < nr ? col_r[slot(pr, k, qr)] : INT_MAX;
+            double ar, ai;
+            int c;
+            if (cc < cr) {
+                const double2 a = val_c[slot(pc, k, qc++)];
+                ar = a.x;
+                ai = a.y;
+                c = cc;
+            } else {
+                ar = val_r[slot(pr, k, qr++)];
+                ai = 0.0;
+                c = cr;
+            }
             for (int u = b; u < e; u++)
                 if (gj[u] == c) {
-                    const double2 a = val_c[t];
-                    tr += a.x * gv[u];
-                    ti += a.y * gv[u];
+                    tr = __dadd_rn(tr, __dmul_rn(ar, gv[u]));
+                    ti = __dadd_rn(ti, __dmul_rn(ai, gv[u]));
                 }
         }
-        for (int q = 0; q < wr[s]; q++) {
-            const long long t = slot(pr, k, q);
-            const int c = col_r[t];
-            for (int u = b; u < e; u++)
-                if (gj[u] == c) tr += val_r[t] * gv[u];
-        }
-        sr += tr * gk;
-        si += ti * gk;
+        sr = __dadd_rn(sr, __dmul_rn(tr, gk));
+        si = __dadd_rn(si, __dmul_rn(ti, gk));
     }
     ds[v] = cdiv(make_double2(1.0, 0.0), make_double2(sr, si));
 }
@@ -188,7 +202,7 @@ int folded_build_diag(const SellMatrix &A, Folded &P, cudaStream_t st)
     k_diag_a<<<ceil_div(A.nb, kThreads), kThreads, 0, st>>>(A.nb, A.d_pc, A.d_col_c, A.d_val_c,
                                                             A.d_diag_slot, P.d_da);
     if (P.m > 0)
-        k_diag_s<<<ceil_div(P.m, 128), 128, 0, st>>>(P.m, P.d_gp, P.d_gj, P.d_gv, A.d_wc, A.d_wr,
+        k_diag_s<<<ceil_div(P.m, 128), 128, 0, st>>>(P.m, P.d_gp, P.d_gj, P.d_gv, A.d_nc, A.d_nr,
                                                      A.d_pc, A.d_pr, A.d_col_c, A.d_val_c,
                                                      A.d_col_r, A.d_val_r, P.d_ds);
     MTGPU_TRY(cudaGetLastError());

@@ -53,6 +53,7 @@ struct SellMatrix {
     double2 *d_val_c = nullptr;
     double *d_val_r = nullptr;
     int *d_diag_slot = nullptr;   // complex slot index of the diagonal, per row
+    int *d_nc = nullptr, *d_nr = nullptr;   // complex / real entries per row
     void release();
 };
 
@@ -144,4 +145,15 @@ void dev_free(T *&p)
     p = nullptr;
 }
 
+}  // namespace mtgpu
+
+// opaque handle of the C ABI
+struct mtgpu_cocr_s {
+    mtgpu::CocrSolver S;
+    bool own_stream = false;
+};
+
+namespace mtgpu {
+int make_stream(mtgpu_cocr_s *c, void *stream);
+double now_seconds();
 }  // namespace mtgpu

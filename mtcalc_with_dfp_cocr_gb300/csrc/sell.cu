@@ -17,7 +17,7 @@ void SellMatrix::release()
 {
     dev_free(d_wc); dev_free(d_wr); dev_free(d_pc); dev_free(d_pr);
     dev_free(d_col_c); dev_free(d_col_r); dev_free(d_val_c); dev_free(d_val_r);
-    dev_free(d_diag_slot);
+    dev_free(d_diag_slot); dev_free(d_nc); dev_free(d_nr);
     nb = nslices = 0;
 }
 
@@ -178,15 +178,16 @@ int sell_from_block2x2_device(int nb, const int *d_ig, const int *d_jg, const in
     A.release();
     A.nb = nb;
     A.nslices = ceil_div(nb, kSlice);
-    int *cnt_c = nullptr, *cnt_r = nullptr, *fill_c = nullptr, *fill_r = nullptr;
+    int *fill_c = nullptr, *fill_r = nullptr;
     unsigned long long *tot = nullptr;
     int rc;
-    if ((rc = dev_alloc(&cnt_c, nb)) || (rc = dev_alloc(&cnt_r, nb)) ||
+    if ((rc = dev_alloc(&A.d_nc, nb)) || (rc = dev_alloc(&A.d_nr, nb)) ||
         (rc = dev_alloc(&fill_c, nb)) || (rc = dev_alloc(&fill_r, nb)) ||
         (rc = dev_alloc(&tot, 2)) || (rc = dev_alloc(&A.d_wc, A.nslices)) ||
         (rc = dev_alloc(&A.d_wr, A.nslices)) || (rc = dev_alloc(&A.d_pc, A.nslices + 1)) ||
         (rc = dev_alloc(&A.d_pr, A.nslices + 1)) || (rc = dev_alloc(&A.d_diag_slot, nb)))
         return rc;
+    int *cnt_c = A.d_nc, *cnt_r = A.d_nr;
     MTGPU_TRY(cudaMemsetAsync(cnt_c, 0, sizeof(int) * nb, st));
     MTGPU_TRY(cudaMemsetAsync(cnt_r, 0, sizeof(int) * nb, st));
     MTGPU_TRY(cudaMemsetAsync(fill_c, 0, sizeof(int) * nb, st));
@@ -231,7 +232,7 @@ int sell_from_block2x2_device(int nb, const int *d_ig, const int *d_jg, const in
                                                         A.d_val_r, A.d_diag_slot);
     MTGPU_TRY(cudaGetLastError());
     MTGPU_TRY(cudaStreamSynchronize(st));
-    dev_free(cnt_c); dev_free(cnt_r); dev_free(fill_c); dev_free(fill_r); dev_free(tot);
+    dev_free(fill_c); dev_free(fill_r); dev_free(tot);
     return MTGPU_OK;
 }
 

@@ -91,9 +91,13 @@ class CocrContext:
     ig, jg, idi, ijg (int32) and di, gg (float64) holding the same 0-based
     lower storage (device-resident input)."""
 
-    def __init__(self, slae, mesh: SolveMesh, nb: int | None = None):
+    def __init__(self, slae=None, mesh: SolveMesh | None = None, nb: int | None = None,
+                 handle=None):
         L = _lib.lib()
         self._keep = []
+        if handle is not None:          # built elsewhere (e.g. from a device assembly)
+            self._h, self.nb = handle, int(nb)
+            return
         h = C.c_void_p()
         if isinstance(slae, BlockSLAE):
             self.nb = slae.nb
@@ -146,6 +150,14 @@ class CocrContext:
     def spmv(self, x, y):
         _lib.check(_lib.lib().mtgpu_cocr_spmv(self._h, C.c_void_p(x.data_ptr()),
                                               C.c_void_p(y.data_ptr())), "mtgpu_cocr_spmv")
+
+    def spmv_timed(self, x, y, reps):
+        """Device milliseconds of `reps` back-to-back SpMV launches."""
+        ms = C.c_float()
+        _lib.check(_lib.lib().mtgpu_cocr_spmv_timed(self._h, C.c_void_p(x.data_ptr()),
+                                                    C.c_void_p(y.data_ptr()), int(reps),
+                                                    C.byref(ms)), "mtgpu_cocr_spmv_timed")
+        return ms.value
 
     def precond(self, x, y):
         _lib.check(_lib.lib().mtgpu_cocr_precond(self._h, C.c_void_p(x.data_ptr()),
