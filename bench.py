@@ -1,19 +1,24 @@
 """Benchmark: time per solve to true relative residual 1e-8 on the
-96x96x64-cell survey mesh (1.8M edges, 0.1 Hz, both polarisations).
+96x96x64-cell survey mesh (1.8M edges, 0.1 Hz, both polarisations):
+the batched double-float solver, with the plain FP64 GPU COCR beside it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
 
-GPU arm (default).  A step solves every system of the workload on the GPU
-from the device-resident assembly: per frequency the COCR context is built on
-the device (A = K + i omega M, folded preconditioner set-up), then each
-polarisation is solved with the reference's stop rule and, in addition, until
-the true residual ||b - A x|| / ||b|| < 1e-8.  `value` is seconds per solve
-(lower is better) from CUDA events on the solver's stream; the matrix
-(~0.9 GB) is larger than L2, so no flush is needed between iterations.
-`e2e` is the same metric through the reference-facing C ABI
-(mtgpu_pcocr_2x2_folded_ex) with the SLAE in host memory: upload, set-up,
-solve and download of x every step.  `roofline` is the SpMV kernel
-(the dominant kernel) against the measured HBM copy bandwidth.
+GPU arm (default).  A step solves every system of the workload together
+from the device-resident assembly with the batched survey solver (set-up of
+the batch included): the reference's COCR with the folded preconditioner and
+MRS stop rule, in double-float arithmetic (FP32 pairs, 48-bit significand)
+on the FP32 pipes, which GB300 runs at 64x its FP64 rate; each system also
+continues until its true residual ||b - A x|| / ||b|| is below 1e-8.
+(Plain FP32 iterations do not converge on these systems: the air layer
+leaves the curl-curl null space regularised below FP32 resolution.)  `value` is seconds
+per solve (lower is better) from CUDA events on the solver's stream; the
+matrix is larger than L2, so no flush is needed between iterations.
+`plain_fp64` times the reference's FP64 algorithm on the GPU on the same
+systems.  `e2e` goes through the reference-facing C ABI
+(mtgpu_pcocr_2x2_folded_ex, double-float) with the SLAE in host memory:
+upload, set-up, solve and download of x every solve.  `roofline` is the
+batched FP32 SpMV against the measured HBM copy bandwidth.
 
 Reference arm (--impl reference).  The reference's CPU algorithm (the
 oracle restatement of COCR_FP, all host threads) on a bounded sample of the
@@ -145,7 +150,7 @@ def gpu_arm(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
-    from mtcalc_with_dfp_cocr_gb300 import _lib, assembly, slae_io, solver, workloads
+    from mtcalc_with_dfp_cocr_gb300 import _lib, assembly, slae_io, solver, survey, workloads
     from mtcalc_with_dfp_cocr_gb300 import build as B
     B.build()
 
@@ -154,21 +159,29 @@ def gpu_arm(args):
     S = len(systems)
     tables = make_inputs(w)
     nb = w.mesh.nb
+    nus = [f for f, _ in systems]
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     A = assembly.Assembly(w.mesh)
     z1d = tables[systems[0][0]][0]
     rhs = torch.empty(S, 2 * nb, dtype=torch.float64, device="cuda")
-    A.rhs([f for f, _ in systems], [a for _, a in systems], z1d,
-          np.stack([tables[f][1] for f, _ in systems]),
-          np.stack([tables[f][2] for f, _ in systems]), rhs)
+    A.rhs(nus, [a for _, a in systems], z1d, np.stack([tables[f][1] for f in nus]),
+          np.stack([tables[f][2] for f in nus]), rhs)
     x = torch.zeros_like(rhs)
-    freqs = sorted(set(f for f, _ in systems))
     eps, maxiter = 1e-8, 20000
-    iters = {}
+    info = {}
 
-    def step():
-        for nu in freqs:
+    def step_batched():
+        sv = survey.Survey(A, nus, stream)
+        x.zero_()
+        code, st = sv.solve(rhs, x, eps=eps, maxiter=maxiter, verify=True)
+        if code != 0:
+            raise RuntimeError(f"survey solve failed: {st}")
+        info["batched"] = st
+        sv.close()
+
+    def step_plain():
+        for nu in sorted(set(nus)):
             ctx = A.cocr(nu, stream)
             for k, (f, a) in enumerate(systems):
                 if f != nu:
@@ -178,7 +191,7 @@ def gpu_arm(args):
                                      stop_on_true_residual=True)
                 if code != 0:
                     raise RuntimeError(f"solve failed with code {code}")
-                iters[(f, a)] = (st.iterations, st.true_residual_rel)
+                info.setdefault("plain", {})[(f, a)] = (st.iterations, st.true_residual_rel)
             ctx.close()
 
     def barrier():
@@ -186,54 +199,77 @@ def gpu_arm(args):
         if world > 1:
             torch.distributed.barrier()
 
-    for _ in range(args.warmup):
-        step()
-    barrier()
-    launches0 = _lib.kernel_launches()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
+    def timed(fn, steps):
+        barrier()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
-        for _ in range(args.steps):
-            step()
+        for _ in range(steps):
+            fn()
         ev1.record(stream)
         barrier()
-    ms = ev0.elapsed_time(ev1)
+        ms = ev0.elapsed_time(ev1)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    # headline: the batched double-float solver
+    for _ in range(args.warmup):
+        step_batched()
+    launches0 = _lib.kernel_launches()
+    with ClockSampler(local) as clk:
+        ms = timed(step_batched, args.steps)
     launches = _lib.kernel_launches() - launches0
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
     ms_per_step = ms / args.steps
     value = (ms / 1e3) / (args.steps * S * world)
+    batched = info["batched"]
 
-    # ---- roofline of the SpMV kernel
-    ctx = A.cocr(freqs[0], stream)
-    nc, nr, m = ctx.info()
+    # comparison: the plain FP64 COCR (the reference's algorithm) on the GPU
+    step_plain()
+    plain_steps = max(1, min(args.steps, 2))
+    ms_plain = timed(step_plain, plain_steps)
+    plain_value = (ms_plain / 1e3) / (plain_steps * S * world)
+
+    # roofline of the dominant kernel: the batched FP32 SpMV
+    peak, peak_kind = load_peaks()
+    sv = survey.Survey(A, nus, stream)
+    sv.spmv_timed(5)
+    reps = 50
+    spmv_ms = sv.spmv_timed(reps) / reps
+    sv.close()
+    inf = A.info()
+    nc, nr = inf["nnz_complex"], inf["nnz_real"]
+    nslices = (nb + 31) // 32
+    meta = nslices * (8 + 8 + 4 + 4)
+    spmv_bytes = nc * (4 + 8 + 8) + nr * (4 + 8) + meta + 2 * S * 16 * nb
+    achieved = spmv_bytes / (spmv_ms * 1e-3) / 1e9
+    # the FP64 SpMV of the plain path (bound by the FP64 pipe on GB300)
+    ctx = A.cocr(nus[0], stream)
     xs = torch.randn(2 * nb, dtype=torch.float64, device="cuda")
     ys = torch.empty_like(xs)
     ctx.spmv_timed(xs, ys, 5)
-    reps = 50
-    spmv_ms = ctx.spmv_timed(xs, ys, reps) / reps
+    spmv64_ms = ctx.spmv_timed(xs, ys, reps) / reps
     ctx.close()
-    nslices = (nb + 31) // 32
-    spmv_bytes = nc * (16 + 4) + nr * (8 + 4) + 16 * nb + 16 * nb + nslices * (8 + 8 + 4 + 4)
-    peak, peak_kind = load_peaks()
-    achieved = spmv_bytes / (spmv_ms * 1e-3) / 1e9
+    spmv64_bytes = nc * (16 + 4) + nr * (8 + 4) + meta + 2 * 16 * nb
+    achieved64 = spmv64_bytes / (spmv64_ms * 1e-3) / 1e9
 
-    # ---- e2e through the reference-facing C ABI with host buffers
+    # e2e through the reference-facing C ABI with host buffers
     mesh_h = slae_io.mesh_to_solve_mesh(w.mesh)
     host = {}
     for k, (f, a) in enumerate(systems):
         t = tables[f]
         host[k] = A.block2x2(f, a, t[0], t[1], t[2], eps=eps, maxiter=maxiter)
     h2d = d2h = 0
-    t0 = time.perf_counter()
     e2e_steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
     for _ in range(e2e_steps):
         for k in range(S):
             s = host[k]
-            code, xh, st = solver.pcocr_2x2_folded(s, mesh_h, stop_on_true_residual=True)
+            code, xh, st = solver.pcocr_2x2_folded(s, mesh_h, double_float=True,
+                                                   stop_on_true_residual=True)
             if code != 0:
                 raise RuntimeError(f"e2e solve failed with code {code}")
             h2d += (s.ig.nbytes + s.jg.nbytes + s.idi.nbytes + s.ijg.nbytes + s.di.nbytes +
@@ -242,31 +278,41 @@ def gpu_arm(args):
     e2e_s = (time.perf_counter() - t0) / (e2e_steps * S)
     A.close()
 
+    lab = lambda f, a: f"{f}Hz/{'XY'[1 - a]}"
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64 (complex128)",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "double-float (FP32 pairs, 48-bit significand) complex; FP64 scalars",
         "data": "synthetic (seeded layered earth + 20 random blocks, reference file formats)",
-        "config": {"workload": "c2: 96x96x64 cells, 1,812,736 edges, 0.1 Hz x 2 polarisations, "
-                               "plain FP64 COCR + folded preconditioner, stop: reference MRS "
-                               "rule and true rel-res < 1e-8",
-                   "systems_per_step": S, "nb": nb, "l2_flush": "none: matrix 0.9 GB > L2",
-                   "iterations": {f"{f}Hz/{'XY'[1 - a]}": v[0] for (f, a), v in iters.items()},
-                   "true_rel_res": {f"{f}Hz/{'XY'[1 - a]}": v[1] for (f, a), v in iters.items()},
+        "config": {"workload": "c2: 96x96x64 cells, 1,812,736 edges, 0.1 Hz x 2 polarisations; "
+                               "batched double-float COCR + folded preconditioner + MRS stop "
+                               "rule, every system also to true rel-res < 1e-8",
+                   "systems_per_step": S, "nb": nb, "l2_flush": "none: matrix > L2 (0.6 GB FP32)",
+                   "iterations": {lab(f, a): it for (f, a), it in zip(systems, batched["iterations"])},
+                   "true_rel_res": {lab(f, a): r for (f, a), r in zip(systems, batched["true_residual_rel"])},
                    "parallelism": f"replicas x{world}"},
-        "roofline": {"bound": "hbm", "kernel": "k_spmv (SELL-32 FP64 complex SpMV)",
+        "plain_fp64": {"value": plain_value, "unit": UNIT,
+                       "iterations": {lab(f, a): v[0] for (f, a), v in info["plain"].items()},
+                       "true_rel_res": {lab(f, a): v[1] for (f, a), v in info["plain"].items()},
+                       "speedup_of_batched_double_float": plain_value / value},
+        "roofline": {"bound": "hbm", "kernel": "k_spmv<SP> (batched double-float SELL-32 SpMV, S systems)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": f"{peak_kind} hbm_gbs",
-                     "bytes_per_launch": spmv_bytes, "ms_per_launch": spmv_ms,
-                     "traffic": None},
+                     "bytes_per_launch": spmv_bytes, "ms_per_launch": spmv_ms, "traffic": None},
+        "roofline_fp64_spmv": {"bound": "fp64 pipe (GB300 FP64 = FP32/64)",
+                               "achieved": achieved64, "peak": peak, "unit": "GB/s",
+                               "frac": achieved64 / peak, "bytes_per_launch": spmv64_bytes,
+                               "ms_per_launch": spmv64_ms},
         "e2e": {"value": e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d // e2e_steps,
-                "d2h_bytes_per_step": d2h // e2e_steps},
+                "d2h_bytes_per_step": d2h // e2e_steps,
+                "path": "mtgpu_pcocr_2x2_folded_ex(double_float=1, stop_on_true_residual=1), host SLAE buffers"},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_sample(host[0], mesh_h, systems[0],
-                                         fallback_iterations=iters[systems[0]][0])
+                                         fallback_iterations=info["plain"][systems[0]][0])
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -352,10 +398,20 @@ def profile_run(args):
     ms = ctx.spmv_timed(xs, ys, 10)
     x = torch.zeros_like(rhs[0])
     code, st = ctx.solve(rhs[0], x, eps=1e-8, maxiter=30)
-    torch.cuda.synchronize()
-    print(json.dumps({"profile": args.workload, "spmv_ms": ms / 10, "code": code,
-                      "iterations": st.iterations}))
     ctx.close()
+    # the batched double-float solver on two systems of the same frequency
+    from mtcalc_with_dfp_cocr_gb300 import survey
+    rhs2 = torch.empty(2, 2 * w.mesh.nb, dtype=torch.float64, device="cuda")
+    A.rhs([nu, nu], [1, 0], t[0], np.stack([t[1], t[1]]), np.stack([t[2], t[2]]), rhs2)
+    sv = survey.Survey(A, [nu, nu], stream)
+    ms2 = sv.spmv_timed(10)
+    x2 = torch.zeros_like(rhs2)
+    code2, st2 = sv.solve(rhs2, x2, eps=1e-8, maxiter=30, verify=False)
+    sv.close()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": args.workload, "spmv_fp64_ms": ms / 10, "code": code,
+                      "iterations": st.iterations, "spmv_batched_ms": ms2 / 10,
+                      "code_batched": code2}))
     A.close()
 
 

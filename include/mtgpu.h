@@ -73,6 +73,9 @@ typedef struct {
     int stop_on_true_residual;
     /* iterations per CUDA-graph launch between host status checks (0: 16) */
     int iterations_per_launch;
+    /* 1: run the same algorithm in double-float arithmetic on the FP32 pipes
+     * (the batched survey solver with one system); 0: FP64 arithmetic. */
+    int double_float;
 } mtgpu_solve_opts;
 
 /* Same as mtgpu_pcocr_2x2_folded with options and statistics and without
@@ -198,6 +201,45 @@ int mtgpu_cocr_create_from_assembly(mtgpu_assembly *a, double nu, void *stream,
                                     mtgpu_cocr **out);
 
 void mtgpu_assembly_destroy(mtgpu_assembly *a);
+
+/* ------------------------------------------------------------------------
+ * Batched survey solver: up to 32 systems (frequencies x polarisations,
+ * CalcStarter's loop in Code/CalcStarter/main.cpp:311-325) sharing one device
+ * assembly are solved together, one lane per system, with the reference's
+ * COCR + folded preconditioner + MRS stop test per system.  The arithmetic is
+ * double-float (pairs of FP32 numbers, 48-bit significand) on the FP32
+ * pipes, which GB300 runs at 64x its FP64 rate; the iteration follows the
+ * FP64 algorithm iteration for iteration.  No counterpart in the reference,
+ * which solves the systems one by one in FP64.
+ * ---------------------------------------------------------------------- */
+typedef struct mtgpu_survey_s mtgpu_survey;
+
+typedef struct {
+    int status[32];               /* MTGPU_OK / MTGPU_MAXITER / ... per system   */
+    int iterations[32];           /* the reference's iteration count per system */
+    int verifications[32];        /* true-residual evaluations per system       */
+    double true_residual_rel[32]; /* final ||b - A x|| / ||b|| per system        */
+    double seconds;               /* host wall time of the solve                 */
+} mtgpu_survey_stats;
+
+/* S systems with frequencies nu[S] [Hz] on assembly a; stream: a
+ * cudaStream_t or NULL. */
+int mtgpu_survey_create(mtgpu_assembly *a, int S, const double *nu, void *stream,
+                        mtgpu_survey **out);
+
+/* d_b: device [S][2 nb] right-hand sides (e.g. from mtgpu_assembly_rhs);
+ * d_x: device [S][2 nb] initial guesses in, solutions out.  Each system stops
+ * when its MRS-smoothed relative residual is below eps (the reference rule,
+ * Code/COCR_FP/rci.cpp:66-75); with verify = 1 it then also continues until
+ * ||b - A x|| / ||b|| < eps.  maxiter: per-system iteration limit. */
+int mtgpu_survey_solve(mtgpu_survey *s, const double *d_b, double *d_x, double eps, int maxiter,
+                       int verify, mtgpu_survey_stats *stats);
+
+/* Time `reps` launches of the batched double-float SpMV (all systems) with
+ * CUDA events on the survey's stream; *ms receives the total. */
+int mtgpu_survey_spmv_timed(mtgpu_survey *s, int reps, float *ms);
+
+void mtgpu_survey_destroy(mtgpu_survey *s);
 
 #ifdef __cplusplus
 }

@@ -36,7 +36,8 @@ class SolveStats(C.Structure):
 
 
 class SolveOpts(C.Structure):
-    _fields_ = [("stop_on_true_residual", C.c_int), ("iterations_per_launch", C.c_int)]
+    _fields_ = [("stop_on_true_residual", C.c_int), ("iterations_per_launch", C.c_int),
+                ("double_float", C.c_int)]
 
 
 class FemMesh(C.Structure):
@@ -46,6 +47,12 @@ class FemMesh(C.Structure):
                 ("nvkat", C.c_void_p), ("mu", C.c_void_p), ("mu0", C.c_void_p),
                 ("sigma", C.c_void_p), ("sigma0", C.c_void_p), ("dpr", C.c_void_p),
                 ("dpr0", C.c_void_p), ("n_bound", C.c_int), ("bound_nodes", C.c_void_p)]
+
+
+class SurveyStats(C.Structure):
+    _fields_ = [("status", C.c_int * 32), ("iterations", C.c_int * 32),
+                ("verifications", C.c_int * 32), ("true_residual_rel", C.c_double * 32),
+                ("seconds", C.c_double)]
 
 
 class MtgpuError(RuntimeError):
@@ -86,6 +93,11 @@ SIGNATURES = {
     "mtgpu_assembly_rhs": (C.c_int, [_vp, C.c_int, _d, _i, C.c_int, _d, _d, _d, _vp]),
     "mtgpu_cocr_create_from_assembly": (C.c_int, [_vp, C.c_double, _vp, C.POINTER(_vp)]),
     "mtgpu_assembly_destroy": (None, [_vp]),
+    "mtgpu_survey_create": (C.c_int, [_vp, C.c_int, _d, _vp, C.POINTER(_vp)]),
+    "mtgpu_survey_solve": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int, C.c_int,
+                                     C.POINTER(SurveyStats)]),
+    "mtgpu_survey_spmv_timed": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_float)]),
+    "mtgpu_survey_destroy": (None, [_vp]),
 }
 
 _lib = None

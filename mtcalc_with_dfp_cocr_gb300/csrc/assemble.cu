@@ -695,3 +695,51 @@ void Block2x2Dev::release()
 }
 
 }  // namespace mtgpu
+
+namespace mtgpu {
+namespace {
+__global__ void k_split_complex(long long len_c, long long len_r, const double2 *val_c,
+                                const double *val_r, double *kc, double *mc, double *kr)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < len_c) {
+        kc[i] = val_c[i].x;
+        mc[i] = val_c[i].y;
+    }
+    if (i < len_r) kr[i] = val_r[i];
+}
+}  // namespace
+
+int param_from_sell(const SellMatrix &A, ParamMatrix &P, cudaStream_t st)
+{
+    P.release();
+    P.nb = A.nb;
+    P.nslices = A.nslices;
+    P.nnz_c = A.nnz_c;
+    P.nnz_r = A.nnz_r;
+    P.len_c = A.len_c;
+    P.len_r = A.len_r;
+    int rc;
+    if ((rc = dev_alloc(&P.d_wc, P.nslices)) || (rc = dev_alloc(&P.d_wr, P.nslices)) ||
+        (rc = dev_alloc(&P.d_pc, P.nslices + 1)) || (rc = dev_alloc(&P.d_pr, P.nslices + 1)) ||
+        (rc = dev_alloc(&P.d_nc, P.nb)) || (rc = dev_alloc(&P.d_nr, P.nb)) ||
+        (rc = dev_alloc(&P.d_col_c, P.len_c)) || (rc = dev_alloc(&P.d_col_r, P.len_r)) ||
+        (rc = dev_alloc(&P.d_kc, P.len_c)) || (rc = dev_alloc(&P.d_mc, P.len_c)) ||
+        (rc = dev_alloc(&P.d_kr, P.len_r)))
+        return rc;
+    MTGPU_TRY(cudaMemcpyAsync(P.d_wc, A.d_wc, sizeof(int) * P.nslices, cudaMemcpyDeviceToDevice, st));
+    MTGPU_TRY(cudaMemcpyAsync(P.d_wr, A.d_wr, sizeof(int) * P.nslices, cudaMemcpyDeviceToDevice, st));
+    MTGPU_TRY(cudaMemcpyAsync(P.d_pc, A.d_pc, sizeof(long long) * (P.nslices + 1), cudaMemcpyDeviceToDevice, st));
+    MTGPU_TRY(cudaMemcpyAsync(P.d_pr, A.d_pr, sizeof(long long) * (P.nslices + 1), cudaMemcpyDeviceToDevice, st));
+    MTGPU_TRY(cudaMemcpyAsync(P.d_nc, A.d_nc, sizeof(int) * P.nb, cudaMemcpyDeviceToDevice, st));
+    MTGPU_TRY(cudaMemcpyAsync(P.d_nr, A.d_nr, sizeof(int) * P.nb, cudaMemcpyDeviceToDevice, st));
+    MTGPU_TRY(cudaMemcpyAsync(P.d_col_c, A.d_col_c, sizeof(int) * P.len_c, cudaMemcpyDeviceToDevice, st));
+    MTGPU_TRY(cudaMemcpyAsync(P.d_col_r, A.d_col_r, sizeof(int) * P.len_r, cudaMemcpyDeviceToDevice, st));
+    const long long len = std::max(P.len_c, P.len_r);
+    k_split_complex<<<(unsigned)((len + kThreads - 1) / kThreads), kThreads, 0, st>>>(
+        P.len_c, P.len_r, A.d_val_c, A.d_val_r, P.d_kc, P.d_mc, P.d_kr);
+    note_launches(1);
+    MTGPU_TRY(cudaGetLastError());
+    return MTGPU_OK;
+}
+}  // namespace mtgpu

@@ -43,6 +43,8 @@ int param_rhs(const ParamMatrix &P, int S, const double *d_omega, const int *d_a
               long long rhs_stride, int interleaved, cudaStream_t st);
 int param_to_sell(const ParamMatrix &P, double omega, SellMatrix &A, cudaStream_t st);
 int param_to_block2x2(const ParamMatrix &P, double omega, Block2x2Dev &B, cudaStream_t st);
+// A (complex, single system) viewed as K = Re A, M = Im A, omega = 1
+int param_from_sell(const SellMatrix &A, ParamMatrix &P, cudaStream_t st);
 int exclusive_scan_host(const int *d_in, int n, int *d_out, long long *total, cudaStream_t st);
 
 }  // namespace mtgpu

@@ -1,5 +1,6 @@
 // extern "C" entry points of libmtgpu (declared in include/mtgpu.h).
 #include "mtgpu_internal.cuh"
+#include "survey.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -124,6 +125,73 @@ int mtgpu::make_stream(mtgpu_cocr_s *c, void *stream)
     }
     return MTGPU_OK;
 }
+
+namespace {
+// One system through the double-float survey solver: K = Re A, M = Im A,
+// omega = 1, so A = K + i M exactly.
+int solve_double_float_host(int nb, const int *ig, const int *jg, const int *idi, const int *ijg,
+                     const double *di, const double *gg, const double *pr, double *x, double eps,
+                     int maxiter, int kpar, int n_nodes_c, const int *nvkat, const int *nver14,
+                     const double *sigma3d, const int *edges2, const int *ig_t, const int *jg_t,
+                     const double *gg_t, const int *is_node_bound, int verify,
+                     mtgpu_solve_stats *stats)
+{
+    const double t0 = now_seconds();
+    int rc = validate_lower(nb, ig, jg, idi, ijg);
+    if (rc) return rc;
+    mtgpu_mesh_desc mesh{kpar, nb, n_nodes_c, nvkat, nver14, sigma3d, edges2, ig_t, jg_t,
+                         gg_t, is_node_bound, 14};
+    if ((rc = validate_mesh(mesh))) return rc;
+    cudaStream_t st;
+    MTGPU_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    SellMatrix A;
+    ParamMatrix P;
+    Survey V;
+    double2 *db = nullptr, *dx = nullptr;
+    mtgpu_survey_stats ss{};
+    {
+        LowerDev L;
+        if (!(rc = upload_lower(nb, ig, jg, idi, ijg, di, gg, L, st)))
+            rc = sell_from_block2x2_device(nb, L.ig, L.jg, L.idi, L.ijg, L.di, L.gg, ig[nb], A, st);
+        note_launches(5);
+    }
+    const double one = 1.0;
+    if (!rc) rc = param_from_sell(A, P, st);
+    if (!rc) {
+        A.release();
+        rc = survey_setup(P, mesh, 1, &one, V, st);
+    }
+    if (!rc && !(rc = upload(&db, (const double2 *)pr, nb, st)) &&
+        !(rc = upload(&dx, (const double2 *)x, nb, st))) {
+        const double t1 = now_seconds();
+        rc = survey_solve(V, db, dx, eps, maxiter, verify, 16, &ss);
+        if (rc > -100) {
+            cudaError_t e = cudaMemcpyAsync(x, dx, sizeof(double2) * nb, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) {
+                set_last_error(e, "download of x", __FILE__, __LINE__);
+                rc = MTGPU_ERR_CUDA;
+            }
+        }
+        if (stats) {
+            stats->iterations = ss.iterations[0];
+            stats->residual_rel = V.hsys ? V.hsys[0].residual_rel : 0.0;
+            stats->true_residual_rel = ss.true_residual_rel[0];
+            stats->setup_seconds = t1 - t0;
+            stats->solve_seconds = now_seconds() - t1;
+            stats->status = ss.status[0];
+        }
+    }
+    cudaStreamSynchronize(st);
+    dev_free(db);
+    dev_free(dx);
+    V.release();
+    P.release();
+    A.release();
+    cudaStreamDestroy(st);
+    return rc;
+}
+}  // namespace
 
 extern "C" {
 
@@ -286,6 +354,10 @@ int mtgpu_pcocr_2x2_folded_ex(int n, const int *ig, const int *jg, const int *id
     const int nb = n / 2;
     MTGPU_CHECK_ARG(n_edges_c == nb, "n_edges_c must equal n/2 (all edges are unknowns)");
     const double t0 = now_s();
+    if (opts && opts->double_float)
+        return solve_double_float_host(nb, ig, jg, idi, ijg, di, gg, pr, x, eps, maxiter, kpar,
+                                n_nodes_c, nvkat, nver14, sigma3d, edges2, ig_t, jg_t, gg_t,
+                                is_node_bound, opts->stop_on_true_residual, stats);
     mtgpu_cocr *c = nullptr;
     int rc = mtgpu_cocr_create(nb, 0, ig, jg, idi, ijg, di, gg, 0, kpar, n_nodes_c, nvkat,
                                nver14, sigma3d, edges2, ig_t, jg_t, gg_t, is_node_bound,

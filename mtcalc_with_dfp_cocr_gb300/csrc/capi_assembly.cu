@@ -176,3 +176,79 @@ int mtgpu_cocr_create_from_assembly(mtgpu_assembly *a, double nu, void *stream, 
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------ survey
+#include "survey.cuh"
+
+struct mtgpu_survey_s {
+    mtgpu::Survey V;
+    mtgpu_assembly *a = nullptr;
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
+};
+
+extern "C" {
+
+int mtgpu_survey_create(mtgpu_assembly *a, int S, const double *nu, void *stream,
+                        mtgpu_survey **out)
+{
+    MTGPU_CHECK_ARG(a && nu && out, "null argument");
+    *out = nullptr;
+    MTGPU_CHECK_ARG(S >= 1 && S <= 32, "a survey batch holds 1 to 32 systems");
+    for (int k = 0; k < S; k++) MTGPU_CHECK_ARG(nu[k] > 0.0, "frequencies must be positive");
+    auto *s = new mtgpu_survey_s();
+    s->a = a;
+    if (stream) {
+        s->st = (cudaStream_t)stream;
+    } else {
+        cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            delete s;
+            set_last_error(e, "cudaStreamCreateWithFlags", __FILE__, __LINE__);
+            return MTGPU_ERR_CUDA;
+        }
+        s->own_stream = true;
+    }
+    std::vector<double> om(S);
+    for (int k = 0; k < S; k++) om[k] = kTwoPi * nu[k];
+    mtgpu_mesh_desc mesh{a->P.kpar, a->P.nb, a->P.kuzlov, a->nvkat.data(), a->nver.data(),
+                         a->sigflag.data(), a->edges.data(), a->ig_t.data(), a->ig_t.data(),
+                         nullptr, a->bound.data(), a->nver_stride};
+    int rc = survey_setup(a->P, mesh, S, om.data(), s->V, s->st);
+    if (rc) {
+        mtgpu_survey_destroy(s);
+        return rc;
+    }
+    *out = s;
+    return MTGPU_OK;
+}
+
+int mtgpu_survey_solve(mtgpu_survey *s, const double *d_b, double *d_x, double eps, int maxiter,
+                       int verify, mtgpu_survey_stats *stats)
+{
+    MTGPU_CHECK_ARG(s && d_b && d_x, "null argument");
+    MTGPU_CHECK_ARG(eps > 0.0, "eps must be positive");
+    MTGPU_TRY(cudaStreamSynchronize(cudaStreamLegacy));
+    const double t0 = now_seconds();
+    int rc = survey_solve(s->V, (const double2 *)d_b, (double2 *)d_x, eps, maxiter, verify, 16,
+                          stats);
+    if (stats) stats->seconds = now_seconds() - t0;
+    return rc;
+}
+
+int mtgpu_survey_spmv_timed(mtgpu_survey *s, int reps, float *ms)
+{
+    MTGPU_CHECK_ARG(s && ms && reps > 0, "bad argument");
+    return survey_spmv_timed(s->V, reps, ms);
+}
+
+void mtgpu_survey_destroy(mtgpu_survey *s)
+{
+    if (!s) return;
+    if (s->st) cudaStreamSynchronize(s->st);
+    s->V.release();
+    if (s->own_stream && s->st) cudaStreamDestroy(s->st);
+    delete s;
+}
+
+}  // extern "C"

@@ -1,0 +1,817 @@
+// Batched double-float COCR survey solver.
+//
+// All systems of a survey (frequencies x polarisations) share the mesh, hence
+// the sparsity pattern and the frequency-independent matrices of
+// A_k = K + i omega_k M.  One launch works on every system: a thread owns one
+// (row, system) pair, the SP systems of a row sit in adjacent lanes, so K, M
+// and the column indices are read once per row for all systems and every
+// gather of a vector row is one contiguous SP-wide segment.
+//
+// Arithmetic.  GB300 issues FP32 at 64x its FP64 rate.  Plain FP32 Krylov
+// iterations do not converge on these systems: the air (sigma = 1e-8 S/m)
+// leaves the gradient null space of the curl-curl operator regularised only
+// at ~1e-12 of its scale, below FP32 resolution.  So every quantity here is a
+// double-float (dfloat.cuh: hi + lo FP32 pair, 48-bit significand) computed
+// on the FP32 pipes; the iteration then follows the FP64 reference, iteration
+// for iteration.
+//
+// Algorithm.  The reference's preconditioned COCR
+// (Code/COCR_FP/pcocr_rci.cpp:52-181) with the folded preconditioner
+// (FoldedPreconditioner.cpp:578-630) and the MRS-smoothed stop test
+// (MRS.cpp:85-153, rci.cpp:66-75), per system; when a system stops, its true
+// residual ||b - A x|| / ||b|| is computed and, if `verify` is set and it is
+// not below eps, the system keeps iterating.  One iteration is four kernels
+// (node gather, edge gather + (a,w), updates + MRS weight, SpMV + MRS +
+// (z,s)), captured in a CUDA graph several iterations at a time; all
+// per-system decisions are taken on the device.
+#include "survey.cuh"
+#include "dfloat.cuh"
+
+namespace mtgpu {
+
+using namespace dfl;
+
+void Survey::release()
+{
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+    dev_free(kc); dev_free(mc); dev_free(kr);
+    dev_free(gv32); dev_free(tv32);
+    dev_free(da); dev_free(ds);
+    dev_free(omega); dev_free(omega64); dev_free(gkg); dev_free(gmg);
+    dev_free(sys);
+    dev_free(b); dev_free(x); dev_free(r); dev_free(s); dev_free(p); dev_free(a);
+    dev_free(z); dev_free(w); dev_free(sm); dev_free(h);
+    dev_free(partials);
+    if (hsys) cudaFreeHost(hsys);
+    hsys = nullptr;
+    G.release();
+}
+
+namespace {
+
+constexpr int kB = 256;   // threads per block of every survey kernel
+enum : int { kRun = 1 };
+
+__device__ __forceinline__ long long slot(const long long *p, int row, int k)
+{
+    return p[row / kSlice] + (long long)k * kSlice + (row % kSlice);
+}
+__device__ __forceinline__ df d2f(float2 v) { return df{v.x, v.y}; }
+__device__ __forceinline__ dfc from_d2(double2 v) { return dfc{from_double(v.x), from_double(v.y)}; }
+
+// Per-system FP64 sums of a block: lanes k, k+SP, ... of a warp hold system
+// k.  The block that finishes last adds all block partials in block order
+// and returns true, with the totals in tot[n][k].
+template <int SP, int N>
+__device__ bool sys_grid_sum(double (&v)[N], double *partials, unsigned int *ticket,
+                             double (*tot)[32])
+{
+    __shared__ double smem[N][kB / 32][SP];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int n = 0; n < N; n++) {
+#pragma unroll
+        for (int o = 16; o >= SP; o >>= 1) v[n] += __shfl_down_sync(0xffffffffu, v[n], o);
+        if (lane < SP) smem[n][warp][lane] = v[n];
+    }
+    __syncthreads();
+    if (threadIdx.x < SP) {
+#pragma unroll
+        for (int n = 0; n < N; n++) {
+            double acc = 0.0;
+            for (int q = 0; q < kB / 32; q++) acc += smem[n][q][threadIdx.x];
+            partials[((size_t)n * gridDim.x + blockIdx.x) * SP + threadIdx.x] = acc;
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    if (threadIdx.x < SP) {
+#pragma unroll
+        for (int n = 0; n < N; n++) {
+            double acc = 0.0;
+            for (int q = 0; q < (int)gridDim.x; q++)
+                acc += __ldcg(&partials[((size_t)n * gridDim.x + q) * SP + threadIdx.x]);
+            tot[n][threadIdx.x] = acc;
+        }
+    }
+    if (threadIdx.x == 0) *ticket = 0u;
+    __syncthreads();
+    return true;
+}
+
+struct Mat {
+    const int *wc, *wr;
+    const long long *pc, *pr;
+    const int *col_c, *col_r;
+    const float2 *kc, *mc, *kr;
+};
+
+// y = (K + i omega M) x for one (row, system): K x and M x accumulated
+// separately, then combined
+template <int SP>
+__device__ __forceinline__ dfc spmv_row(const Mat &A, int row, int k, df om,
+                                        const float4 *__restrict__ x)
+{
+    const int sl = row / kSlice, l = row % kSlice;
+    acc kr_, ki_, mr_, mi_;
+    {
+        const long long base = A.pc[sl] + l;
+        const int n = A.wc[sl];
+#pragma unroll 2
+        for (int q = 0; q < n; q++) {
+            const long long t = base + (long long)q * kSlice;
+            const dfc xv = ld(x, (long long)A.col_c[t] * SP + k);
+            const df kv = d2f(A.kc[t]), mv = d2f(A.mc[t]);
+            kr_.mac(kv, xv.re);
+            ki_.mac(kv, xv.im);
+            mr_.mac(mv, xv.re);
+            mi_.mac(mv, xv.im);
+        }
+    }
+    {
+        const long long base = A.pr[sl] + l;
+        const int n = A.wr[sl];
+#pragma unroll 4
+        for (int q = 0; q < n; q++) {
+            const long long t = base + (long long)q * kSlice;
+            const dfc xv = ld(x, (long long)A.col_r[t] * SP + k);
+            const df kv = d2f(A.kr[t]);
+            kr_.mac(kv, xv.re);
+            ki_.mac(kv, xv.im);
+        }
+    }
+    // y = Kx + i omega Mx
+    const df mxr = mr_.get(), mxi = mi_.get();
+    kr_.mac(neg(om), mxi);
+    ki_.mac(om, mxr);
+    return dfc{kr_.get(), ki_.get()};
+}
+
+__device__ __forceinline__ dfc csubd(dfc a, dfc b)
+{
+    return dfc{add(a.re, neg(b.re)), add(a.im, neg(b.im))};
+}
+
+// ------------------------------------------------------------ set-up
+// r = b - A x, s_m = r, ||b||, ||r||: stage 2 and the x0 test
+template <int SP>
+__global__ void __launch_bounds__(kB)
+k_init(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict__ b,
+       const float4 *__restrict__ x, float4 *__restrict__ r, float4 *__restrict__ sm,
+       SysState *sys, double *partials)
+{
+    const int k = threadIdx.x % SP;
+    const bool on = sys[k].status == kRun;
+    const df om = d2f(omega[k]);
+    acc nb2, nr2;
+    const int rpb = kB / SP;
+    for (int row = blockIdx.x * rpb + threadIdx.x / SP; row < nb; row += gridDim.x * rpb) {
+        if (!on) continue;
+        const long long i = (long long)row * SP + k;
+        const dfc bv = ld(b, i);
+        const dfc rv = csubd(bv, spmv_row<SP>(A, row, k, om, x));
+        st(r, i, rv);
+        st(sm, i, rv);
+        nb2.mac(bv.re, bv.re); nb2.mac(bv.im, bv.im);
+        nr2.mac(rv.re, rv.re); nr2.mac(rv.im, rv.im);
+    }
+    double v[2] = {nb2.to_double(), nr2.to_double()};
+    __shared__ double tot[2][32];
+    if (sys_grid_sum<SP, 2>(v, partials, &sys[0].ticket[0], tot) && threadIdx.x < SP) {
+        SysState &q = sys[threadIdx.x];
+        if (q.status == kRun) {
+            const double bb = tot[0][threadIdx.x], rr = tot[1][threadIdx.x];
+            q.r_old = bb > 0.0 ? sqrt(bb) : 0.0;
+            q.residual = rr > 0.0 ? sqrt(rr) : 0.0;
+            q.residual_rel = 1.0;
+            q.beta = make_double2(0.0, 0.0);
+            q.mrs_mode = 0;
+            q.iter = 1;
+            if (q.residual < 1e-30) {
+                q.status = MTGPU_X0_NULL;
+                q.iter = 0;
+            } else if (q.maxiter < 1) {
+                q.status = MTGPU_MAXITER;
+            }
+        }
+    }
+}
+
+// h = D_S G (z + beta a); use_beta = 0: h = D_S G z
+template <int SP>
+__global__ void __launch_bounds__(kB)
+k_node(int m, const int *__restrict__ gp, const int *__restrict__ gj, const float *__restrict__ gv,
+       const float4 *__restrict__ ds, const float4 *__restrict__ z, const float4 *__restrict__ a,
+       float4 *__restrict__ h, const SysState *sys, int use_beta)
+{
+    const int k = threadIdx.x % SP;
+    if (sys[k].status != kRun) return;
+    const dfc be = from_d2(sys[k].beta);
+    const int rpb = kB / SP;
+    for (int v = blockIdx.x * rpb + threadIdx.x / SP; v < m; v += gridDim.x * rpb) {
+        acc hr, hi;
+        for (int j = gp[v]; j < gp[v + 1]; j++) {
+            const long long idx = (long long)gj[j] * SP + k;
+            dfc an = ld(z, idx);
+            if (use_beta) an = caxpy(an, be, ld(a, idx));
+            hr.macf(an.re, gv[j]);
+            hi.macf(an.im, gv[j]);
+        }
+        st(h, (long long)v * SP + k, cmul(dfc{hr.get(), hi.get()}, ld(ds, (long long)v * SP + k)));
+    }
+}
+
+// mode 1: p = s + beta p, a = z + beta a, w = D_A a + G^T h, (a, w) -> alpha
+// mode 0: w = D_A src + G^T h (preconditioner application, no reduction)
+template <int SP>
+__global__ void __launch_bounds__(kB)
+k_edge(int n, const int *__restrict__ tp, const int *__restrict__ tj, const float *__restrict__ tv,
+       const float4 *__restrict__ da, const float4 *__restrict__ h, const float4 *__restrict__ src,
+       const float4 *__restrict__ z, float4 *__restrict__ p, float4 *__restrict__ a,
+       float4 *__restrict__ w, SysState *sys, double *partials, int mode)
+{
+    const int k = threadIdx.x % SP;
+    const bool on = sys[k].status == kRun;
+    const dfc be = from_d2(sys[k].beta);
+    acc awr, awi;
+    const int rpb = kB / SP;
+    for (int e = blockIdx.x * rpb + threadIdx.x / SP; e < n; e += gridDim.x * rpb) {
+        if (!on) continue;
+        const long long idx = (long long)e * SP + k;
+        dfc an;
+        if (mode == 0) {
+            an = ld(src, idx);
+        } else {
+            st(p, idx, caxpy(ld(src, idx), be, ld(p, idx)));
+            an = caxpy(ld(z, idx), be, ld(a, idx));
+            st(a, idx, an);
+        }
+        const dfc dv = cmul(an, ld(da, idx));
+        acc wr, wi;
+        wr.h = dv.re.h; wr.l = dv.re.l;
+        wi.h = dv.im.h; wi.l = dv.im.l;
+        for (int j = tp[e]; j < tp[e + 1]; j++) {
+            const dfc hv = ld(h, (long long)tj[j] * SP + k);
+            wr.macf(hv.re, tv[j]);
+            wi.macf(hv.im, tv[j]);
+        }
+        const dfc wn{wr.get(), wi.get()};
+        st(w, idx, wn);
+        awr.mac(an.re, wn.re);
+        awr.mac(neg(an.im), wn.im);
+        awi.mac(an.re, wn.im);
+        awi.mac(an.im, wn.re);
+    }
+    if (mode == 0) return;
+    double v[2] = {awr.to_double(), awi.to_double()};
+    __shared__ double tot[2][32];
+    if (sys_grid_sum<SP, 2>(v, partials, &sys[0].ticket[1], tot) && threadIdx.x < SP) {
+        SysState &q = sys[threadIdx.x];
+        if (q.status == kRun) {
+            const double2 aw = make_double2(tot[0][threadIdx.x], tot[1][threadIdx.x]);
+            if (fabs(aw.x) < 1e-40 && fabs(aw.y) < 1e-40) q.status = MTGPU_DIV_BY_ZERO;
+            else q.alpha = cdiv(q.zs, aw);
+        }
+    }
+}
+
+// x += alpha p, r -= alpha a, s -= alpha w; MRS weight from (s_m, r - s_m)
+template <int SP>
+__global__ void __launch_bounds__(kB)
+k_update(int n, const float4 *__restrict__ p, const float4 *__restrict__ a,
+         const float4 *__restrict__ w, const float4 *__restrict__ sm, float4 *__restrict__ x,
+         float4 *__restrict__ r, float4 *__restrict__ s, SysState *sys, double *partials)
+{
+    const int k = threadIdx.x % SP;
+    const bool on = sys[k].status == kRun;
+    const dfc al = from_d2(sys[k].alpha);
+    const dfc nal{neg(al.re), neg(al.im)};
+    acc su, uu;
+    const int rpb = kB / SP;
+    for (int e = blockIdx.x * rpb + threadIdx.x / SP; e < n; e += gridDim.x * rpb) {
+        if (!on) continue;
+        const long long idx = (long long)e * SP + k;
+        st(x, idx, caxpy(ld(x, idx), al, ld(p, idx)));
+        const dfc rn = caxpy(ld(r, idx), nal, ld(a, idx));
+        st(r, idx, rn);
+        st(s, idx, caxpy(ld(s, idx), nal, ld(w, idx)));
+        const dfc sv = ld(sm, idx);
+        const df ur = add(rn.re, neg(sv.re)), ui = add(rn.im, neg(sv.im));
+        su.mac(sv.re, ur); su.mac(sv.im, ui);
+        uu.mac(ur, ur); uu.mac(ui, ui);
+    }
+    double v[2] = {su.to_double(), uu.to_double()};
+    __shared__ double tot[2][32];
+    if (sys_grid_sum<SP, 2>(v, partials, &sys[0].ticket[2], tot) && threadIdx.x < SP) {
+        SysState &q = sys[threadIdx.x];
+        if (q.status == kRun) {
+            const double s_u = tot[0][threadIdx.x], u_u = tot[1][threadIdx.x];
+            const double wm = fabs(u_u) < 1e-100 ? 0.0 : -s_u / u_u;
+            if (wm < 0.0) q.mrs_mode = 0;
+            else if (wm > 1.0) q.mrs_mode = 1;
+            else {
+                q.mrs_mode = 2;
+                q.mrs_w = wm;
+            }
+        }
+    }
+}
+
+// z = A s, MRS update of s_m, ||s_m||, (z, s) -> stop test and beta.
+// mode 0 (set-up): z = A s and (z, s) only.
+template <int SP>
+__global__ void __launch_bounds__(kB)
+k_spmv(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict__ s,
+       const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
+       SysState *sys, double *partials, double eps, int mode)
+{
+    const int k = threadIdx.x % SP;
+    const bool on = sys[k].status == kRun;
+    const df om = d2f(omega[k]);
+    const int mm = mode ? sys[k].mrs_mode : 0;
+    const df wm = from_double(sys[k].mrs_w);
+    acc zsr, zsi, nn;
+    const int rpb = kB / SP;
+    for (int row = blockIdx.x * rpb + threadIdx.x / SP; row < nb; row += gridDim.x * rpb) {
+        if (!on) continue;
+        const long long i = (long long)row * SP + k;
+        const dfc y = spmv_row<SP>(A, row, k, om, s);
+        st(z, i, y);
+        const dfc sv = ld(s, i);
+        zsr.mac(y.re, sv.re); zsr.mac(neg(y.im), sv.im);
+        zsi.mac(y.re, sv.im); zsi.mac(y.im, sv.re);
+        if (mm != 0) {
+            dfc smv = ld(r, i);
+            if (mm == 2) {
+                const dfc old = ld(sm, i);
+                acc tr, ti;
+                tr.h = old.re.h; tr.l = old.re.l;
+                ti.h = old.im.h; ti.l = old.im.l;
+                tr.mac(wm, add(smv.re, neg(old.re)));
+                ti.mac(wm, add(smv.im, neg(old.im)));
+                smv = dfc{tr.get(), ti.get()};
+            }
+            st(sm, i, smv);
+            nn.mac(smv.re, smv.re);
+            nn.mac(smv.im, smv.im);
+        }
+    }
+    double v[3] = {zsr.to_double(), zsi.to_double(), nn.to_double()};
+    __shared__ double tot[3][32];
+    if (sys_grid_sum<SP, 3>(v, partials, &sys[0].ticket[3], tot) && threadIdx.x < SP) {
+        SysState &q = sys[threadIdx.x];
+        if (q.status == kRun) {
+            const double2 zs_new = make_double2(tot[0][threadIdx.x], tot[1][threadIdx.x]);
+            if (mode == 0) {
+                q.zs = zs_new;
+            } else {
+                if (q.mrs_mode != 0) q.residual = sqrt(tot[2][threadIdx.x]);
+                q.residual_rel = q.residual / q.r_old;
+                q.beta = cdiv(zs_new, q.zs);
+                q.zs = zs_new;
+                if (q.residual_rel < eps) {
+                    q.status = MTGPU_OK;
+                } else {
+                    q.iter += 1;
+                    if (q.iter > q.maxiter) q.status = MTGPU_MAXITER;
+                }
+            }
+        }
+    }
+}
+
+// true residual ||b - A x|| / ||b|| for the systems flagged in `check`
+template <int SP>
+__global__ void __launch_bounds__(kB)
+k_true(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict__ b,
+       const float4 *__restrict__ x, SysState *sys, const int *check, double *partials)
+{
+    const int k = threadIdx.x % SP;
+    const bool on = check[k] != 0;
+    const df om = d2f(omega[k]);
+    acc nb2, nr2;
+    const int rpb = kB / SP;
+    for (int row = blockIdx.x * rpb + threadIdx.x / SP; row < nb; row += gridDim.x * rpb) {
+        if (!on) continue;
+        const long long i = (long long)row * SP + k;
+        const dfc bv = ld(b, i);
+        const dfc rv = csubd(bv, spmv_row<SP>(A, row, k, om, x));
+        nb2.mac(bv.re, bv.re); nb2.mac(bv.im, bv.im);
+        nr2.mac(rv.re, rv.re); nr2.mac(rv.im, rv.im);
+    }
+    double v[2] = {nb2.to_double(), nr2.to_double()};
+    __shared__ double tot[2][32];
+    if (sys_grid_sum<SP, 2>(v, partials, &sys[0].ticket[0], tot) && threadIdx.x < SP &&
+        check[threadIdx.x]) {
+        const double bb = tot[0][threadIdx.x], rr = tot[1][threadIdx.x];
+        sys[threadIdx.x].true_rel = bb > 0.0 ? sqrt(rr) / sqrt(bb) : 0.0;
+        sys[threadIdx.x].checks += 1;
+    }
+}
+
+// ------------------------------------------------------- conversions
+__global__ void k_to_df(long long n, const double *src, float2 *dst)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const df v = from_double(src[i]);
+        dst[i] = make_float2(v.h, v.l);
+    }
+}
+
+// system-major FP64 [S][nb] -> row-major double-float [nb][SP]
+__global__ void k_in(int nb, int S, int SP, const double2 *src, float4 *dst)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)nb * SP) return;
+    const int k = (int)(i % SP);
+    const long long row = i / SP;
+    const double2 v = k < S ? src[(long long)k * nb + row] : make_double2(0.0, 0.0);
+    st(dst, i, from_d2(v));
+}
+
+__global__ void k_out(int nb, int S, int SP, const float4 *src, double2 *dst)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)nb * SP) return;
+    const int k = (int)(i % SP);
+    if (k >= S) return;
+    const float4 v = src[i];
+    dst[(long long)k * nb + i / SP] = make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+}
+
+// D_A[row][k] = 1 / (K_ii + i omega_k M_ii), computed in FP64
+__global__ void k_diag_a(int nb, int SP, const int *nc, const long long *pc, const int *col_c,
+                         const double *kcd, const double *mcd, const double *omega64, float4 *da)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)nb * SP) return;
+    const int k = (int)(i % SP);
+    const int row = (int)(i / SP);
+    double kk = 0.0, mm = 0.0;
+    for (int q = 0; q < nc[row]; q++) {
+        const long long t = slot(pc, row, q);
+        if (col_c[t] == row) {
+            kk = kcd[t];
+            mm = mcd[t];
+        }
+    }
+    const double2 inv = cdiv(make_double2(1.0, 0.0), make_double2(kk, omega64[k] * mm));
+    st(da, i, from_d2(inv));
+}
+
+// D_S[v][k] = 1 / (diag(G K G^T) + i omega_k diag(G M G^T)), in FP64
+__global__ void k_diag_s(int m, int SP, const double *gkg, const double *gmg,
+                         const double *omega64, float4 *ds)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)m * SP) return;
+    const int k = (int)(i % SP);
+    const int v = (int)(i / SP);
+    const double2 inv = cdiv(make_double2(1.0, 0.0), make_double2(gkg[v], omega64[k] * gmg[v]));
+    st(ds, i, from_d2(inv));
+}
+
+// diag(G K G^T) and diag(G M G^T), FP64, in the reference's summation order
+// (row k of A by increasing column, unfused multiply-add; see folded.cu)
+__global__ void k_gdiag(int m, const int *gp, const int *gj, const double *gv, const int *nc_row,
+                        const int *nr_row, const long long *pc, const long long *pr,
+                        const int *col_c, const double *kc, const double *mc, const int *col_r,
+                        const double *kr, double *gkg, double *gmg)
+{
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= m) return;
+    const int b0 = gp[v], e0 = gp[v + 1];
+    double sk = 0.0, sm = 0.0;
+    for (int j = b0; j < e0; j++) {
+        const int k = gj[j];
+        const int nc = nc_row[k], nr = nr_row[k];
+        double tk = 0.0, tm = 0.0;
+        int qc = 0, qr = 0;
+        while (qc < nc || qr < nr) {
+            const int cc = qc < nc ? col_c[slot(pc, k, qc)] : 0x7fffffff;
+            const int cr = qr < nr ? col_r[slot(pr, k, qr)] : 0x7fffffff;
+            double kv, mv;
+            int c;
+            if (cc < cr) {
+                const long long t = slot(pc, k, qc++);
+                kv = kc[t];
+                mv = mc[t];
+                c = cc;
+            } else {
+                kv = kr[slot(pr, k, qr++)];
+                mv = 0.0;
+                c = cr;
+            }
+            for (int u = b0; u < e0; u++)
+                if (gj[u] == c) {
+                    tk = __dadd_rn(tk, __dmul_rn(kv, gv[u]));
+                    tm = __dadd_rn(tm, __dmul_rn(mv, gv[u]));
+                }
+        }
+        sk = __dadd_rn(sk, __dmul_rn(tk, gv[j]));
+        sm = __dadd_rn(sm, __dmul_rn(tm, gv[j]));
+    }
+    gkg[v] = sk;
+    gmg[v] = sm;
+}
+
+__global__ void k_f64_to_f32(long long n, const double *src, float *dst)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = (float)src[i];
+}
+
+// ---------------------------------------------------------- dispatch
+template <int SP>
+struct Impl {
+    static Mat mat(const Survey &V)
+    {
+        const ParamMatrix &P = *V.P;
+        return Mat{P.d_wc, P.d_wr, P.d_pc, P.d_pr, P.d_col_c, P.d_col_r, V.kc, V.mc, V.kr};
+    }
+    static void iteration(Survey &V)
+    {
+        if (V.G.m > 0)
+            k_node<SP><<<V.grid_nodes, kB, 0, V.st>>>(V.G.m, V.G.d_gp, V.G.d_gj, V.gv32, V.ds, V.z,
+                                                      V.a, V.h, V.sys, 1);
+        k_edge<SP><<<V.grid_rows, kB, 0, V.st>>>(V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.da, V.h, V.s,
+                                                 V.z, V.p, V.a, V.w, V.sys, V.partials, 1);
+        k_update<SP><<<V.grid_rows, kB, 0, V.st>>>(V.nb, V.p, V.a, V.w, V.sm, V.x, V.r, V.s,
+                                                   V.sys, V.partials);
+        k_spmv<SP><<<V.grid_rows, kB, 0, V.st>>>(V.nb, mat(V), V.omega, V.s, V.r, V.z, V.sm, V.sys,
+                                                 V.partials, V.eps, 1);
+    }
+    // stages 1-4 of PCOCR_RCI::Run: r = b - A x, x0 test, s = M^-1 r,
+    // p = a = 0, z = A s, (z, s)
+    static void start(Survey &V)
+    {
+        k_init<SP><<<V.grid_rows, kB, 0, V.st>>>(V.nb, mat(V), V.omega, V.b, V.x, V.r, V.sm,
+                                                 V.sys, V.partials);
+        if (V.G.m > 0)
+            k_node<SP><<<V.grid_nodes, kB, 0, V.st>>>(V.G.m, V.G.d_gp, V.G.d_gj, V.gv32, V.ds, V.r,
+                                                      V.a, V.h, V.sys, 0);
+        k_edge<SP><<<V.grid_rows, kB, 0, V.st>>>(V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.da, V.h, V.r,
+                                                 V.z, V.p, V.a, V.s, V.sys, V.partials, 0);
+        cudaMemsetAsync(V.p, 0, sizeof(float4) * (size_t)V.nb * SP, V.st);
+        cudaMemsetAsync(V.a, 0, sizeof(float4) * (size_t)V.nb * SP, V.st);
+        k_spmv<SP><<<V.grid_rows, kB, 0, V.st>>>(V.nb, mat(V), V.omega, V.s, V.r, V.z, V.sm, V.sys,
+                                                 V.partials, V.eps, 0);
+        note_launches(V.G.m > 0 ? 4 : 3);
+    }
+    static void true_res(Survey &V, const int *check)
+    {
+        k_true<SP><<<V.grid_rows, kB, 0, V.st>>>(V.nb, mat(V), V.omega, V.b, V.x, V.sys, check,
+                                                 V.partials);
+        note_launches(1);
+    }
+    static void spmv_only(Survey &V)
+    {
+        k_spmv<SP><<<V.grid_rows, kB, 0, V.st>>>(V.nb, mat(V), V.omega, V.s, V.r, V.z, V.sm, V.sys,
+                                                 V.partials, V.eps, 0);
+    }
+};
+
+#define MTGPU_SP_DISPATCH(SPV, CALL)          \
+    switch (SPV) {                            \
+    case 1: Impl<1>::CALL; break;             \
+    case 2: Impl<2>::CALL; break;             \
+    case 4: Impl<4>::CALL; break;             \
+    case 8: Impl<8>::CALL; break;             \
+    case 16: Impl<16>::CALL; break;           \
+    default: Impl<32>::CALL; break;           \
+    }
+
+int sync_sys(Survey &V)
+{
+    MTGPU_TRY(cudaMemcpyAsync(V.hsys, V.sys, sizeof(SysState) * 32, cudaMemcpyDeviceToHost, V.st));
+    MTGPU_TRY(cudaStreamSynchronize(V.st));
+    return MTGPU_OK;
+}
+
+}  // namespace
+
+int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const double *omega,
+                 Survey &V, cudaStream_t st)
+{
+    V.release();
+    MTGPU_CHECK_ARG(S >= 1 && S <= 32, "a survey batch holds 1 to 32 systems");
+    V.P = &P;
+    V.st = st;
+    V.nb = P.nb;
+    V.S = S;
+    V.SP = 1;
+    while (V.SP < S) V.SP <<= 1;
+    int dev = 0, nsm = 0;
+    MTGPU_TRY(cudaGetDevice(&dev));
+    MTGPU_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const int rpb = kB / V.SP;
+    V.grid_rows = std::max(1, std::min(ceil_div(V.nb, rpb), nsm * 8));
+    int rc;
+    if ((rc = folded_build_g(mesh, V.G, st))) return rc;
+    const int m = V.G.m, mm = std::max(m, 1);
+    V.grid_nodes = std::max(1, std::min(ceil_div(mm, rpb), nsm * 8));
+    const size_t nv = (size_t)V.nb * V.SP;
+    if ((rc = dev_alloc(&V.kc, P.len_c)) || (rc = dev_alloc(&V.mc, P.len_c)) ||
+        (rc = dev_alloc(&V.kr, P.len_r)) || (rc = dev_alloc(&V.da, nv)) ||
+        (rc = dev_alloc(&V.ds, (size_t)mm * V.SP)) || (rc = dev_alloc(&V.gkg, mm)) ||
+        (rc = dev_alloc(&V.gmg, mm)) || (rc = dev_alloc(&V.omega, 32)) ||
+        (rc = dev_alloc(&V.omega64, 32)) || (rc = dev_alloc(&V.sys, 32)) ||
+        (rc = dev_alloc(&V.b, nv)) || (rc = dev_alloc(&V.x, nv)) || (rc = dev_alloc(&V.r, nv)) ||
+        (rc = dev_alloc(&V.s, nv)) || (rc = dev_alloc(&V.p, nv)) || (rc = dev_alloc(&V.a, nv)) ||
+        (rc = dev_alloc(&V.z, nv)) || (rc = dev_alloc(&V.w, nv)) || (rc = dev_alloc(&V.sm, nv)) ||
+        (rc = dev_alloc(&V.h, (size_t)mm * V.SP)) ||
+        (rc = dev_alloc(&V.partials, (size_t)3 * std::max(V.grid_rows, V.grid_nodes) * V.SP)))
+        return rc;
+    MTGPU_TRY(cudaMallocHost((void **)&V.hsys, sizeof(SysState) * 32));
+    std::vector<float2> omdf(32, make_float2(0.f, 0.f));
+    std::vector<double> om64(32, 0.0);
+    for (int k = 0; k < S; k++) {
+        const dfl::df v = dfl::from_double(omega[k]);
+        omdf[k] = make_float2(v.h, v.l);
+        om64[k] = omega[k];
+    }
+    MTGPU_TRY(cudaMemcpyAsync(V.omega, omdf.data(), sizeof(float2) * 32, cudaMemcpyHostToDevice, st));
+    MTGPU_TRY(cudaMemcpyAsync(V.omega64, om64.data(), sizeof(double) * 32, cudaMemcpyHostToDevice, st));
+    k_to_df<<<(unsigned)((P.len_c + kB - 1) / kB), kB, 0, st>>>(P.len_c, P.d_kc, V.kc);
+    k_to_df<<<(unsigned)((P.len_c + kB - 1) / kB), kB, 0, st>>>(P.len_c, P.d_mc, V.mc);
+    k_to_df<<<(unsigned)((P.len_r + kB - 1) / kB), kB, 0, st>>>(P.len_r, P.d_kr, V.kr);
+    k_diag_a<<<(unsigned)((nv + kB - 1) / kB), kB, 0, st>>>(V.nb, V.SP, P.d_nc, P.d_pc, P.d_col_c,
+                                                          P.d_kc, P.d_mc, V.omega64, V.da);
+    {
+        std::vector<int> gp(m + 1);
+        MTGPU_TRY(cudaMemcpyAsync(gp.data(), V.G.d_gp, sizeof(int) * (m + 1), cudaMemcpyDeviceToHost, st));
+        MTGPU_TRY(cudaStreamSynchronize(st));
+        const int nnz = gp[m];
+        if ((rc = dev_alloc(&V.gv32, std::max(nnz, 1))) || (rc = dev_alloc(&V.tv32, std::max(nnz, 1))))
+            return rc;
+        if (nnz > 0) {
+            k_f64_to_f32<<<(nnz + kB - 1) / kB, kB, 0, st>>>(nnz, V.G.d_gv, V.gv32);
+            k_f64_to_f32<<<(nnz + kB - 1) / kB, kB, 0, st>>>(nnz, V.G.d_tv, V.tv32);
+        }
+    }
+    if (m > 0) {
+        k_gdiag<<<ceil_div(m, 128), 128, 0, st>>>(m, V.G.d_gp, V.G.d_gj, V.G.d_gv, P.d_nc, P.d_nr,
+                                                   P.d_pc, P.d_pr, P.d_col_c, P.d_kc, P.d_mc,
+                                                   P.d_col_r, P.d_kr, V.gkg, V.gmg);
+        const size_t nm = (size_t)m * V.SP;
+        k_diag_s<<<(unsigned)((nm + kB - 1) / kB), kB, 0, st>>>(m, V.SP, V.gkg, V.gmg, V.omega64, V.ds);
+    }
+    MTGPU_TRY(cudaGetLastError());
+    MTGPU_TRY(cudaStreamSynchronize(st));
+    note_launches(8);
+    return MTGPU_OK;
+}
+
+int survey_spmv_timed(Survey &V, int reps, float *ms)
+{
+    std::vector<SysState> init(32);
+    for (int k = 0; k < 32; k++) {
+        SysState s{};
+        s.status = k < V.S ? kRun : MTGPU_OK;
+        s.maxiter = 1;
+        init[k] = s;
+    }
+    MTGPU_TRY(cudaMemcpyAsync(V.sys, init.data(), sizeof(SysState) * 32, cudaMemcpyHostToDevice, V.st));
+    MTGPU_TRY(cudaMemsetAsync(V.s, 0, sizeof(float4) * (size_t)V.nb * V.SP, V.st));
+    cudaEvent_t e0, e1;
+    MTGPU_TRY(cudaEventCreate(&e0));
+    MTGPU_TRY(cudaEventCreate(&e1));
+    MTGPU_TRY(cudaEventRecord(e0, V.st));
+    for (int q = 0; q < reps; q++) MTGPU_SP_DISPATCH(V.SP, spmv_only(V));
+    note_launches((unsigned long long)reps);
+    MTGPU_TRY(cudaEventRecord(e1, V.st));
+    MTGPU_TRY(cudaEventSynchronize(e1));
+    MTGPU_TRY(cudaEventElapsedTime(ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    MTGPU_TRY(cudaGetLastError());
+    return MTGPU_OK;
+}
+
+int survey_solve(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, double eps,
+                 int maxiter, int verify, int iters_per_launch, mtgpu_survey_stats *stats)
+{
+    const long long tot = (long long)V.nb * V.SP;
+    const unsigned ge = (unsigned)((tot + kB - 1) / kB);
+    V.eps = eps;
+    if (iters_per_launch <= 0) iters_per_launch = 16;
+    std::vector<SysState> init(32);
+    for (int k = 0; k < 32; k++) {
+        SysState s{};
+        s.status = k < V.S ? kRun : MTGPU_OK;
+        s.maxiter = maxiter;
+        s.residual_rel = 1.0;
+        s.true_rel = -1.0;
+        init[k] = s;
+    }
+    MTGPU_TRY(cudaMemcpyAsync(V.sys, init.data(), sizeof(SysState) * 32, cudaMemcpyHostToDevice, V.st));
+    k_in<<<ge, kB, 0, V.st>>>(V.nb, V.S, V.SP, b_sys_major, V.b);
+    k_in<<<ge, kB, 0, V.st>>>(V.nb, V.S, V.SP, x_sys_major, V.x);
+    note_launches(2);
+    MTGPU_SP_DISPATCH(V.SP, start(V));
+    MTGPU_TRY(cudaGetLastError());
+    int rc;
+    if ((rc = sync_sys(V))) return rc;
+    if (!V.graph || V.graph_iters != iters_per_launch) {
+        if (V.graph) cudaGraphExecDestroy(V.graph);
+        V.graph = nullptr;
+        cudaGraph_t g;
+        MTGPU_TRY(cudaStreamBeginCapture(V.st, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < iters_per_launch; k++) MTGPU_SP_DISPATCH(V.SP, iteration(V));
+        MTGPU_TRY(cudaStreamEndCapture(V.st, &g));
+        cudaError_t e = cudaGraphInstantiate(&V.graph, g, 0);
+        cudaGraphDestroy(g);
+        MTGPU_TRY(e);
+        V.graph_iters = iters_per_launch;
+    }
+    int *d_check = nullptr;
+    if ((rc = dev_alloc(&d_check, 32))) return rc;
+    std::vector<int> check(32, 0);
+    const unsigned long long kpi = V.G.m > 0 ? 4 : 3;
+    long long guard = 0;
+    const long long guard_max = (long long)maxiter + 64LL * iters_per_launch + 64;
+    for (;;) {
+        bool running = false;
+        for (int k = 0; k < V.S; k++) running |= V.hsys[k].status == kRun;
+        if (running) {
+            cudaError_t e = cudaGraphLaunch(V.graph, V.st);
+            if (e != cudaSuccess) {
+                set_last_error(e, "cudaGraphLaunch", __FILE__, __LINE__);
+                rc = MTGPU_ERR_CUDA;
+                break;
+            }
+            note_launches(kpi * (unsigned long long)iters_per_launch);
+            guard += iters_per_launch;
+            if ((rc = sync_sys(V))) break;
+            if (guard > guard_max) {
+                set_last_message("survey solve did not finish within its iteration guard");
+                rc = MTGPU_ERR_TIMEOUT;
+                break;
+            }
+            continue;
+        }
+        // every system stopped: measure the true residual of the converged
+        // ones (first time, or again after further iterations)
+        bool any = false;
+        for (int k = 0; k < 32; k++) {
+            const SysState &q = V.hsys[k];
+            check[k] = k < V.S && q.status == MTGPU_OK && (q.checks == 0 || (verify && q.true_rel >= eps));
+            any |= check[k] != 0;
+        }
+        if (!any) break;
+        cudaError_t e = cudaMemcpyAsync(d_check, check.data(), sizeof(int) * 32, cudaMemcpyHostToDevice, V.st);
+        if (e != cudaSuccess) {
+            set_last_error(e, "cudaMemcpyAsync", __FILE__, __LINE__);
+            rc = MTGPU_ERR_CUDA;
+            break;
+        }
+        MTGPU_SP_DISPATCH(V.SP, true_res(V, d_check));
+        if ((rc = sync_sys(V))) break;
+        bool resume = false;
+        for (int k = 0; k < V.S; k++) {
+            SysState &q = V.hsys[k];
+            if (check[k] && verify && q.true_rel >= eps && q.iter < q.maxiter) {
+                // keep iterating: the recurrences already hold the next
+                // iteration's z, s and beta
+                q.status = kRun;
+                q.iter += 1;
+                resume = true;
+            }
+        }
+        if (!resume) break;
+        e = cudaMemcpyAsync(V.sys, V.hsys, sizeof(SysState) * 32, cudaMemcpyHostToDevice, V.st);
+        if (e != cudaSuccess) {
+            set_last_error(e, "cudaMemcpyAsync", __FILE__, __LINE__);
+            rc = MTGPU_ERR_CUDA;
+            break;
+        }
+        if ((rc = sync_sys(V))) break;
+    }
+    dev_free(d_check);
+    if (rc) return rc;
+    k_out<<<ge, kB, 0, V.st>>>(V.nb, V.S, V.SP, V.x, x_sys_major);
+    note_launches(1);
+    MTGPU_TRY(cudaGetLastError());
+    MTGPU_TRY(cudaStreamSynchronize(V.st));
+    int worst = MTGPU_OK;
+    for (int k = 0; k < V.S; k++) {
+        const SysState &q = V.hsys[k];
+        if (stats) {
+            stats->status[k] = q.status;
+            stats->iterations[k] = q.iter;
+            stats->verifications[k] = q.checks;
+            stats->true_residual_rel[k] = q.true_rel;
+        }
+        if (q.status != MTGPU_OK && worst == MTGPU_OK) worst = q.status;
+    }
+    return worst;
+}
+
+}  // namespace mtgpu

@@ -1,0 +1,54 @@
+// Batched double-float survey solver (survey.cu).
+#pragma once
+#include "assemble.cuh"
+
+namespace mtgpu {
+
+// per-system state, read and written by the kernels' last blocks
+struct SysState {
+    double2 zs, alpha, beta;
+    double r_old;          // ||b||
+    double residual;       // ||s_m|| (MRS-smoothed residual)
+    double residual_rel;   // residual / r_old: the reference's stop quantity
+    double true_rel;       // ||b - A x|| / ||b|| of the last verification
+    double mrs_w;
+    int mrs_mode;          // 0 keep s_m, 1 s_m = r, 2 s_m += w (r - s_m)
+    int status;            // 1 running, else MTGPU_OK / MTGPU_DIV_BY_ZERO / MTGPU_MAXITER / MTGPU_X0_NULL
+    int iter;              // the reference's iteration counter
+    int checks;            // true-residual verifications
+    int maxiter;
+    unsigned int ticket[4];  // block-completion counters (system 0 only)
+};
+
+struct Survey {
+    const ParamMatrix *P = nullptr;
+    cudaStream_t st = nullptr;
+    int nb = 0, S = 0, SP = 1;
+    int grid_rows = 0, grid_nodes = 0;
+    Folded G;                                    // pattern of G and G^T
+    float2 *kc = nullptr, *mc = nullptr, *kr = nullptr;   // double-float K and M per slot
+    float *gv32 = nullptr, *tv32 = nullptr;      // values of G and G^T (+-1/2, exact in FP32)
+    float4 *da = nullptr, *ds = nullptr;         // 1/diag(A_k), 1/diag(G A_k G^T): [row][SP]
+    float2 *omega = nullptr;                     // double-float omega_k
+    double *omega64 = nullptr;
+    double *gkg = nullptr, *gmg = nullptr;       // FP64 diag(G K G^T), diag(G M G^T)
+    SysState *sys = nullptr, *hsys = nullptr;
+    float4 *b = nullptr, *x = nullptr, *r = nullptr, *s = nullptr, *p = nullptr, *a = nullptr,
+           *z = nullptr, *w = nullptr, *sm = nullptr;     // [row][SP]
+    float4 *h = nullptr;                          // [node][SP]
+    double *partials = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int graph_iters = 0;
+    double eps = 1e-8;
+    void release();
+};
+
+int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const double *omega,
+                 Survey &V, cudaStream_t st);
+// b, x: system-major FP64 [S][nb] complex; x is the initial guess in and the
+// solution out.  verify: continue until the true residual is below eps too.
+int survey_solve(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, double eps,
+                 int maxiter, int verify, int iters_per_launch, mtgpu_survey_stats *stats);
+int survey_spmv_timed(Survey &V, int reps, float *ms);
+
+}  // namespace mtgpu

@@ -33,7 +33,8 @@ def _mesh_args(m: SolveMesh):
 
 
 def pcocr_2x2_folded(slae: BlockSLAE, mesh: SolveMesh, x0=None, eps=None, maxiter=None,
-                     stop_on_true_residual=False, iterations_per_launch=0, write_kit_in=None):
+                     stop_on_true_residual=False, iterations_per_launch=0, write_kit_in=None,
+                     double_float=False):
     """Solve A x = pr on the GPU.  Returns (code, x, stats).
 
     write_kit_in: a directory; when given, the reference entry point
@@ -54,7 +55,8 @@ def pcocr_2x2_folded(slae: BlockSLAE, mesh: SolveMesh, x0=None, eps=None, maxite
         _lib.check(rc, "mtgpu_pcocr_2x2_folded")
         return rc, x, None
     st = _lib.SolveStats()
-    opts = _lib.SolveOpts(int(stop_on_true_residual), int(iterations_per_launch))
+    opts = _lib.SolveOpts(int(stop_on_true_residual), int(iterations_per_launch),
+                          int(double_float))
     rc = L.mtgpu_pcocr_2x2_folded_ex(*slae_args, *_mesh_args(mesh), C.byref(opts), C.byref(st))
     _lib.check(rc, "mtgpu_pcocr_2x2_folded_ex")
     return rc, x, st
@@ -140,7 +142,7 @@ class CocrContext:
               iterations_per_launch=0):
         """b, x: torch CUDA float64 tensors of 2*nb; x is updated in place."""
         st = _lib.SolveStats()
-        opts = _lib.SolveOpts(int(stop_on_true_residual), int(iterations_per_launch))
+        opts = _lib.SolveOpts(int(stop_on_true_residual), int(iterations_per_launch), 0)
         rc = _lib.lib().mtgpu_cocr_solve(self._h, C.c_void_p(b.data_ptr()),
                                          C.c_void_p(x.data_ptr()), float(eps), int(maxiter),
                                          C.byref(opts), C.byref(st))

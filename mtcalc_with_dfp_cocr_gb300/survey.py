@@ -1,0 +1,65 @@
+"""Batched survey solver over libmtgpu.
+
+All frequencies x polarisations of a survey share the mesh, hence the
+sparsity pattern and the matrices K and M of A(omega) = K + i omega M.
+Survey solves up to 32 such systems together with the reference's COCR,
+folded preconditioner and MRS stop test, one lane per system, in
+double-float arithmetic (FP32 pairs, 48-bit significand) on the FP32 pipes;
+with verify=True every system also reaches a true relative residual
+||b - A x|| / ||b|| below eps.
+
+The reference solves the systems one by one in FP64 (CalcStarter runs
+COCR_FP per frequency and polarisation, Code/CalcStarter/main.cpp:311-325).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+
+
+class Survey:
+    def __init__(self, assembly, nus, stream=None):
+        """assembly: an Assembly; nus: frequency [Hz] of every system."""
+        nus = np.ascontiguousarray(nus, np.float64)
+        self.S = len(nus)
+        self.nb = assembly.nb
+        self._assembly = assembly
+        h = C.c_void_p()
+        sp = None if stream is None else C.c_void_p(stream.cuda_stream)
+        rc = _lib.lib().mtgpu_survey_create(assembly._h, self.S, nus, sp, C.byref(h))
+        _lib.check(rc, "mtgpu_survey_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.lib().mtgpu_survey_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def spmv_timed(self, reps):
+        """Device milliseconds of `reps` batched FP32 SpMV launches."""
+        ms = C.c_float()
+        _lib.check(_lib.lib().mtgpu_survey_spmv_timed(self._h, int(reps), C.byref(ms)),
+                   "mtgpu_survey_spmv_timed")
+        return ms.value
+
+    def solve(self, b, x, eps=1e-8, maxiter=20000, verify=True):
+        """b, x: torch CUDA float64 tensors shaped (S, 2 nb); x: initial
+        guesses in, solutions out.  Returns (code, stats dict)."""
+        st = _lib.SurveyStats()
+        rc = _lib.lib().mtgpu_survey_solve(self._h, C.c_void_p(b.data_ptr()),
+                                           C.c_void_p(x.data_ptr()), float(eps), int(maxiter),
+                                           int(verify), C.byref(st))
+        _lib.check(rc, "mtgpu_survey_solve")
+        S = self.S
+        return rc, {"status": list(st.status[:S]), "iterations": list(st.iterations[:S]),
+                    "verifications": list(st.verifications[:S]),
+                    "true_residual_rel": list(st.true_residual_rel[:S]), "seconds": st.seconds}

@@ -172,3 +172,17 @@ def test_dropin_executable(gpu, tmp_path):
     assert np.linalg.norm(x - v3) <= 1e-6 * np.linalg.norm(v3)
     kr, keps, kit, ktime = slae_io.read_kit(os.path.join(d, "kit"))
     assert abs(kit - kit_iter) <= 2 and kr < s.eps
+
+
+def test_dropin_double_float(gpu):
+    """The reference entry point in double-float arithmetic: same iteration
+    count as FP64 and the true relative residual 1e-8 (checked in FP64 on
+    the CPU)."""
+    w, s, mesh = _c1_system(0)
+    code, x, st = solver.pcocr_2x2_folded(s, mesh, double_float=True, stop_on_true_residual=True)
+    code64, x64, st64 = solver.pcocr_2x2_folded(s, mesh, stop_on_true_residual=True)
+    assert code == code64 == 0
+    assert abs(st.iterations - st64.iterations) <= 3
+    assert st.true_residual_rel < 1e-8
+    assert _true_rel_res(s, x) < 1e-8
+    assert np.linalg.norm(x - x64) <= 1e-6 * np.linalg.norm(x64)

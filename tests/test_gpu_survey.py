@@ -1,0 +1,81 @@
+"""Batched double-float survey solver: the reference's COCR iteration for
+every system at once, in double-float arithmetic on the FP32 pipes.  It must
+follow the FP64 solver's iteration counts and reach the true FP64 relative
+residual 1e-8."""
+import numpy as np
+import pytest
+
+from mtcalc_with_dfp_cocr_gb300 import assembly, normal1d, slae_io, solver, survey, workloads
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _tables(w, nus):
+    tops, sig = [l.top for l in w.mesh.layers], [l.sigma for l in w.mesh.layers]
+    return [normal1d.solve_1d(nu, tops, sig) for nu in nus]
+
+
+def _run(torch, name, systems, eps=1e-8, verify=True, maxiter=20000):
+    w = workloads.make(name)
+    nus = [f for f, _ in systems]
+    alfas = [a for _, a in systems]
+    tabs = _tables(w, nus)
+    A = assembly.Assembly(w.mesh)
+    S = len(systems)
+    b = torch.empty(S, 2 * w.mesh.nb, dtype=torch.float64, device="cuda")
+    A.rhs(nus, alfas, tabs[0][0], np.stack([t[1] for t in tabs]), np.stack([t[2] for t in tabs]), b)
+    x = torch.zeros_like(b)
+    sv = survey.Survey(A, nus)
+    code, st = sv.solve(b, x, eps=eps, maxiter=maxiter, verify=verify)
+    return w, A, tabs, b, x, code, st
+
+
+@pytest.mark.parametrize("name,systems", [
+    ("small", [(0.1, 1), (0.1, 0), (10.0, 1)]),
+    ("c1", [(1.0, 1), (1.0, 0)]),
+])
+def test_survey_follows_fp64_and_reaches_true_residual(gpu, name, systems):
+    torch = gpu
+    w, A, tabs, b, x, code, st = _run(torch, name, systems)
+    assert code == 0, st
+    mesh = slae_io.mesh_to_solve_mesh(w.mesh)
+    for k, (nu, alfa) in enumerate(systems):
+        assert st["status"][k] == 0
+        assert st["true_residual_rel"][k] < 1e-8
+        s = A.block2x2(nu, alfa, *tabs[k])
+        xk = x[k].cpu().numpy()
+        r = s.pr - O.spmv(s, xk)
+        assert np.linalg.norm(r) / np.linalg.norm(s.pr) < 1e-8        # checked in FP64 on the CPU
+        code64, x64, st64 = solver.pcocr_2x2_folded(s, mesh, stop_on_true_residual=True)
+        assert code64 == 0
+        assert abs(st["iterations"][k] - st64.iterations) <= 3
+        assert np.linalg.norm(xk - x64) <= 1e-6 * np.linalg.norm(x64)
+
+
+def test_survey_reference_stop_rule_matches_oracle(gpu):
+    """Without verification the stop rule is the reference's alone; the
+    iteration counts match the oracle's."""
+    torch = gpu
+    w, A, tabs, b, x, code, st = _run(torch, "c1", [(1.0, 1), (1.0, 0)], verify=False)
+    assert code == 0
+    mesh = slae_io.mesh_to_solve_mesh(w.mesh)
+    for k, alfa in enumerate((1, 0)):
+        s = A.block2x2(1.0, alfa, *tabs[k])
+        c, xo, sto = O.pcocr(s, mesh, nthreads=4)
+        assert abs(st["iterations"][k] - sto.iterations) <= 2
+
+
+def test_survey_single_system_and_padding(gpu):
+    torch = gpu
+    w, A, tabs, b, x, code, st = _run(torch, "tiny", [(1.0, 1)])
+    assert code == 0 and st["true_residual_rel"][0] < 1e-8
+    # five systems pad to eight lanes; all must finish
+    w, A, tabs, b, x, code, st = _run(torch, "tiny", [(0.01, 1), (0.1, 0), (1.0, 1), (10.0, 0), (100.0, 1)])
+    assert code == 0 and max(st["true_residual_rel"]) < 1e-8
+
+
+def test_survey_iteration_limit(gpu):
+    torch = gpu
+    w, A, tabs, b, x, code, st = _run(torch, "small", [(0.1, 1)], maxiter=5)
+    assert code == -3 and st["status"][0] == -3 and st["iterations"][0] == 6
