@@ -342,7 +342,17 @@ int cocr_alloc(CocrSolver &S)
     int dev = 0, nsm = 0;
     MTGPU_TRY(cudaGetDevice(&dev));
     MTGPU_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    S.grid = std::max(1, std::min(ceil_div(nb, kRedThreads), nsm * 8));
+    // as many blocks as are resident at once (the loops are grid-stride), so
+    // no block waits for a second wave
+    int occ = 64;
+    const void *fs[] = {(const void *)k_it_edge, (const void *)k_it_update, (const void *)k_it_spmv,
+                        (const void *)k_init_norms};
+    for (const void *f : fs) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, kRedThreads, 0) == cudaSuccess && b > 0)
+            occ = std::min(occ, b);
+    }
+    S.grid = std::max(1, std::min(ceil_div(nb, kRedThreads), occ * nsm));
     int rc;
     if ((rc = dev_alloc(&S.r, nb)) || (rc = dev_alloc(&S.p, nb)) || (rc = dev_alloc(&S.s, nb)) ||
         (rc = dev_alloc(&S.z, nb)) || (rc = dev_alloc(&S.a, nb)) || (rc = dev_alloc(&S.w, nb)) ||

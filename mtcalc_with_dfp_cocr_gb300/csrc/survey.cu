@@ -113,8 +113,10 @@ struct Mat {
 };
 
 // y = (K + i omega M) x for one (row, system): K x and M x accumulated
-// separately, then combined
-template <int SP>
+// separately, then combined.  Slots are processed in batches of CH: the
+// batch's column indices and matrix values are loaded first, then all its x
+// gathers are issued together, so CH loads are in flight per thread.
+template <int SP, int CH>
 __device__ __forceinline__ dfc spmv_row(const Mat &A, int row, int k, df om,
                                         const float4 *__restrict__ x)
 {
@@ -123,27 +125,61 @@ __device__ __forceinline__ dfc spmv_row(const Mat &A, int row, int k, df om,
     {
         const long long base = A.pc[sl] + l;
         const int n = A.wc[sl];
-#pragma unroll 2
-        for (int q = 0; q < n; q++) {
-            const long long t = base + (long long)q * kSlice;
-            const dfc xv = ld(x, (long long)A.col_c[t] * SP + k);
-            const df kv = d2f(A.kc[t]), mv = d2f(A.mc[t]);
-            kr_.mac(kv, xv.re);
-            ki_.mac(kv, xv.im);
-            mr_.mac(mv, xv.re);
-            mi_.mac(mv, xv.im);
+        for (int q0 = 0; q0 < n; q0 += CH) {
+            int cols[CH];
+            float2 kv[CH], mv[CH];
+            float4 xv[CH];
+#pragma unroll
+            for (int j = 0; j < CH; j++) {
+                if (q0 + j < n) {
+                    const long long t = base + (long long)(q0 + j) * kSlice;
+                    cols[j] = A.col_c[t];
+                    kv[j] = A.kc[t];
+                    mv[j] = A.mc[t];
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < CH; j++)
+                if (q0 + j < n) xv[j] = x[(long long)cols[j] * SP + k];
+#pragma unroll
+            for (int j = 0; j < CH; j++) {
+                if (q0 + j < n) {
+                    const df kd = d2f(kv[j]), md = d2f(mv[j]);
+                    const df xr{xv[j].x, xv[j].y}, xi{xv[j].z, xv[j].w};
+                    kr_.mac(kd, xr);
+                    ki_.mac(kd, xi);
+                    mr_.mac(md, xr);
+                    mi_.mac(md, xi);
+                }
+            }
         }
     }
     {
         const long long base = A.pr[sl] + l;
         const int n = A.wr[sl];
-#pragma unroll 4
-        for (int q = 0; q < n; q++) {
-            const long long t = base + (long long)q * kSlice;
-            const dfc xv = ld(x, (long long)A.col_r[t] * SP + k);
-            const df kv = d2f(A.kr[t]);
-            kr_.mac(kv, xv.re);
-            ki_.mac(kv, xv.im);
+        for (int q0 = 0; q0 < n; q0 += CH) {
+            int cols[CH];
+            float2 kv[CH];
+            float4 xv[CH];
+#pragma unroll
+            for (int j = 0; j < CH; j++) {
+                if (q0 + j < n) {
+                    const long long t = base + (long long)(q0 + j) * kSlice;
+                    cols[j] = A.col_r[t];
+                    kv[j] = A.kr[t];
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < CH; j++)
+                if (q0 + j < n) xv[j] = x[(long long)cols[j] * SP + k];
+#pragma unroll
+            for (int j = 0; j < CH; j++) {
+                if (q0 + j < n) {
+                    const df kd = d2f(kv[j]);
+                    kr_.mac(kd, df{xv[j].x, xv[j].y});
+                    ki_.mac(kd, df{xv[j].z, xv[j].w});
+                }
+            }
         }
     }
     // y = Kx + i omega Mx
@@ -175,7 +211,7 @@ k_init(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict
         if (!on) continue;
         const long long i = (long long)row * SP + k;
         const dfc bv = ld(b, i);
-        const dfc rv = csubd(bv, spmv_row<SP>(A, row, k, om, x));
+        const dfc rv = csubd(bv, spmv_row<SP, 4>(A, row, k, om, x));
         st(r, i, rv);
         st(sm, i, rv);
         nb2.mac(bv.re, bv.re); nb2.mac(bv.im, bv.im);
@@ -325,7 +361,7 @@ k_update(int n, const float4 *__restrict__ p, const float4 *__restrict__ a,
 
 // z = A s, MRS update of s_m, ||s_m||, (z, s) -> stop test and beta.
 // mode 0 (set-up): z = A s and (z, s) only.
-template <int SP>
+template <int SP, int CH>
 __global__ void __launch_bounds__(kB)
 k_spmv(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict__ s,
        const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
@@ -341,7 +377,7 @@ k_spmv(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict
     for (int row = blockIdx.x * rpb + threadIdx.x / SP; row < nb; row += gridDim.x * rpb) {
         if (!on) continue;
         const long long i = (long long)row * SP + k;
-        const dfc y = spmv_row<SP>(A, row, k, om, s);
+        const dfc y = spmv_row<SP, CH>(A, row, k, om, s);
         st(z, i, y);
         const dfc sv = ld(s, i);
         zsr.mac(y.re, sv.re); zsr.mac(neg(y.im), sv.im);
@@ -401,7 +437,7 @@ k_true(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict
         if (!on) continue;
         const long long i = (long long)row * SP + k;
         const dfc bv = ld(b, i);
-        const dfc rv = csubd(bv, spmv_row<SP>(A, row, k, om, x));
+        const dfc rv = csubd(bv, spmv_row<SP, 4>(A, row, k, om, x));
         nb2.mac(bv.re, bv.re); nb2.mac(bv.im, bv.im);
         nr2.mac(rv.re, rv.re); nr2.mac(rv.im, rv.im);
     }
@@ -536,45 +572,69 @@ struct Impl {
         const ParamMatrix &P = *V.P;
         return Mat{P.d_wc, P.d_wr, P.d_pc, P.d_pr, P.d_col_c, P.d_col_r, V.kc, V.mc, V.kr};
     }
+    static void spmv(Survey &V, int mode)
+    {
+        const Mat A = mat(V);
+        switch (V.ch) {
+        case 2: k_spmv<SP, 2><<<V.g_spmv, kB, 0, V.st>>>(V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, V.eps, mode); break;
+        case 8: k_spmv<SP, 8><<<V.g_spmv, kB, 0, V.st>>>(V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, V.eps, mode); break;
+        default: k_spmv<SP, 4><<<V.g_spmv, kB, 0, V.st>>>(V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, V.eps, mode); break;
+        }
+    }
     static void iteration(Survey &V)
     {
         if (V.G.m > 0)
-            k_node<SP><<<V.grid_nodes, kB, 0, V.st>>>(V.G.m, V.G.d_gp, V.G.d_gj, V.gv32, V.ds, V.z,
-                                                      V.a, V.h, V.sys, 1);
-        k_edge<SP><<<V.grid_rows, kB, 0, V.st>>>(V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.da, V.h, V.s,
-                                                 V.z, V.p, V.a, V.w, V.sys, V.partials, 1);
-        k_update<SP><<<V.grid_rows, kB, 0, V.st>>>(V.nb, V.p, V.a, V.w, V.sm, V.x, V.r, V.s,
-                                                   V.sys, V.partials);
-        k_spmv<SP><<<V.grid_rows, kB, 0, V.st>>>(V.nb, mat(V), V.omega, V.s, V.r, V.z, V.sm, V.sys,
-                                                 V.partials, V.eps, 1);
+            k_node<SP><<<V.g_node, kB, 0, V.st>>>(V.G.m, V.G.d_gp, V.G.d_gj, V.gv32, V.ds, V.z, V.a,
+                                                  V.h, V.sys, 1);
+        k_edge<SP><<<V.g_edge, kB, 0, V.st>>>(V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.da, V.h, V.s, V.z,
+                                              V.p, V.a, V.w, V.sys, V.partials, 1);
+        k_update<SP><<<V.g_update, kB, 0, V.st>>>(V.nb, V.p, V.a, V.w, V.sm, V.x, V.r, V.s, V.sys,
+                                                  V.partials);
+        spmv(V, 1);
     }
     // stages 1-4 of PCOCR_RCI::Run: r = b - A x, x0 test, s = M^-1 r,
     // p = a = 0, z = A s, (z, s)
     static void start(Survey &V)
     {
-        k_init<SP><<<V.grid_rows, kB, 0, V.st>>>(V.nb, mat(V), V.omega, V.b, V.x, V.r, V.sm,
-                                                 V.sys, V.partials);
+        k_init<SP><<<V.g_init, kB, 0, V.st>>>(V.nb, mat(V), V.omega, V.b, V.x, V.r, V.sm, V.sys,
+                                              V.partials);
         if (V.G.m > 0)
-            k_node<SP><<<V.grid_nodes, kB, 0, V.st>>>(V.G.m, V.G.d_gp, V.G.d_gj, V.gv32, V.ds, V.r,
-                                                      V.a, V.h, V.sys, 0);
-        k_edge<SP><<<V.grid_rows, kB, 0, V.st>>>(V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.da, V.h, V.r,
-                                                 V.z, V.p, V.a, V.s, V.sys, V.partials, 0);
+            k_node<SP><<<V.g_node, kB, 0, V.st>>>(V.G.m, V.G.d_gp, V.G.d_gj, V.gv32, V.ds, V.r, V.a,
+                                                  V.h, V.sys, 0);
+        k_edge<SP><<<V.g_edge, kB, 0, V.st>>>(V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.da, V.h, V.r, V.z,
+                                              V.p, V.a, V.s, V.sys, V.partials, 0);
         cudaMemsetAsync(V.p, 0, sizeof(float4) * (size_t)V.nb * SP, V.st);
         cudaMemsetAsync(V.a, 0, sizeof(float4) * (size_t)V.nb * SP, V.st);
-        k_spmv<SP><<<V.grid_rows, kB, 0, V.st>>>(V.nb, mat(V), V.omega, V.s, V.r, V.z, V.sm, V.sys,
-                                                 V.partials, V.eps, 0);
+        spmv(V, 0);
         note_launches(V.G.m > 0 ? 4 : 3);
     }
     static void true_res(Survey &V, const int *check)
     {
-        k_true<SP><<<V.grid_rows, kB, 0, V.st>>>(V.nb, mat(V), V.omega, V.b, V.x, V.sys, check,
-                                                 V.partials);
+        k_true<SP><<<V.g_true, kB, 0, V.st>>>(V.nb, mat(V), V.omega, V.b, V.x, V.sys, check,
+                                              V.partials);
         note_launches(1);
     }
-    static void spmv_only(Survey &V)
+    static void spmv_only(Survey &V) { spmv(V, 0); }
+
+    // launch grids: as many blocks as fit on the device at once (grid-stride
+    // loops do the rest), never more than there is work for
+    static int occ(const void *f)
     {
-        k_spmv<SP><<<V.grid_rows, kB, 0, V.st>>>(V.nb, mat(V), V.omega, V.s, V.r, V.z, V.sm, V.sys,
-                                                 V.partials, V.eps, 0);
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, kB, 0) != cudaSuccess || b < 1) b = 1;
+        return b;
+    }
+    static void grids(Survey &V, int nsm)
+    {
+        auto g = [&](const void *f, int work) { return std::max(1, std::min(occ(f) * nsm, work)); };
+        V.g_init = g((const void *)k_init<SP>, V.grid_rows);
+        V.g_node = g((const void *)k_node<SP>, V.grid_nodes);
+        V.g_edge = g((const void *)k_edge<SP>, V.grid_rows);
+        V.g_update = g((const void *)k_update<SP>, V.grid_rows);
+        V.g_true = g((const void *)k_true<SP>, V.grid_rows);
+        const void *fs = V.ch == 2 ? (const void *)k_spmv<SP, 2>
+                         : V.ch == 8 ? (const void *)k_spmv<SP, 8> : (const void *)k_spmv<SP, 4>;
+        V.g_spmv = g(fs, V.grid_rows);
     }
 };
 
@@ -612,11 +672,13 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
     MTGPU_TRY(cudaGetDevice(&dev));
     MTGPU_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     const int rpb = kB / V.SP;
-    V.grid_rows = std::max(1, std::min(ceil_div(V.nb, rpb), nsm * 8));
+    V.grid_rows = std::max(1, ceil_div(V.nb, rpb));
     int rc;
     if ((rc = folded_build_g(mesh, V.G, st))) return rc;
     const int m = V.G.m, mm = std::max(m, 1);
-    V.grid_nodes = std::max(1, std::min(ceil_div(mm, rpb), nsm * 8));
+    V.grid_nodes = std::max(1, ceil_div(mm, rpb));
+    MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+    const int gmax = std::max({V.g_init, V.g_node, V.g_edge, V.g_update, V.g_true, V.g_spmv});
     const size_t nv = (size_t)V.nb * V.SP;
     if ((rc = dev_alloc(&V.kc, P.len_c)) || (rc = dev_alloc(&V.mc, P.len_c)) ||
         (rc = dev_alloc(&V.kr, P.len_r)) || (rc = dev_alloc(&V.da, nv)) ||
@@ -627,7 +689,7 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
         (rc = dev_alloc(&V.s, nv)) || (rc = dev_alloc(&V.p, nv)) || (rc = dev_alloc(&V.a, nv)) ||
         (rc = dev_alloc(&V.z, nv)) || (rc = dev_alloc(&V.w, nv)) || (rc = dev_alloc(&V.sm, nv)) ||
         (rc = dev_alloc(&V.h, (size_t)mm * V.SP)) ||
-        (rc = dev_alloc(&V.partials, (size_t)3 * std::max(V.grid_rows, V.grid_nodes) * V.SP)))
+        (rc = dev_alloc(&V.partials, (size_t)3 * std::max(gmax, nsm * 32) * V.SP)))
         return rc;
     MTGPU_TRY(cudaMallocHost((void **)&V.hsys, sizeof(SysState) * 32));
     std::vector<float2> omdf(32, make_float2(0.f, 0.f));
@@ -666,6 +728,26 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
     MTGPU_TRY(cudaGetLastError());
     MTGPU_TRY(cudaStreamSynchronize(st));
     note_launches(8);
+    // autotune the SpMV slot batch: time each candidate, keep the fastest
+    {
+        const int cand[3] = {2, 4, 8};
+        float best = 1e30f;
+        int best_ch = 4;
+        for (int c = 0; c < 3; c++) {
+            V.ch = cand[c];
+            MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+            float ms = 0.f;
+            if ((rc = survey_spmv_timed(V, 1, &ms))) return rc;   // warm-up
+            if ((rc = survey_spmv_timed(V, 3, &ms))) return rc;
+            V.tune_ms[c] = ms / 3.f;
+            if (ms < best) {
+                best = ms;
+                best_ch = cand[c];
+            }
+        }
+        V.ch = best_ch;
+        MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+    }
     return MTGPU_OK;
 }
 

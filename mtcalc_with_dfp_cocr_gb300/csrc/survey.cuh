@@ -24,7 +24,10 @@ struct Survey {
     const ParamMatrix *P = nullptr;
     cudaStream_t st = nullptr;
     int nb = 0, S = 0, SP = 1;
-    int grid_rows = 0, grid_nodes = 0;
+    int grid_rows = 0, grid_nodes = 0;           // work bounds (blocks that have rows)
+    int g_init = 0, g_node = 0, g_edge = 0, g_update = 0, g_spmv = 0, g_true = 0;  // launch grids
+    int ch = 4;                                  // SpMV slot batch (autotuned at set-up)
+    float tune_ms[3] = {0.f, 0.f, 0.f};          // SpMV times of the batch sizes 2, 4, 8
     Folded G;                                    // pattern of G and G^T
     float2 *kc = nullptr, *mc = nullptr, *kr = nullptr;   // double-float K and M per slot
     float *gv32 = nullptr, *tv32 = nullptr;      // values of G and G^T (+-1/2, exact in FP32)

@@ -185,4 +185,10 @@ def test_dropin_double_float(gpu):
     assert abs(st.iterations - st64.iterations) <= 3
     assert st.true_residual_rel < 1e-8
     assert _true_rel_res(s, x) < 1e-8
-    assert np.linalg.norm(x - x64) <= 1e-6 * np.linalg.norm(x64)
+    # earth and surface edges agree to ~1e-8; air gradient components are
+    # free at ~1e-5 under a 1e-8 residual (see test_gpu_survey)
+    xyz = w.mesh.xyz()
+    e = w.mesh.edges()
+    earth = 0.5 * (xyz[e[:, 0], 2] + xyz[e[:, 1], 2]) <= 0.0
+    c, c64 = x[0::2] + 1j * x[1::2], x64[0::2] + 1j * x64[1::2]
+    assert np.linalg.norm((c - c64)[earth]) <= 1e-7 * np.linalg.norm(c64[earth])
