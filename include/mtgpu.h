@@ -95,6 +95,23 @@ int mtgpu_mult_mv_block_2x2(int nb, const int *ig, const int *jg, const int *idi
                             const int *ijg, const double *di, const double *gg,
                             const double *x, double *y);
 
+/* y = A x on DEVICE buffers, allocating no device memory.  No counterpart in
+ * the reference.  For callers that manage all GPU memory themselves (a
+ * framework's caching allocator, an application that sizes every buffer up
+ * front) and cannot let a library call cudaMalloc/cudaFree, which
+ * synchronise the device and fail once the caller's pool holds the memory.
+ * Same storage and result as mtgpu_mult_mv_block_2x2, 0-based device arrays.
+ * Limit: nb <= 1048576 edges; larger nb returns MTGPU_ERR_ARG.  The work uses
+ * a 16 MiB static device scratch array that every GPU loading the library
+ * holds until exit and that all calls share: calls whose kernels overlap on
+ * the GPU (e.g. on two streams at once) race on it.  The first call on a
+ * device looks the array's address up for that device.  The call only
+ * enqueues work on `stream` (a cudaStream_t, NULL = default stream):
+ * synchronise before reading d_y. */
+int mtgpu_mult_mv_block_2x2_noalloc(int nb, const int *d_ig, const int *d_jg, const int *d_idi,
+                                    const int *d_ijg, const double *d_di, const double *d_gg,
+                                    const double *d_x, double *d_y, void *stream);
+
 /* Folded preconditioner on host buffers: BuildGMatrix + BuildDiagComplex +
  * ApplyPreconditionerComplex (Code/COCR_FP/FoldedPreconditioner.cpp:68-259,
  * 473-574, 578-630).  y = D_A x + G^T D_S G x.  When diag_a (2*nb doubles)

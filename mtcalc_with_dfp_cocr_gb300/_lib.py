@@ -71,6 +71,8 @@ SIGNATURES = {
         C.c_int, C.c_int, C.c_int, _d, _i, _i, _d, _i, _i, _i, _d, _i,
         C.POINTER(SolveOpts), C.POINTER(SolveStats)]),
     "mtgpu_mult_mv_block_2x2": (C.c_int, [C.c_int, _i, _i, _i, _i, _d, _d, _d, _d]),
+    "mtgpu_mult_mv_block_2x2_noalloc": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                                  _vp, _vp]),
     "mtgpu_folded_apply": (C.c_int, [
         C.c_int, _i, _i, _i, _i, _d, _d, C.c_int, C.c_int, _i, _i, _d, _i, _i, _i, _d, _i,
         _d, _d, C.POINTER(C.c_int), _vp, _vp]),

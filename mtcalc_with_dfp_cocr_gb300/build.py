@@ -19,7 +19,8 @@ OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libmtgpu.so")
 EXE = os.path.join(OUT, "mtgpu_cocr_fp")
 
-CU_SOURCES = ["sell.cu", "folded.cu", "cocr.cu", "assemble.cu", "survey.cu", "capi.cu", "capi_assembly.cu"]
+CU_SOURCES = ["sell.cu", "folded.cu", "cocr.cu", "assemble.cu", "survey.cu", "capi.cu", "capi_assembly.cu",
+              "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
