@@ -115,71 +115,88 @@ struct Mat {
 // y = (K + i omega M) x for one (row, system): K x and M x accumulated
 // separately, then combined.  Slots are processed in batches of CH: the
 // batch's column indices and matrix values are loaded first, then all its x
-// gathers are issued together, so CH loads are in flight per thread.
+// gathers are issued together, so CH gathers are in flight per thread.
+// Offsets stay 32-bit inside a row; full batches carry no predicates.
+__device__ __forceinline__ dfc from4(float4 v) { return dfc{df{v.x, v.y}, df{v.z, v.w}}; }
+__device__ __forceinline__ float4 to4(dfc v) { return make_float4(v.re.h, v.re.l, v.im.h, v.im.l); }
+
 template <int SP, int CH>
 __device__ __forceinline__ dfc spmv_row(const Mat &A, int row, int k, df om,
                                         const float4 *__restrict__ x)
 {
-    const int sl = row / kSlice, l = row % kSlice;
+    const int sl = row >> 5, l = row & 31;
+    const float4 *__restrict__ xk = x + k;
     acc kr_, ki_, mr_, mi_;
     {
-        const long long base = A.pc[sl] + l;
+        const long long b0 = A.pc[sl] + l;
+        const int *__restrict__ cc = A.col_c + b0;
+        const float2 *__restrict__ kk = A.kc + b0;
+        const float2 *__restrict__ mm = A.mc + b0;
         const int n = A.wc[sl];
-        for (int q0 = 0; q0 < n; q0 += CH) {
-            int cols[CH];
+        int q = 0;
+        for (; q + CH <= n; q += CH) {
+            int c[CH];
             float2 kv[CH], mv[CH];
             float4 xv[CH];
 #pragma unroll
             for (int j = 0; j < CH; j++) {
-                if (q0 + j < n) {
-                    const long long t = base + (long long)(q0 + j) * kSlice;
-                    cols[j] = A.col_c[t];
-                    kv[j] = A.kc[t];
-                    mv[j] = A.mc[t];
-                }
+                c[j] = __ldg(cc + kSlice * (q + j));
+                kv[j] = __ldg(kk + kSlice * (q + j));
+                mv[j] = __ldg(mm + kSlice * (q + j));
             }
 #pragma unroll
-            for (int j = 0; j < CH; j++)
-                if (q0 + j < n) xv[j] = x[(long long)cols[j] * SP + k];
+            for (int j = 0; j < CH; j++) xv[j] = __ldg(xk + c[j] * SP);
 #pragma unroll
             for (int j = 0; j < CH; j++) {
-                if (q0 + j < n) {
-                    const df kd = d2f(kv[j]), md = d2f(mv[j]);
-                    const df xr{xv[j].x, xv[j].y}, xi{xv[j].z, xv[j].w};
-                    kr_.mac(kd, xr);
-                    ki_.mac(kd, xi);
-                    mr_.mac(md, xr);
-                    mi_.mac(md, xi);
-                }
+                const df kd = d2f(kv[j]), md = d2f(mv[j]);
+                const df xr{xv[j].x, xv[j].y}, xi{xv[j].z, xv[j].w};
+                kr_.mac(kd, xr);
+                ki_.mac(kd, xi);
+                mr_.mac(md, xr);
+                mi_.mac(md, xi);
             }
+        }
+        for (; q < n; q++) {
+            const int c = __ldg(cc + kSlice * q);
+            const df kd = d2f(__ldg(kk + kSlice * q)), md = d2f(__ldg(mm + kSlice * q));
+            const float4 xv = __ldg(xk + c * SP);
+            const df xr{xv.x, xv.y}, xi{xv.z, xv.w};
+            kr_.mac(kd, xr);
+            ki_.mac(kd, xi);
+            mr_.mac(md, xr);
+            mi_.mac(md, xi);
         }
     }
     {
-        const long long base = A.pr[sl] + l;
+        const long long b0 = A.pr[sl] + l;
+        const int *__restrict__ cc = A.col_r + b0;
+        const float2 *__restrict__ kk = A.kr + b0;
         const int n = A.wr[sl];
-        for (int q0 = 0; q0 < n; q0 += CH) {
-            int cols[CH];
-            float2 kv[CH];
-            float4 xv[CH];
+        int q = 0;
+        for (; q + 2 * CH <= n; q += 2 * CH) {
+            int c[2 * CH];
+            float2 kv[2 * CH];
+            float4 xv[2 * CH];
 #pragma unroll
-            for (int j = 0; j < CH; j++) {
-                if (q0 + j < n) {
-                    const long long t = base + (long long)(q0 + j) * kSlice;
-                    cols[j] = A.col_r[t];
-                    kv[j] = A.kr[t];
-                }
+            for (int j = 0; j < 2 * CH; j++) {
+                c[j] = __ldg(cc + kSlice * (q + j));
+                kv[j] = __ldg(kk + kSlice * (q + j));
             }
 #pragma unroll
-            for (int j = 0; j < CH; j++)
-                if (q0 + j < n) xv[j] = x[(long long)cols[j] * SP + k];
+            for (int j = 0; j < 2 * CH; j++) xv[j] = __ldg(xk + c[j] * SP);
 #pragma unroll
-            for (int j = 0; j < CH; j++) {
-                if (q0 + j < n) {
-                    const df kd = d2f(kv[j]);
-                    kr_.mac(kd, df{xv[j].x, xv[j].y});
-                    ki_.mac(kd, df{xv[j].z, xv[j].w});
-                }
+            for (int j = 0; j < 2 * CH; j++) {
+                const df kd = d2f(kv[j]);
+                kr_.mac(kd, df{xv[j].x, xv[j].y});
+                ki_.mac(kd, df{xv[j].z, xv[j].w});
             }
+        }
+        for (; q < n; q++) {
+            const int c = __ldg(cc + kSlice * q);
+            const df kd = d2f(__ldg(kk + kSlice * q));
+            const float4 xv = __ldg(xk + c * SP);
+            kr_.mac(kd, df{xv.x, xv.y});
+            ki_.mac(kd, df{xv.z, xv.w});
         }
     }
     // y = Kx + i omega Mx
@@ -210,10 +227,10 @@ k_init(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict
     for (int row = blockIdx.x * rpb + threadIdx.x / SP; row < nb; row += gridDim.x * rpb) {
         if (!on) continue;
         const long long i = (long long)row * SP + k;
-        const dfc bv = ld(b, i);
-        const dfc rv = csubd(bv, spmv_row<SP, 4>(A, row, k, om, x));
-        st(r, i, rv);
-        st(sm, i, rv);
+        const dfc bv = from4(b[i]);
+        const dfc rv = csubd(bv, spmv_row<SP, 2>(A, row, k, om, x));
+        r[i] = to4(rv);
+        sm[i] = to4(rv);
         nb2.mac(bv.re, bv.re); nb2.mac(bv.im, bv.im);
         nr2.mac(rv.re, rv.re); nr2.mac(rv.im, rv.im);
     }
@@ -251,20 +268,25 @@ k_node(int m, const int *__restrict__ gp, const int *__restrict__ gj, const floa
     const dfc be = from_d2(sys[k].beta);
     const int rpb = kB / SP;
     for (int v = blockIdx.x * rpb + threadIdx.x / SP; v < m; v += gridDim.x * rpb) {
+        const int j0 = __ldg(gp + v), j1 = __ldg(gp + v + 1);
+        const float4 dsv = __ldg(ds + (long long)v * SP + k);
         acc hr, hi;
-        for (int j = gp[v]; j < gp[v + 1]; j++) {
-            const long long idx = (long long)gj[j] * SP + k;
-            dfc an = ld(z, idx);
-            if (use_beta) an = caxpy(an, be, ld(a, idx));
-            hr.macf(an.re, gv[j]);
-            hi.macf(an.im, gv[j]);
+        for (int j = j0; j < j1; j++) {
+            const long long idx = (long long)__ldg(gj + j) * SP + k;
+            const float g = __ldg(gv + j);
+            const float4 zv = __ldg(z + idx);
+            dfc an = from4(zv);
+            if (use_beta) an = caxpy(an, be, from4(__ldg(a + idx)));
+            hr.macf(an.re, g);
+            hi.macf(an.im, g);
         }
-        st(h, (long long)v * SP + k, cmul(dfc{hr.get(), hi.get()}, ld(ds, (long long)v * SP + k)));
+        h[(long long)v * SP + k] = to4(cmul(dfc{hr.get(), hi.get()}, from4(dsv)));
     }
 }
 
 // mode 1: p = s + beta p, a = z + beta a, w = D_A a + G^T h, (a, w) -> alpha
 // mode 0: w = D_A src + G^T h (preconditioner application, no reduction)
+// Every input of an element is loaded before anything is stored.
 template <int SP>
 __global__ void __launch_bounds__(kB)
 k_edge(int n, const int *__restrict__ tp, const int *__restrict__ tj, const float *__restrict__ tv,
@@ -280,25 +302,52 @@ k_edge(int n, const int *__restrict__ tp, const int *__restrict__ tj, const floa
     for (int e = blockIdx.x * rpb + threadIdx.x / SP; e < n; e += gridDim.x * rpb) {
         if (!on) continue;
         const long long idx = (long long)e * SP + k;
+        const int j0 = __ldg(tp + e), j1 = __ldg(tp + e + 1);
+        const float4 srcv = src[idx], dav = __ldg(da + idx);
+        float4 pv = make_float4(0.f, 0.f, 0.f, 0.f), zv = pv, av = pv;
+        if (mode != 0) {
+            pv = p[idx];
+            zv = z[idx];
+            av = a[idx];
+        }
+        float4 hv0 = make_float4(0.f, 0.f, 0.f, 0.f), hv1 = hv0;
+        float t0 = 0.f, t1 = 0.f;
+        if (j1 > j0) {
+            hv0 = __ldg(h + (long long)__ldg(tj + j0) * SP + k);
+            t0 = __ldg(tv + j0);
+        }
+        if (j1 > j0 + 1) {
+            hv1 = __ldg(h + (long long)__ldg(tj + j0 + 1) * SP + k);
+            t1 = __ldg(tv + j0 + 1);
+        }
         dfc an;
         if (mode == 0) {
-            an = ld(src, idx);
+            an = from4(srcv);
         } else {
-            st(p, idx, caxpy(ld(src, idx), be, ld(p, idx)));
-            an = caxpy(ld(z, idx), be, ld(a, idx));
-            st(a, idx, an);
+            p[idx] = to4(caxpy(from4(srcv), be, from4(pv)));
+            an = caxpy(from4(zv), be, from4(av));
+            a[idx] = to4(an);
         }
-        const dfc dv = cmul(an, ld(da, idx));
+        const dfc dv = cmul(an, from4(dav));
         acc wr, wi;
         wr.h = dv.re.h; wr.l = dv.re.l;
         wi.h = dv.im.h; wi.l = dv.im.l;
-        for (int j = tp[e]; j < tp[e + 1]; j++) {
-            const dfc hv = ld(h, (long long)tj[j] * SP + k);
-            wr.macf(hv.re, tv[j]);
-            wi.macf(hv.im, tv[j]);
+        if (j1 > j0) {
+            wr.macf(df{hv0.x, hv0.y}, t0);
+            wi.macf(df{hv0.z, hv0.w}, t0);
+        }
+        if (j1 > j0 + 1) {
+            wr.macf(df{hv1.x, hv1.y}, t1);
+            wi.macf(df{hv1.z, hv1.w}, t1);
+        }
+        for (int j = j0 + 2; j < j1; j++) {       // T-matrix rows only
+            const float4 hv = __ldg(h + (long long)__ldg(tj + j) * SP + k);
+            const float t = __ldg(tv + j);
+            wr.macf(df{hv.x, hv.y}, t);
+            wi.macf(df{hv.z, hv.w}, t);
         }
         const dfc wn{wr.get(), wi.get()};
-        st(w, idx, wn);
+        w[idx] = to4(wn);
         awr.mac(an.re, wn.re);
         awr.mac(neg(an.im), wn.im);
         awi.mac(an.re, wn.im);
@@ -317,7 +366,8 @@ k_edge(int n, const int *__restrict__ tp, const int *__restrict__ tj, const floa
     }
 }
 
-// x += alpha p, r -= alpha a, s -= alpha w; MRS weight from (s_m, r - s_m)
+// x += alpha p, r -= alpha a, s -= alpha w; MRS weight from (s_m, r - s_m).
+// Every input of an element is loaded before anything is stored.
 template <int SP>
 __global__ void __launch_bounds__(kB)
 k_update(int n, const float4 *__restrict__ p, const float4 *__restrict__ a,
@@ -333,13 +383,15 @@ k_update(int n, const float4 *__restrict__ p, const float4 *__restrict__ a,
     for (int e = blockIdx.x * rpb + threadIdx.x / SP; e < n; e += gridDim.x * rpb) {
         if (!on) continue;
         const long long idx = (long long)e * SP + k;
-        st(x, idx, caxpy(ld(x, idx), al, ld(p, idx)));
-        const dfc rn = caxpy(ld(r, idx), nal, ld(a, idx));
-        st(r, idx, rn);
-        st(s, idx, caxpy(ld(s, idx), nal, ld(w, idx)));
-        const dfc sv = ld(sm, idx);
-        const df ur = add(rn.re, neg(sv.re)), ui = add(rn.im, neg(sv.im));
-        su.mac(sv.re, ur); su.mac(sv.im, ui);
+        const float4 pv = __ldg(p + idx), av = __ldg(a + idx), wv = __ldg(w + idx),
+                     smv = __ldg(sm + idx), xv = x[idx], rv = r[idx], sv = s[idx];
+        const dfc rn = caxpy(from4(rv), nal, from4(av));
+        x[idx] = to4(caxpy(from4(xv), al, from4(pv)));
+        r[idx] = to4(rn);
+        s[idx] = to4(caxpy(from4(sv), nal, from4(wv)));
+        const dfc smd = from4(smv);
+        const df ur = add(rn.re, neg(smd.re)), ui = add(rn.im, neg(smd.im));
+        su.mac(smd.re, ur); su.mac(smd.im, ui);
         uu.mac(ur, ur); uu.mac(ui, ui);
     }
     double v[2] = {su.to_double(), uu.to_double()};
@@ -362,7 +414,7 @@ k_update(int n, const float4 *__restrict__ p, const float4 *__restrict__ a,
 // z = A s, MRS update of s_m, ||s_m||, (z, s) -> stop test and beta.
 // mode 0 (set-up): z = A s and (z, s) only.
 template <int SP, int CH>
-__global__ void __launch_bounds__(kB)
+__global__ void __launch_bounds__(kB, 3)
 k_spmv(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict__ s,
        const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
        SysState *sys, double *partials, double eps, int mode)
@@ -377,15 +429,19 @@ k_spmv(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict
     for (int row = blockIdx.x * rpb + threadIdx.x / SP; row < nb; row += gridDim.x * rpb) {
         if (!on) continue;
         const long long i = (long long)row * SP + k;
+        const float4 sv4 = __ldg(s + i);
+        float4 rv4 = make_float4(0.f, 0.f, 0.f, 0.f), smo4 = rv4;
+        if (mm != 0) rv4 = __ldg(r + i);
+        if (mm == 2) smo4 = sm[i];
         const dfc y = spmv_row<SP, CH>(A, row, k, om, s);
-        st(z, i, y);
-        const dfc sv = ld(s, i);
+        z[i] = to4(y);
+        const dfc sv = from4(sv4);
         zsr.mac(y.re, sv.re); zsr.mac(neg(y.im), sv.im);
         zsi.mac(y.re, sv.im); zsi.mac(y.im, sv.re);
         if (mm != 0) {
-            dfc smv = ld(r, i);
+            dfc smv = from4(rv4);
             if (mm == 2) {
-                const dfc old = ld(sm, i);
+                const dfc old = from4(smo4);
                 acc tr, ti;
                 tr.h = old.re.h; tr.l = old.re.l;
                 ti.h = old.im.h; ti.l = old.im.l;
@@ -393,7 +449,7 @@ k_spmv(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict
                 ti.mac(wm, add(smv.im, neg(old.im)));
                 smv = dfc{tr.get(), ti.get()};
             }
-            st(sm, i, smv);
+            sm[i] = to4(smv);
             nn.mac(smv.re, smv.re);
             nn.mac(smv.im, smv.im);
         }
@@ -436,8 +492,8 @@ k_true(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict
     for (int row = blockIdx.x * rpb + threadIdx.x / SP; row < nb; row += gridDim.x * rpb) {
         if (!on) continue;
         const long long i = (long long)row * SP + k;
-        const dfc bv = ld(b, i);
-        const dfc rv = csubd(bv, spmv_row<SP, 4>(A, row, k, om, x));
+        const dfc bv = from4(__ldg(b + i));
+        const dfc rv = csubd(bv, spmv_row<SP, 2>(A, row, k, om, x));
         nb2.mac(bv.re, bv.re); nb2.mac(bv.im, bv.im);
         nr2.mac(rv.re, rv.re); nr2.mac(rv.im, rv.im);
     }
