@@ -10,6 +10,8 @@
 #   COCR_FP      Code/COCR_FP/*.cpp      the reference solver (PCOCR_2x2_Folded)
 #   BuildMatrix  Code/BuildMatrix/*.cpp  the reference SLAE assembly
 #   Harm1D       Code/Harm1D/*.cpp       the reference 1-D normal field
+#   ref_receivers  Code/OutputNu/{T_Brick,OutputArbitrary,For_Solvers,in_out}.cpp
+#                plus ref_receivers_main.cpp: the receiver evaluation
 #
 # Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
 set -euo pipefail
@@ -49,3 +51,24 @@ build_prog() {
 build_prog COCR_FP
 build_prog BuildMatrix -include "$SHIM/llp64.h"
 build_prog Harm1D -include "$SHIM/llp64.h"
+
+# Receiver evaluation (direct path) of Code/OutputNu: four of its sources plus
+# the harness oracle/ref_receivers_main.cpp.  Only those four are compiled: the
+# rest of OutputNu needs MKL PARDISO.
+build_receivers() {
+    local src="$REF/Code/OutputNu"
+    local objdir="$OUT/obj_OutputNu"
+    mkdir -p "$objdir"
+    local flags=("${COMMON[@]}" -I "$SHIM/mkl" -I "$src")
+    local objs=()
+    for n in T_Brick OutputArbitrary For_Solvers in_out; do
+        "$CXX" "${flags[@]}" -c "$src/$n.cpp" -o "$objdir/$n.o" &
+        objs+=("$objdir/$n.o")
+    done
+    "$CXX" "${flags[@]}" -c "$HERE/ref_receivers_main.cpp" -o "$objdir/main.o" &
+    objs+=("$objdir/main.o")
+    wait
+    "$CXX" -fopenmp -o "$OUT/ref_receivers" "${objs[@]}"
+    echo "build_ref: $OUT/ref_receivers"
+}
+build_receivers

@@ -697,3 +697,269 @@ int orc_folded_apply_once(int nb, const int *ig, const int *jg, const int *idi, 
     orc_folded_free(&P);
     return m;
 }
+
+/* ---- receivers and MT responses ------------------------------------------ */
+
+/* Code/OutputNu/OutputArbitrary.cpp:385-500: the reference scans the elements
+ * in index order and keeps, for every receiver, the first whose closed box
+ * (vertex 0 to vertex 7, exact comparisons) holds it. */
+int orc_locate_receivers(int kpar, const int *nver14, const double *xyz, int nrec,
+                         const double *rec, int *elem)
+{
+    int missing = 0;
+    for (int r = 0; r < nrec; r++) {
+        const double *p = rec + 3 * r;
+        elem[r] = -1;
+        for (int e = 0; e < kpar; e++) {
+            const double *lo = xyz + 3 * nver14[14 * e + 0];
+            const double *hi = xyz + 3 * nver14[14 * e + 7];
+            if (p[0] >= lo[0] && p[1] >= lo[1] && p[2] >= lo[2] &&
+                p[0] <= hi[0] && p[1] <= hi[1] && p[2] <= hi[2]) {
+                elem[r] = e;
+                break;
+            }
+        }
+        if (elem[r] < 0) missing++;
+    }
+    return missing;
+}
+
+static double lin0(double t) { return 0.5 * (1.0 - t); }
+static double lin1(double t) { return 0.5 * (1.0 + t); }
+
+/* Lowest-order edge basis on a brick with local coordinates in [-1,1]^3
+ * (T_Brick.cpp:980-1060): edge i of direction d carries the tangential
+ * component (2/h_d) l_a l_b in the two other local coordinates.  The curl
+ * components follow from l0' = -1/2, l1' = +1/2 (T_Brick.cpp:1484-1618,
+ * 1842-1918): each depends on one local coordinate only. */
+void orc_receiver_eval(const int *nver14, const int *ed25, const double *xyz, int nrec,
+                       const double *rec, const int *elem, const double *v3,
+                       double *a, double *curl)
+{
+    for (int r = 0; r < nrec; r++) {
+        double *ar = a + 6 * r, *cr = curl + 6 * r;
+        for (int k = 0; k < 6; k++) ar[k] = cr[k] = 0.0;
+        const int e = elem[r];
+        if (e < 0) continue;
+        const double *lo = xyz + 3 * nver14[14 * e + 0];
+        const double *hi = xyz + 3 * nver14[14 * e + 7];
+        const double hx = hi[0] - lo[0], hy = hi[1] - lo[1], hz = hi[2] - lo[2];
+        const double *p = rec + 3 * r;
+        const double xi = (2.0 * p[0] - lo[0] - hi[0]) / hx;
+        const double et = (2.0 * p[1] - lo[1] - hi[1]) / hy;
+        const double ze = (2.0 * p[2] - lo[2] - hi[2]) / hz;
+        for (int part = 0; part < 2; part++) {
+            double v[12];
+            for (int i = 0; i < 12; i++) v[i] = v3[2 * ed25[25 * e + i] + part];
+            ar[0 + part] = 2.0 / hx * (v[0] * lin0(et) * lin0(ze) + v[1] * lin1(et) * lin0(ze) +
+                                       v[2] * lin0(et) * lin1(ze) + v[3] * lin1(et) * lin1(ze));
+            ar[2 + part] = 2.0 / hy * (v[4] * lin0(ze) * lin0(xi) + v[5] * lin1(ze) * lin0(xi) +
+                                       v[6] * lin0(ze) * lin1(xi) + v[7] * lin1(ze) * lin1(xi));
+            ar[4 + part] = 2.0 / hz * (v[8] * lin0(xi) * lin0(et) + v[9] * lin1(xi) * lin0(et) +
+                                       v[10] * lin0(xi) * lin1(et) + v[11] * lin1(xi) * lin1(et));
+            /* curl_x = dAz/dy - dAy/dz, curl_y = dAx/dz - dAz/dx, curl_z = dAy/dx - dAx/dy */
+            cr[0 + part] = 2.0 / (hy * hz) * (lin0(xi) * (v[4] - v[5] - v[8] + v[10]) +
+                                              lin1(xi) * (v[6] - v[7] - v[9] + v[11]));
+            cr[2 + part] = 2.0 / (hx * hz) * (lin0(et) * (v[2] - v[0] + v[8] - v[9]) +
+                                              lin1(et) * (v[3] - v[1] + v[10] - v[11]));
+            cr[4 + part] = 2.0 / (hx * hy) * (lin0(ze) * (v[0] - v[1] - v[4] + v[6]) +
+                                              lin1(ze) * (v[2] - v[3] - v[5] + v[7]));
+        }
+    }
+}
+
+/* Code/Harm1D/divgrad_1d.cpp:90-138: outside [z1, z_{n-2}] the end slopes;
+ * inside, the node slopes (weighted averages of the two adjacent slopes) at
+ * the ends of the containing interval, interpolated linearly; where one of
+ * them does not exist, the interval's own slope. */
+double orc_dspline(double x, int n, const double *z, const double *v)
+{
+    if (x < z[1]) return (v[1] - v[0]) / (z[1] - z[0]);
+    if (x > z[n - 2]) return (v[n - 1] - v[n - 2]) / (z[n - 1] - z[n - 2]);
+    int i = 1;
+    while (i < n && !(x <= z[i])) i++;
+    double d0 = 0.0, d1 = 0.0;
+    int f0 = 0, f1 = 0;
+    if (i - 1 > 0) {
+        f0 = 1;
+        const double w = (z[i - 1] - z[i - 2]) / (z[i] - z[i - 2]);
+        const double s0 = (v[i - 1] - v[i - 2]) / (z[i - 1] - z[i - 2]);
+        const double s1 = (v[i] - v[i - 1]) / (z[i] - z[i - 1]);
+        d0 = s0 * (1.0 - w) + s1 * w;
+    }
+    if (i + 1 < n) {
+        f1 = 1;
+        const double w = (z[i] - z[i - 1]) / (z[i + 1] - z[i - 1]);
+        const double s0 = (v[i] - v[i - 1]) / (z[i] - z[i - 1]);
+        const double s1 = (v[i + 1] - v[i]) / (z[i + 1] - z[i]);
+        d1 = s0 * (1.0 - w) + s1 * w;
+    }
+    if (f0 && f1) {
+        const double t = (x - z[i - 1]) / (z[i] - z[i - 1]);
+        return (1.0 - t) * d0 + t * d1;
+    }
+    return (v[i] - v[i - 1]) / (z[i] - z[i - 1]);   /* one node slope missing: the interval's */
+}
+
+/* Code/Harm1D/divgrad_1d.cpp:290-330.  b: below the surface the z-derivative
+ * of the 1-D potential, above it the air value B = MU0 (unit H); e: the
+ * potential itself, taken at z = 0 for receivers above the surface. */
+void orc_normal_field(double z, int n1d, const double *z1d, const double *usin,
+                      const double *ucos, int alfa, double omega, double *e, double *b)
+{
+    const double mu = 4.0 * 3.1415926535897932 * 1e-7;   /* Code/Harm1D/divgrad_1d.cpp:288 */
+    const double a = (double)alfa;
+    double ds, dc;
+    if (z < 0.0) {
+        ds = orc_dspline(z, n1d, z1d, usin);
+        dc = orc_dspline(z, n1d, z1d, ucos);
+    } else {
+        ds = mu;
+        dc = 0.0;
+    }
+    b[0] = (a - 1.0) * ds; b[1] = a * ds; b[2] = 0.0;
+    b[3] = (a - 1.0) * dc; b[4] = a * dc; b[5] = 0.0;
+    const double zz = (z > 0.0) ? 0.0 : z;
+    const double us = orc_spline(zz, n1d, z1d, usin);
+    const double uc = orc_spline(zz, n1d, z1d, ucos);
+    e[0] = omega * a * uc;  e[1] = omega * (1.0 - a) * uc; e[2] = 0.0;
+    e[3] = -omega * a * us; e[4] = omega * (a - 1.0) * us; e[5] = 0.0;
+}
+
+#define ORC_MU0 1.25663706143591729e-6   /* Code/OutputNu/stdafx.h:31 */
+
+void orc_receiver_fields(int nrec, const double *a, const double *curl, double omega,
+                         const double *e1d, const double *b1d, double *e, double *h,
+                         double *rho_imp)
+{
+    for (int r = 0; r < nrec; r++) {
+        const double *ar = a + 6 * r, *cr = curl + 6 * r;
+        double *er = e + 6 * r, *hr = h + 6 * r;
+        for (int d = 0; d < 3; d++) {
+            /* E = -i omega A (give_out_vec_mt.cpp:141-165), H = curl A / mu0 (:173-195) */
+            er[2 * d] = omega * ar[2 * d + 1];
+            er[2 * d + 1] = -omega * ar[2 * d];
+            hr[2 * d] = cr[2 * d] / ORC_MU0;
+            hr[2 * d + 1] = cr[2 * d + 1] / ORC_MU0;
+        }
+        /* normal field on x and y (give_out_vec_mt.cpp:58-99, 239-245) */
+        for (int d = 0; d < 2; d++) {
+            er[2 * d] += e1d[6 * r + d];
+            er[2 * d + 1] += e1d[6 * r + 3 + d];
+            hr[2 * d] += b1d[6 * r + d] / ORC_MU0;
+            hr[2 * d + 1] += b1d[6 * r + 3 + d] / ORC_MU0;
+        }
+        /* give_out_vec_mt.cpp:247-264: moduli of the real and imaginary parts */
+        const double ere = sqrt(er[0] * er[0] + er[2] * er[2] + er[4] * er[4]);
+        const double eim = sqrt(er[1] * er[1] + er[3] * er[3] + er[5] * er[5]);
+        const double hre = sqrt(hr[0] * hr[0] + hr[2] * hr[2] + hr[4] * hr[4]);
+        const double him = sqrt(hr[1] * hr[1] + hr[3] * hr[3] + hr[5] * hr[5]);
+        const double ea = sqrt(ere * ere + eim * eim), ha = sqrt(hre * hre + him * him);
+        rho_imp[2 * r] = (ea / ha) * (ea / ha) / (omega * ORC_MU0);
+        rho_imp[2 * r + 1] = ea / ha;   /* |e_abs / h_abs| */
+    }
+}
+
+/* calcimpedance.for:163-171: quadrant rule, then the near-axis overrides in
+ * the reference's order (a later match wins).  Where nothing matches
+ * (both parts exactly 0) the reference keeps the previous value; 0 here. */
+static double mt_phase(double re, double im, int overrides)
+{
+    const double pi = 3.14159265358979323846264;
+    double f = 0.0;
+    if (re > 0.0 && im > 0.0) f = atan(im / re);
+    if (re < 0.0 && im > 0.0) f = atan(im / re) + pi;
+    if (re < 0.0 && im < 0.0) f = atan(im / re) - pi;
+    if (re > 0.0 && im < 0.0) f = atan(im / re);
+    if (overrides) {
+        if (re > 0.0 && fabs(im) < 1e-15) f = 0.0;
+        if (fabs(re) < 1e-15 && im > 0.0) f = pi / 2.0;
+        if (re < 0.0 && fabs(im) < 1e-15) f = pi;
+        if (fabs(re) < 1e-15 && im < 0.0) f = -pi / 2.0;
+    }
+    return f;
+}
+
+/* Determinant of the 3x3 matrix m (row-major) by the rule of Sarrus, as
+ * calcimpedance.for's `minor` (:379-386). */
+static double det3(const double *m)
+{
+    return m[0] * m[4] * m[8] + m[3] * m[7] * m[2] + m[1] * m[5] * m[6] -
+           m[2] * m[4] * m[6] - m[1] * m[3] * m[8] - m[0] * m[5] * m[7];
+}
+
+/* Inverse of a 4x4 matrix by cofactors over the first-row expansion of the
+ * determinant, calcimpedance.for:346-416 (makeQ, determinan). */
+static void inverse4(const double *b, double *q)
+{
+    double cof[16];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+            double m[9];
+            int k = 0;
+            for (int r = 0; r < 4; r++) {
+                if (r == i) continue;
+                for (int c = 0; c < 4; c++)
+                    if (c != j) m[k++] = b[4 * r + c];
+            }
+            cof[4 * i + j] = (((i + j) & 1) ? -1.0 : 1.0) * det3(m);
+        }
+    double det = 0.0;
+    for (int j = 0; j < 4; j++) det += b[j] * cof[j];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) q[4 * j + i] = cof[4 * i + j] / det;
+}
+
+/* calcimpedance.for:125-301.  With complex fields written re + i im, the
+ * real 4x4 system B u = f states E = Z H for both polarisations:
+ * rows (re, im) of polarisation X then Y, unknowns (re, im) of Z_.x, Z_.y. */
+void orc_mt_response(const double *e0, const double *h0, const double *e1, const double *h1,
+                     double omega, double *out)
+{
+    const double pi = 3.14159265358979323846264;
+    const double mu0 = 4.0 * pi * 1e-7;   /* calcimpedance.for:41 */
+    const double deg = 180.0 / pi;
+    double B[16], Q[16];
+    const double *hh[2] = {h0, h1};
+    for (int p = 0; p < 2; p++) {
+        const double hxr = hh[p][0], hxi = hh[p][1], hyr = hh[p][2], hyi = hh[p][3];
+        double *r0 = B + 8 * p, *r1 = B + 8 * p + 4;
+        r0[0] = hxr; r0[1] = -hxi; r0[2] = hyr; r0[3] = -hyi;
+        r1[0] = hxi; r1[1] = hxr;  r1[2] = hyi; r1[3] = hyr;
+    }
+    inverse4(B, Q);
+    double Z[8], W[4];
+    for (int c = 0; c < 3; c++) {   /* right-hand sides: Ex, Ey, Hz */
+        const double f[4] = {c < 2 ? e0[2 * c] : h0[4], c < 2 ? e0[2 * c + 1] : h0[5],
+                             c < 2 ? e1[2 * c] : h1[4], c < 2 ? e1[2 * c + 1] : h1[5]};
+        double u[4];
+        for (int i = 0; i < 4; i++) {
+            u[i] = 0.0;
+            for (int j = 0; j < 4; j++) u[i] += Q[4 * i + j] * f[j];
+        }
+        double *dst = c < 2 ? Z + 4 * c : W;
+        for (int i = 0; i < 4; i++) dst[i] = u[i];
+    }
+    for (int i = 0; i < 8; i++) out[i] = Z[i];
+    for (int i = 0; i < 4; i++) out[8 + i] = W[i];
+    for (int k = 0; k < 4; k++) {
+        const double re = Z[2 * k], im = Z[2 * k + 1];
+        const double m = sqrt(re * re + im * im), f = mt_phase(re, im, 1);
+        out[12 + k] = m;
+        out[16 + k] = -f * deg;
+        out[20 + k] = m * m / (mu0 * omega);
+        out[24 + k] = -2.0 * f * deg;
+    }
+    /* calcimpedance.for:259-276: det Z = Zxx Zyy - Zxy Zyx */
+    const double dre = (Z[0] * Z[6] - Z[1] * Z[7]) - (Z[4] * Z[2] - Z[5] * Z[3]);
+    const double dim = (Z[0] * Z[7] + Z[1] * Z[6]) - (Z[4] * Z[3] + Z[5] * Z[2]);
+    const double zmod = sqrt(sqrt(dre * dre + dim * dim));
+    const double zfi = mt_phase(dre, dim, 0) / 2.0;
+    out[28] = zmod * zmod / (mu0 * omega);
+    out[29] = -2.0 * zfi * deg;
+    for (int k = 0; k < 2; k++) {
+        const double re = W[2 * k], im = W[2 * k + 1];
+        out[30 + k] = sqrt(re * re + im * im);
+        out[32 + k] = -mt_phase(re, im, 1) * deg;
+    }
+}

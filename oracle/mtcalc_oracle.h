@@ -106,6 +106,47 @@ void orc_brick_bc(double hx, double hy, double hz, double *b, double *c);
 /* Linear interpolation of a 1-D table; Code/BuildMatrix/For_Solvers.cpp:236-270. */
 double orc_spline(double x, int n, const double *z, const double *v);
 
+/* ---- receivers and MT responses ------------------------------------------ */
+
+/* Receiver location, Code/OutputNu/OutputArbitrary.cpp:385-500
+ * (FindElemForReceivers): receiver r goes to the lowest-numbered brick whose
+ * closed box [xyz(nver[e][0]), xyz(nver[e][7])] holds it; -1 if none.
+ * Returns the number of receivers left without an element. */
+int orc_locate_receivers(int kpar, const int *nver14, const double *xyz, int nrec,
+                         const double *rec, int *elem);
+
+/* A and curl A of the edge solution v3 ([nb][2] re/im) at the receivers,
+ * Code/OutputNu/T_Brick.cpp:980-1137 (basis, VectorFieldOnPar) and :1842-1918
+ * with :1484-1618 (RotX/Y/ZOnPar).  a, curl: [nrec][3][2]; zero where elem < 0. */
+void orc_receiver_eval(const int *nver14, const int *ed25, const double *xyz, int nrec,
+                       const double *rec, const int *elem, const double *v3,
+                       double *a, double *curl);
+
+/* Derivative of a 1-D table, Code/Harm1D/divgrad_1d.cpp:90-135 (dSpline). */
+double orc_dspline(double x, int n, const double *z, const double *v);
+
+/* 1-D normal field at depth z as Harm1D writes it into e2d / b2d
+ * (divgrad_1d.cpp:290-330): e, b = (x_re, y_re, z_re, x_im, y_im, z_im). */
+void orc_normal_field(double z, int n1d, const double *z1d, const double *usin,
+                      const double *ucos, int alfa, double omega, double *e, double *b);
+
+/* Total receiver fields of Give_out_on_hex (Code/OutputNu/give_out_vec_mt.cpp:
+ * 135-195 and 232-266), direct evaluation, MT task: E = -i omega A + E_1d,
+ * H = curl A / MU_0 + B_1d / MU_0 (normal part on x, y only), and the two
+ * scalars written to `rok` and `impedance`.
+ * e, h: [nrec][3][2]; rho_imp: [nrec][2] (rho, |Z|); e1d, b1d: [nrec][6]. */
+void orc_receiver_fields(int nrec, const double *a, const double *curl, double omega,
+                         const double *e1d, const double *b1d, double *e, double *h,
+                         double *rho_imp);
+
+/* MT responses of one receiver and frequency from the X- and Y-polarisation
+ * fields, Code/calcimpedance/calcimpedance.for:125-301 (in FP64; the
+ * reference computes in FP32).  e0, h0, e1, h1: [3][2] complex (polarisation
+ * X, Y).  out: ORC_MT_RECORD doubles, layout as mtgpu.h's MTGPU_MT_*. */
+#define ORC_MT_RECORD 34
+void orc_mt_response(const double *e0, const double *h0, const double *e1, const double *h1,
+                     double omega, double *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -52,6 +52,14 @@ def lib():
             C.c_int, _i, _i, _i, _i, _d, _d, C.c_int, C.c_int, _i, _i, _d, _i, _i, _i, _d, _i,
             _d, _d, _d, _d]
         L.orc_brick_bc.argtypes = [C.c_double, C.c_double, C.c_double, _d, _d]
+        L.orc_locate_receivers.argtypes = [C.c_int, _i, _d, C.c_int, _d, _i]
+        L.orc_receiver_eval.argtypes = [_i, _i, _d, C.c_int, _d, _i, _d, _d, _d]
+        L.orc_dspline.restype = C.c_double
+        L.orc_dspline.argtypes = [C.c_double, C.c_int, _d, _d]
+        L.orc_normal_field.argtypes = [C.c_double, C.c_int, _d, _d, _d, C.c_int, C.c_double,
+                                       _d, _d]
+        L.orc_receiver_fields.argtypes = [C.c_int, _d, _d, C.c_double, _d, _d, _d, _d, _d]
+        L.orc_mt_response.argtypes = [_d, _d, _d, _d, C.c_double, _d]
         _lib = L
     return _lib
 
@@ -134,3 +142,72 @@ def assemble(m, nu, alfa, z1d, usin, ucos, eps=1e-8, maxiter=10000):
                    float(nu), int(alfa), len(z1d), c64(z1d), c64(usin), c64(ucos),
                    m.kuzlov, len(bnd), bnd, ig, jg, idi, ijg, di, gg, pr)
     return BlockSLAE(nb, ig, jg, idi, ijg, di, gg, pr, eps, maxiter)
+
+
+# ---- receivers and MT responses ---------------------------------------------
+
+MT_RECORD = 34
+
+
+def locate_receivers(m, rec):
+    """First element (index order) whose closed box holds each receiver."""
+    nver = np.zeros((m.kpar, 14), np.int32)
+    nver[:, :8] = m.cell_nodes()
+    rec = c64(rec)
+    elem = np.empty(len(rec), np.int32)
+    lib().orc_locate_receivers(m.kpar, nver, c64(m.xyz()), len(rec), rec, elem)
+    return elem
+
+
+def receiver_eval(m, rec, v3, elem=None):
+    """A and curl A at the receivers: two (R, 3) complex arrays."""
+    rec = c64(rec)
+    if elem is None:
+        elem = locate_receivers(m, rec)
+    nver = np.zeros((m.kpar, 14), np.int32)
+    nver[:, :8] = m.cell_nodes()
+    ed = np.zeros((m.kpar, 25), np.int32)
+    ed[:, :12] = m.cell_edges()
+    v = c64(np.asarray(v3).view(np.float64) if np.iscomplexobj(v3) else v3)
+    a = np.zeros(6 * len(rec))
+    curl = np.zeros(6 * len(rec))
+    lib().orc_receiver_eval(nver, ed, c64(m.xyz()), len(rec), rec, c32(elem), v, a, curl)
+    return a.view(np.complex128).reshape(-1, 3), curl.view(np.complex128).reshape(-1, 3)
+
+
+def dspline(x, z, v):
+    return lib().orc_dspline(float(x), len(z), c64(z), c64(v))
+
+
+def normal_field(rec, z1d, usin, ucos, alfa, omega):
+    """e2d / b2d rows (R, 6) of the 1-D field at the receivers."""
+    rec = np.asarray(rec, np.float64)
+    e = np.zeros((len(rec), 6))
+    b = np.zeros((len(rec), 6))
+    for r in range(len(rec)):
+        er, br = np.zeros(6), np.zeros(6)
+        lib().orc_normal_field(float(rec[r, 2]), len(z1d), c64(z1d), c64(usin), c64(ucos),
+                               int(alfa), float(omega), er, br)
+        e[r], b[r] = er, br
+    return e, b
+
+
+def receiver_fields(a, curl, omega, e1d, b1d):
+    """Total E, H (R, 3) complex and the (rho, |Z|) scalars (R, 2)."""
+    R = len(a)
+    e = np.zeros(6 * R)
+    h = np.zeros(6 * R)
+    s = np.zeros(2 * R)
+    lib().orc_receiver_fields(R, c64(np.asarray(a, np.complex128).view(np.float64)),
+                              c64(np.asarray(curl, np.complex128).view(np.float64)),
+                              float(omega), c64(e1d), c64(b1d), e, h, s)
+    return e.view(np.complex128).reshape(R, 3), h.view(np.complex128).reshape(R, 3), \
+        s.reshape(R, 2)
+
+
+def mt_response(e0, h0, e1, h1, omega):
+    """MT_RECORD doubles from the X- and Y-polarisation fields (3 complex each)."""
+    out = np.zeros(MT_RECORD)
+    f = lambda v: c64(np.asarray(v, np.complex128).view(np.float64))
+    lib().orc_mt_response(f(e0), f(h0), f(e1), f(h1), float(omega), out)
+    return out
