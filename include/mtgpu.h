@@ -258,6 +258,61 @@ int mtgpu_survey_spmv_timed(mtgpu_survey *s, int reps, float *ms);
 
 void mtgpu_survey_destroy(mtgpu_survey *s);
 
+/* ------------------------------------------------------------------------
+ * Receivers and MT responses.  Replaces the direct-evaluation output of
+ * Code/OutputNu (Give_out_vec_mt::Give_out_on_hex, give_out_vec_mt.cpp:
+ * 101-266, with OutputVect3d::OutputFieldAtReceivers, OutputArbitrary.cpp:
+ * 202-293) and the impedance program Code/calcimpedance/calcimpedance.for:
+ * 125-301.  Everything is FP64 on the device; the reference's impedance step
+ * is FP32.
+ * ---------------------------------------------------------------------- */
+typedef struct mtgpu_receivers_s mtgpu_receivers;
+
+/* Locates nrec receivers xyz_rec[nrec][3] (host) in the assembly's mesh: each
+ * goes to the lowest-numbered brick whose closed box holds it
+ * (OutputArbitrary.cpp:385-500).  Receivers outside the mesh get element -1
+ * and only the 1-D normal field. */
+int mtgpu_receivers_create(const mtgpu_assembly *a, int nrec, const double *xyz_rec,
+                           mtgpu_receivers **out);
+
+/* nrec, receivers without an element, and (if elem != NULL) the element of
+ * every receiver (host [nrec]). */
+int mtgpu_receivers_info(const mtgpu_receivers *r, int *nrec, int *n_unlocated, int *elem);
+
+/* Total fields of S systems at the receivers: E = -i omega A + E_1d and
+ * H = curl A / MU_0 + H_1d, the 1-D part on x and y only, with A the
+ * anomalous potential d_x [S][2 nb] (device, re/im interleaved, e.g. the
+ * solutions of mtgpu_survey_solve).  nu[S] [Hz], alfa[S] (1: x, 0: y) and the
+ * 1-D tables (z1d[n1d] ascending, usin/ucos [S][n1d], host) are those given to
+ * mtgpu_assembly_rhs; the 1-D field at the receiver depth follows Harm1D's
+ * e2d / b2d (Code/Harm1D/divgrad_1d.cpp:290-330).  Device outputs:
+ * d_e, d_h [S][nrec][3] complex (re, im); d_rho_imp [S][nrec][2]: the
+ * reference's scalar rho and |Z| of `rok` / `impedance`
+ * (give_out_vec_mt.cpp:247-264). */
+int mtgpu_receivers_fields(mtgpu_receivers *r, int S, const double *nu, const int *alfa, int n1d,
+                           const double *z1d, const double *usin, const double *ucos,
+                           const double *d_x, double *d_e, double *d_h, double *d_rho_imp);
+
+/* One MT response record (doubles) per frequency and receiver: */
+#define MTGPU_MT_Z 0         /* Zxx, Zxy, Zyx, Zyy as (re, im): 8            */
+#define MTGPU_MT_W 8         /* tipper Wzx, Wzy as (re, im): 4               */
+#define MTGPU_MT_ZABS 12     /* |Z..|: 4                                     */
+#define MTGPU_MT_ZPHASE 16   /* -arg Z.. in degrees (files Fxx ...): 4       */
+#define MTGPU_MT_RHO 20      /* |Z..|^2 / (omega mu0) (files Rxx ...): 4     */
+#define MTGPU_MT_RHOPHASE 24 /* -2 arg Z.. in degrees (files Fixx ...): 4    */
+#define MTGPU_MT_RHOEFF 28   /* |det Z| / (omega mu0), -arg det Z degrees: 2 */
+#define MTGPU_MT_WABS 30     /* |Wz.|: 2, then -arg Wz. in degrees: 2        */
+#define MTGPU_MT_RECORD 34
+
+/* MT responses of nf frequencies nu[nf] [Hz]: sys_x[f] / sys_y[f] index the
+ * X- and Y-polarisation systems (0 <= index < S) of d_e, d_h [S][nrec][3]
+ * from mtgpu_receivers_fields.  d_out: device [nf][nrec][MTGPU_MT_RECORD]. */
+int mtgpu_mt_response(mtgpu_receivers *r, int nf, const double *nu, const int *sys_x,
+                      const int *sys_y, int S, const double *d_e, const double *d_h,
+                      double *d_out);
+
+void mtgpu_receivers_destroy(mtgpu_receivers *r);
+
 #ifdef __cplusplus
 }
 #endif

@@ -100,6 +100,12 @@ SIGNATURES = {
                                      C.POINTER(SurveyStats)]),
     "mtgpu_survey_spmv_timed": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_float)]),
     "mtgpu_survey_destroy": (None, [_vp]),
+    "mtgpu_receivers_create": (C.c_int, [_vp, C.c_int, _d, C.POINTER(_vp)]),
+    "mtgpu_receivers_info": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), _vp]),
+    "mtgpu_receivers_fields": (C.c_int, [_vp, C.c_int, _d, _i, C.c_int, _d, _d, _d, _vp, _vp,
+                                         _vp, _vp]),
+    "mtgpu_mt_response": (C.c_int, [_vp, C.c_int, _d, _i, _i, C.c_int, _vp, _vp, _vp]),
+    "mtgpu_receivers_destroy": (None, [_vp]),
 }
 
 _lib = None

@@ -4,6 +4,8 @@
 #pragma once
 #include "mtgpu_internal.cuh"
 
+#include <vector>
+
 namespace mtgpu {
 
 struct ParamMatrix {
@@ -48,3 +50,14 @@ int param_from_sell(const SellMatrix &A, ParamMatrix &P, cudaStream_t st);
 int exclusive_scan_host(const int *d_in, int n, int *d_out, long long *total, cudaStream_t st);
 
 }  // namespace mtgpu
+
+// opaque handle of the device assembly (include/mtgpu.h)
+struct mtgpu_assembly_s {
+    mtgpu::ParamMatrix P;
+    cudaStream_t st = nullptr;
+    // host copies of what the folded preconditioner set-up reads
+    std::vector<int> nver, nvkat, edges, bound;
+    std::vector<double> sigflag;
+    std::vector<int> ig_t;
+    int nver_stride = 14;
+};

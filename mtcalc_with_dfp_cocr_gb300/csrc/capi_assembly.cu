@@ -5,16 +5,6 @@
 
 using namespace mtgpu;
 
-struct mtgpu_assembly_s {
-    ParamMatrix P;
-    cudaStream_t st = nullptr;
-    // host copies of what the folded preconditioner set-up reads
-    std::vector<int> nver, nvkat, edges, bound;
-    std::vector<double> sigflag;
-    std::vector<int> ig_t;
-    int nver_stride = 14;
-};
-
 namespace {
 constexpr double kTwoPi = 2.0 * 3.1415926535897932384626433832795;   // BuildMatrix/stdafx.h:32
 

@@ -53,3 +53,15 @@ def test_argument_errors_without_gpu(lib):
     rc = lib.mtgpu_mult_mv_block_2x2(2, ig, jg, idi, ijg, d, d, d, d)
     assert rc == _lib.MTGPU_ERR_ARG
     assert "lower" in _lib.last_error()
+
+
+def test_receiver_argument_errors_without_gpu(lib):
+    from mtcalc_with_dfp_cocr_gb300 import _lib
+    pts = np.zeros(3)
+    out = C.c_void_p()
+    assert lib.mtgpu_receivers_create(None, 1, pts, C.byref(out)) == _lib.MTGPU_ERR_ARG
+    assert "null" in _lib.last_error()
+    assert lib.mtgpu_receivers_info(None, None, None, None) == _lib.MTGPU_ERR_ARG
+    i1 = np.zeros(1, np.int32)
+    d1 = np.ones(1)
+    assert lib.mtgpu_mt_response(None, 1, d1, i1, i1, 1, None, None, None) == _lib.MTGPU_ERR_ARG
