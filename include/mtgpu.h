@@ -313,6 +313,36 @@ int mtgpu_mt_response(mtgpu_receivers *r, int nf, const double *nu, const int *s
 
 void mtgpu_receivers_destroy(mtgpu_receivers *r);
 
+/* ------------------------------------------------------------------------
+ * Adjoint gradient of the impedance misfit
+ *   J = sum_{f, r} sum_{i, j in {x, y}} |Z_ij - Zobs_ij|^2
+ * with respect to the log-conductivity of every cell.  No reference
+ * counterpart: the reference computes forward responses only.
+ * ---------------------------------------------------------------------- */
+
+/* The adjoint right-hand sides d_src [S][2 nb] (device, zero except on the
+ * receivers' bricks) = dJ/du for the anomalous potentials u of the S systems
+ * (dJ = 2 Re sum_k d_src_k^T du_k), from the fields d_e, d_h of
+ * mtgpu_receivers_fields and the observed impedances d_zobs (device,
+ * [nf][nrec][4] complex: Zxx, Zxy, Zyx, Zyy).  Frequencies nu[nf], systems
+ * sys_x[f] / sys_y[f] as in mtgpu_mt_response; every system belongs to one
+ * frequency at most.  *misfit (if not NULL) receives J. */
+int mtgpu_adjoint_source(mtgpu_receivers *r, int nf, const double *nu, const int *sys_x,
+                         const int *sys_y, int S, const double *d_e, const double *d_h,
+                         const double *d_zobs, double *d_src, double *misfit);
+
+/* d_grad[kpar] (device) = dJ / d ln(sigma_c) for every cell c, from the
+ * forward solutions d_u and the adjoint solutions d_lambda (both [S][2 nb]
+ * device; A lambda_k = src_k, A being complex symmetric) of the systems
+ * nu[S], alfa[S] with the 1-D tables given to mtgpu_assembly_rhs:
+ *   grad_c = sigma_c sum_k -2 Re(lambda_k^T i omega_k P C_c (u_k + a0_k))
+ * with C_c the cell's mass matrix, P the non-Dirichlet rows and a0_k the 1-D
+ * potential as edge values.  sigma_c is the conductivity of the cell's
+ * material: with one material per cell this is the per-cell gradient. */
+int mtgpu_adjoint_gradient(mtgpu_assembly *a, int S, const double *nu, const int *alfa, int n1d,
+                           const double *z1d, const double *usin, const double *ucos,
+                           const double *d_u, const double *d_lambda, double *d_grad);
+
 #ifdef __cplusplus
 }
 #endif

@@ -21,22 +21,30 @@ MU_0 = 1.25663706143591729e-6   # Code/BuildMatrix/stdafx.h:31
 
 
 class Assembly:
-    def __init__(self, mesh):
-        """mesh: a RegularMesh (mesh.py)."""
+    def __init__(self, mesh, cell_sigma=None):
+        """mesh: a RegularMesh (mesh.py).  cell_sigma: optional conductivity
+        of every cell (unrounded); then every cell is its own material, with
+        the mesh's background conductivity as its sigma0."""
         L = _lib.lib()
         nver = np.ascontiguousarray(mesh.cell_nodes(), np.int32)
         ed = np.ascontiguousarray(mesh.cell_edges(), np.int32)
+        if cell_sigma is None:
+            nvkat, sig, sig0 = mesh.nvkat, mesh.mat_sigma, mesh.mat_sigma0
+        else:
+            sig = np.asarray(cell_sigma, np.float64).reshape(mesh.kpar)
+            nvkat = np.arange(mesh.kpar, dtype=np.int32)
+            sig0 = mesh.cell_sigma0
         self._arrays = dict(
             xyz=np.ascontiguousarray(mesh.xyz(), np.float64), nver=nver, ed=ed,
             edges=np.ascontiguousarray(mesh.edges(), np.int32),
-            nvkat=np.ascontiguousarray(mesh.nvkat, np.int32),
-            mu=np.full(len(mesh.mat_sigma), MU_0),
-            sigma=np.ascontiguousarray(mesh.mat_sigma, np.float64),
-            sigma0=np.ascontiguousarray(mesh.mat_sigma0, np.float64),
+            nvkat=np.ascontiguousarray(nvkat, np.int32),
+            mu=np.full(len(sig), MU_0),
+            sigma=np.ascontiguousarray(sig, np.float64),
+            sigma0=np.ascontiguousarray(sig0, np.float64),
             bound=np.ascontiguousarray(mesh.boundary_nodes(), np.int32))
         a = self._arrays
         p = lambda k: a[k].ctypes.data_as(C.c_void_p)
-        fm = _lib.FemMesh(mesh.kuzlov, mesh.kpar, mesh.nb, len(mesh.mat_sigma), p("xyz"), p("nver"),
+        fm = _lib.FemMesh(mesh.kuzlov, mesh.kpar, mesh.nb, len(a["sigma"]), p("xyz"), p("nver"),
                           8, p("ed"), 12, p("edges"), p("nvkat"), p("mu"), None, p("sigma"),
                           p("sigma0"), None, None, len(a["bound"]), p("bound"))
         h = C.c_void_p()

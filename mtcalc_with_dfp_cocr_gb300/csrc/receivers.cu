@@ -9,7 +9,7 @@
 // kernel runs in FP64 with one thread per (receiver, system) or (receiver,
 // frequency); the only sizeable step is the one-off receiver location, a
 // scan of all bricks against the receiver list staged in shared memory.
-#include "assemble.cuh"
+#include "receivers.cuh"
 
 #include <climits>
 #include <cmath>
@@ -322,35 +322,10 @@ __global__ void k_mt_response(int nrec, int nf, const double *__restrict__ omega
     }
 }
 
-// grow-only device buffer
-template <class T>
-int ensure(T **p, size_t *cap, size_t n)
-{
-    if (n <= *cap && *p) return MTGPU_OK;
-    dev_free(*p);
-    *cap = 0;
-    int rc = dev_alloc(p, n);
-    if (rc) return rc;
-    *cap = n;
-    return MTGPU_OK;
-}
-
 }  // namespace
 }  // namespace mtgpu
 
 using namespace mtgpu;
-
-struct mtgpu_receivers_s {
-    cudaStream_t st = nullptr;
-    int nrec = 0, nb = 0, n_unlocated = 0;
-    int *d_elem = nullptr, *d_edge = nullptr;
-    double4 *d_loc = nullptr, *d_h = nullptr;
-    std::vector<int> elem;
-    // per-call inputs (grow-only)
-    double *d_omega = nullptr, *d_tab = nullptr;
-    int *d_int = nullptr;
-    size_t cap_omega = 0, cap_tab = 0, cap_int = 0;
-};
 
 extern "C" {
 
@@ -365,6 +340,11 @@ void mtgpu_receivers_destroy(mtgpu_receivers *r)
     dev_free(r->d_omega);
     dev_free(r->d_tab);
     dev_free(r->d_int);
+    dev_free(r->d_contrib);
+    dev_free(r->d_misfit);
+    dev_free(r->d_touch_ptr);
+    dev_free(r->d_touch_edge);
+    dev_free(r->d_touch_slot);
     if (r->st) cudaStreamDestroy(r->st);
     delete r;
 }

@@ -65,3 +65,14 @@ def test_receiver_argument_errors_without_gpu(lib):
     i1 = np.zeros(1, np.int32)
     d1 = np.ones(1)
     assert lib.mtgpu_mt_response(None, 1, d1, i1, i1, 1, None, None, None) == _lib.MTGPU_ERR_ARG
+
+
+def test_adjoint_argument_errors_without_gpu(lib):
+    from mtcalc_with_dfp_cocr_gb300 import _lib
+    i1 = np.zeros(1, np.int32)
+    d1 = np.ones(1)
+    J = C.c_double()
+    rc = lib.mtgpu_adjoint_source(None, 1, d1, i1, i1, 2, None, None, None, None, C.byref(J))
+    assert rc == _lib.MTGPU_ERR_ARG
+    rc = lib.mtgpu_adjoint_gradient(None, 1, d1, i1, 2, d1, d1, d1, None, None, None)
+    assert rc == _lib.MTGPU_ERR_ARG
