@@ -374,6 +374,129 @@ def reference_arm(args):
     print(json.dumps(out), flush=True)
 
 
+def survey_run(args):
+    """A whole survey in one batch (--survey WORKLOAD, default c2s: the c2
+    mesh under 16 frequencies x 2 polarisations = 32 systems): the batched
+    double-float solver against the plain FP64 COCR on every system, and the
+    impedance tensor, apparent resistivity and phase of both at the
+    receivers, with the batched solver's error against FP64 per result."""
+    import torch
+    from mtcalc_with_dfp_cocr_gb300 import _lib, assembly, receivers, survey, workloads
+    from mtcalc_with_dfp_cocr_gb300 import build as B
+    B.build()
+    torch.cuda.set_device(0)
+    w = workloads.make(args.survey)
+    systems = w.systems
+    S = len(systems)
+    tables = make_inputs(w)
+    nb = w.mesh.nb
+    nus = [f for f, _ in systems]
+    alfas = [a for _, a in systems]
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    A = assembly.Assembly(w.mesh)
+    z1d = tables[nus[0]][0]
+    us = np.stack([tables[f][1] for f in nus])
+    uc = np.stack([tables[f][2] for f in nus])
+    rhs = torch.empty(S, 2 * nb, dtype=torch.float64, device="cuda")
+    A.rhs(nus, alfas, z1d, us, uc, rhs)
+    eps, maxiter = 1e-8, 50000
+    xb = torch.zeros_like(rhs)
+    res = {}
+
+    def step_batched():
+        sv = survey.Survey(A, nus, stream)
+        xb.zero_()
+        code, st = sv.solve(rhs, xb, eps=eps, maxiter=maxiter, verify=True)
+        if code != 0:
+            raise RuntimeError(f"survey solve failed: {st}")
+        res["batched"] = st
+        sv.close()
+
+    def timed(fn, steps):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    for _ in range(args.warmup):
+        step_batched()
+    l0 = _lib.kernel_launches()
+    with ClockSampler(0) as clk:
+        ms_b = timed(step_batched, args.steps)
+    launches = _lib.kernel_launches() - l0
+    t_b = ms_b / 1e3 / (args.steps * S)
+
+    x64 = torch.zeros_like(rhs)
+    plain = {}
+
+    def step_plain():
+        for k, (f, a) in enumerate(systems):
+            ctx = A.cocr(f, stream)
+            x64[k].zero_()
+            code, st = ctx.solve(rhs[k], x64[k], eps=eps, maxiter=maxiter,
+                                 stop_on_true_residual=True)
+            ctx.close()
+            if code != 0:
+                raise RuntimeError(f"FP64 solve of system {k} failed with code {code}")
+            plain[k] = (st.iterations, st.true_residual_rel)
+
+    ms_p = timed(step_plain, 1)
+    t_p = ms_p / 1e3 / S
+
+    # impedances of both
+    R = receivers.Receivers(A, w.receivers)
+    freqs = sorted(set(nus))
+    sx = [next(k for k, (f, a) in enumerate(systems) if f == nu and a == 1) for nu in freqs]
+    sy = [next(k for k, (f, a) in enumerate(systems) if f == nu and a == 0) for nu in freqs]
+    outs = []
+    for x in (xb, x64):
+        E, H, _ = R.fields(x, nus, alfas, z1d, us, uc)
+        outs.append(R.mt_response(freqs, sx, sy, E, H).cpu().numpy())
+    ob, o64 = outs
+    zb = ob[..., 0:8].reshape(len(freqs), -1, 4, 2)
+    z64 = o64[..., 0:8].reshape(len(freqs), -1, 4, 2)
+    zb = zb[..., 0] + 1j * zb[..., 1]
+    z64 = z64[..., 0] + 1j * z64[..., 1]
+    off = [1, 2]   # Zxy, Zyx
+    zerr = np.abs(zb - z64)[..., off] / np.abs(z64)[..., off]
+    # the diagonal components, relative to the off-diagonal scale
+    dscale = np.abs(z64)[..., off].max(axis=-1)
+    derr = np.abs(zb - z64)[..., [0, 3]] / dscale[..., None]
+    rho_err = np.abs(ob[..., 21:23] - o64[..., 21:23]) / np.abs(o64[..., 21:23])
+    ph = np.abs(ob[..., 17:19] - o64[..., 17:19]) % 360.0
+    ph_err = np.minimum(ph, 360.0 - ph)
+    lab = lambda f, a: f"{f:.4g}Hz/{'XY'[1 - a]}"
+    per_freq = {f"{nu:.4g}Hz": {"Z_offdiag_rel_max": float(zerr[i].max()),
+                                "Z_diag_rel_to_offdiag_max": float(derr[i].max()),
+                                "rho_a_rel_max": float(rho_err[i].max()),
+                                "phase_deg_max": float(ph_err[i].max())}
+                for i, nu in enumerate(freqs)}
+    out = {
+        "survey": args.survey, "systems": S, "nb": nb, "receivers": len(w.receivers),
+        "steps": args.steps, "warmup": args.warmup,
+        "batched_s_per_solve": t_b, "batched_ms_per_survey": ms_b / args.steps,
+        "plain_fp64_s_per_solve": t_p, "plain_fp64_ms_per_survey": ms_p,
+        "speedup": t_p / t_b,
+        "iterations_batched": {lab(f, a): it for (f, a), it in zip(systems, res["batched"]["iterations"])},
+        "iterations_fp64": {lab(f, a): plain[k][0] for k, (f, a) in enumerate(systems)},
+        "true_rel_res_batched_max": max(res["batched"]["true_residual_rel"]),
+        "true_rel_res_fp64_max": max(v[1] for v in plain.values()),
+        "impedance_error_vs_fp64": {
+            "Z_offdiag_rel_max": float(zerr.max()), "Z_diag_rel_to_offdiag_max": float(derr.max()),
+            "rho_a_rel_max": float(rho_err.max()), "phase_deg_max": float(ph_err.max()),
+            "per_frequency": per_freq},
+        "gpu_launches": int(launches), "clocks": clk.summary(),
+    }
+    print(json.dumps(out), flush=True)
+    R.close()
+    A.close()
+
+
 def profile_run(args):
     """A short fixed run for ncu: the device assembly, one COCR context,
     10 SpMV launches and 30 COCR iterations (ends with the iteration-limit
@@ -425,7 +548,14 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="short fixed run for ncu captures (see profile_run)")
     ap.add_argument("--workload", default=None, help="workload of --profile (default c3)")
+    ap.add_argument("--survey", default=None, metavar="WORKLOAD",
+                    help="time a whole survey in one batch (e.g. c2s, c3); see survey_run")
     args = ap.parse_args()
+    if args.survey:
+        args.steps = min(args.steps, 1) if args.steps else 1
+        args.warmup = min(args.warmup, 1)
+        survey_run(args)
+        return
     if args.profile:
         args.workload = args.workload or "c3"
         profile_run(args)

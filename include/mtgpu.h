@@ -74,7 +74,8 @@ typedef struct {
     /* iterations per CUDA-graph launch between host status checks (0: 16) */
     int iterations_per_launch;
     /* 1: run the same algorithm in double-float arithmetic on the FP32 pipes
-     * (the batched survey solver with one system); 0: FP64 arithmetic. */
+     * (the batched survey solver with one system; if its smoothed residual
+     * stalls, the system is solved again in FP64 from x = 0); 0: FP64. */
     int double_float;
 } mtgpu_solve_opts;
 
@@ -226,16 +227,23 @@ void mtgpu_assembly_destroy(mtgpu_assembly *a);
  * COCR + folded preconditioner + MRS stop test per system.  The arithmetic is
  * double-float (pairs of FP32 numbers, 48-bit significand) on the FP32
  * pipes, which GB300 runs at 64x its FP64 rate; the iteration follows the
- * FP64 algorithm iteration for iteration.  No counterpart in the reference,
+ * FP64 algorithm iteration for iteration.  The solution is accumulated in
+ * FP64 (group updates every 16 iterations) and true residuals are evaluated
+ * in FP64 from the FP64 matrix.  A system the double-float iteration cannot
+ * finish (its smoothed residual stalls: very low frequencies on fine meshes,
+ * where omega sigma_air is ~1e-13 of the curl-curl scale) is solved again by
+ * the FP64 COCR from x = 0.  No counterpart in the reference,
  * which solves the systems one by one in FP64.
  * ---------------------------------------------------------------------- */
 typedef struct mtgpu_survey_s mtgpu_survey;
 
 typedef struct {
     int status[32];               /* MTGPU_OK / MTGPU_MAXITER / ... per system   */
-    int iterations[32];           /* the reference's iteration count per system */
+    int iterations[32];           /* double-float iterations per system         */
     int verifications[32];        /* true-residual evaluations per system       */
+    int fp64_iterations[32];      /* iterations of the FP64 re-solve (0: none)  */
     double true_residual_rel[32]; /* final ||b - A x|| / ||b|| per system        */
+    double residual_rel[32];      /* last smoothed (stop-test) residual per system */
     double seconds;               /* host wall time of the solve                 */
 } mtgpu_survey_stats;
 
@@ -248,7 +256,8 @@ int mtgpu_survey_create(mtgpu_assembly *a, int S, const double *nu, void *stream
  * d_x: device [S][2 nb] initial guesses in, solutions out.  Each system stops
  * when its MRS-smoothed relative residual is below eps (the reference rule,
  * Code/COCR_FP/rci.cpp:66-75); with verify = 1 it then also continues until
- * ||b - A x|| / ||b|| < eps.  maxiter: per-system iteration limit. */
+ * ||b - A x|| / ||b|| < eps.  maxiter: per-system iteration limit (double-float
+ * and FP64 re-solve iterations together). */
 int mtgpu_survey_solve(mtgpu_survey *s, const double *d_b, double *d_x, double eps, int maxiter,
                        int verify, mtgpu_survey_stats *stats);
 

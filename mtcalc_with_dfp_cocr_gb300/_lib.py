@@ -51,7 +51,8 @@ class FemMesh(C.Structure):
 
 class SurveyStats(C.Structure):
     _fields_ = [("status", C.c_int * 32), ("iterations", C.c_int * 32),
-                ("verifications", C.c_int * 32), ("true_residual_rel", C.c_double * 32),
+                ("verifications", C.c_int * 32), ("fp64_iterations", C.c_int * 32),
+                ("true_residual_rel", C.c_double * 32), ("residual_rel", C.c_double * 32),
                 ("seconds", C.c_double)]
 
 

@@ -354,10 +354,25 @@ int mtgpu_pcocr_2x2_folded_ex(int n, const int *ig, const int *jg, const int *id
     const int nb = n / 2;
     MTGPU_CHECK_ARG(n_edges_c == nb, "n_edges_c must equal n/2 (all edges are unknowns)");
     const double t0 = now_s();
-    if (opts && opts->double_float)
-        return solve_double_float_host(nb, ig, jg, idi, ijg, di, gg, pr, x, eps, maxiter, kpar,
-                                n_nodes_c, nvkat, nver14, sigma3d, edges2, ig_t, jg_t, gg_t,
-                                is_node_bound, opts->stop_on_true_residual, stats);
+    int df_iters = 0;
+    if (opts && opts->double_float) {
+        mtgpu_solve_stats sd{};
+        const int r = solve_double_float_host(nb, ig, jg, idi, ijg, di, gg, pr, x, eps, maxiter,
+                                              kpar, n_nodes_c, nvkat, nver14, sigma3d, edges2,
+                                              ig_t, jg_t, gg_t, is_node_bound,
+                                              opts->stop_on_true_residual, &sd);
+        // a system the double-float iteration cannot finish (its smoothed
+        // residual stalls) is solved again in FP64 from x = 0: the stalled
+        // iterate's errors in the air's gradient components are not a start
+        // the FP64 iteration recovers from
+        if (r != MTGPU_MAXITER || sd.iterations >= maxiter) {
+            if (stats) *stats = sd;
+            return r;
+        }
+        df_iters = sd.iterations;
+        maxiter -= df_iters;
+        for (int i = 0; i < n; i++) x[i] = 0.0;
+    }
     mtgpu_cocr *c = nullptr;
     int rc = mtgpu_cocr_create(nb, 0, ig, jg, idi, ijg, di, gg, 0, kpar, n_nodes_c, nvkat,
                                nver14, sigma3d, edges2, ig_t, jg_t, gg_t, is_node_bound,
@@ -393,6 +408,7 @@ int mtgpu_pcocr_2x2_folded_ex(int n, const int *ig, const int *jg, const int *id
         }
         st.solve_seconds = now_s() - t1;
     }
+    st.iterations += df_iters;
     if (stats) *stats = st;
 out:
     dev_free(d_b);

@@ -172,6 +172,7 @@ int mtgpu_cocr_create_from_assembly(mtgpu_assembly *a, double nu, void *stream, 
 
 struct mtgpu_survey_s {
     mtgpu::Survey V;
+    std::vector<double> nu;
     mtgpu_assembly *a = nullptr;
     cudaStream_t st = nullptr;
     bool own_stream = false;
@@ -188,6 +189,7 @@ int mtgpu_survey_create(mtgpu_assembly *a, int S, const double *nu, void *stream
     for (int k = 0; k < S; k++) MTGPU_CHECK_ARG(nu[k] > 0.0, "frequencies must be positive");
     auto *s = new mtgpu_survey_s();
     s->a = a;
+    s->nu.assign(nu, nu + S);
     if (stream) {
         s->st = (cudaStream_t)stream;
     } else {
@@ -220,10 +222,39 @@ int mtgpu_survey_solve(mtgpu_survey *s, const double *d_b, double *d_x, double e
     MTGPU_CHECK_ARG(eps > 0.0, "eps must be positive");
     MTGPU_TRY(cudaStreamSynchronize(cudaStreamLegacy));
     const double t0 = now_seconds();
+    mtgpu_survey_stats local{};
+    mtgpu_survey_stats *st = stats ? stats : &local;
     int rc = survey_solve(s->V, (const double2 *)d_b, (double2 *)d_x, eps, maxiter, verify, 16,
-                          stats);
-    if (stats) stats->seconds = now_seconds() - t0;
-    return rc;
+                          st);
+    if (rc <= MTGPU_ERR_ARG) return rc;
+    // systems the double-float iteration could not finish: FP64 COCR from a
+    // zero initial guess, with the iterations left (the stalled double-float
+    // iterate carries large errors in the air's gradient components, from
+    // which the FP64 iteration does not recover)
+    const long long nb = s->V.nb;
+    int worst = MTGPU_OK;
+    for (int k = 0; k < s->V.S; k++) {
+        const int left = maxiter - st->iterations[k];
+        if (st->status[k] == MTGPU_MAXITER && left > 0) {
+            mtgpu_cocr *c = nullptr;
+            int r2 = mtgpu_cocr_create_from_assembly(s->a, s->nu[k], s->st, &c);
+            if (r2) return r2;
+            mtgpu_solve_opts opts{verify, 0, 0};
+            mtgpu_solve_stats s64{};
+            MTGPU_TRY(cudaMemsetAsync(d_x + 2 * nb * k, 0, sizeof(double) * 2 * nb, s->st));
+            MTGPU_TRY(cudaStreamSynchronize(s->st));
+            r2 = mtgpu_cocr_solve(c, d_b + 2 * nb * k, d_x + 2 * nb * k, eps, left, &opts, &s64);
+            mtgpu_cocr_destroy(c);
+            if (r2 <= MTGPU_ERR_ARG) return r2;
+            st->status[k] = r2;
+            st->fp64_iterations[k] = s64.iterations;
+            st->true_residual_rel[k] = s64.true_residual_rel;
+            st->residual_rel[k] = s64.residual_rel;
+        }
+        if (st->status[k] != MTGPU_OK && worst == MTGPU_OK) worst = st->status[k];
+    }
+    st->seconds = now_seconds() - t0;
+    return worst;
 }
 
 int mtgpu_survey_spmv_timed(mtgpu_survey *s, int reps, float *ms)

@@ -12,6 +12,9 @@ struct SysState {
     double residual_rel;   // residual / r_old: the reference's stop quantity
     double true_rel;       // ||b - A x|| / ||b|| of the last verification
     double mrs_w;
+    double eps_k;          // the inner stop threshold on residual_rel
+    double bnorm;          // ||b|| of the system (FP64)
+    double rnorm;          // ||b - A x|| of the last FP64 residual evaluation
     int mrs_mode;          // 0 keep s_m, 1 s_m = r, 2 s_m += w (r - s_m)
     int status;            // 1 running, else MTGPU_OK / MTGPU_DIV_BY_ZERO / MTGPU_MAXITER / MTGPU_X0_NULL
     int iter;              // the reference's iteration counter
@@ -39,6 +42,8 @@ struct Survey {
     float4 *b = nullptr, *x = nullptr, *r = nullptr, *s = nullptr, *p = nullptr, *a = nullptr,
            *z = nullptr, *w = nullptr, *sm = nullptr;     // [row][SP]
     float4 *h = nullptr;                          // [node][SP]
+    double2 *b64 = nullptr, *xacc = nullptr;      // FP64 b and accumulated x: [row][SP]
+    int *all_on = nullptr;                        // 32 flags, all set
     double *partials = nullptr;
     cudaGraphExec_t graph = nullptr;
     int graph_iters = 0;

@@ -62,4 +62,6 @@ class Survey:
         S = self.S
         return rc, {"status": list(st.status[:S]), "iterations": list(st.iterations[:S]),
                     "verifications": list(st.verifications[:S]),
-                    "true_residual_rel": list(st.true_residual_rel[:S]), "seconds": st.seconds}
+                    "fp64_iterations": list(st.fp64_iterations[:S]),
+                    "true_residual_rel": list(st.true_residual_rel[:S]),
+                    "residual_rel": list(st.residual_rel[:S]), "seconds": st.seconds}

@@ -10,6 +10,8 @@ benchmark configurations of this project:
   c2  FP64 at scale: 96x96x64 cells, 50 m core, 10 padding cells per side
       (ratio 1.4), 3-layer earth (100, 10, 1000 Ohm.m; 500 m, 2 km, half-space)
       plus 20 random blocks with log10(rho) ~ U(0, 3); 0.1 Hz
+  c2s the c2 mesh and model under a 16-frequency survey (1e-3..1e3 Hz, 32
+      systems); 15x15 receivers at 200 m
   c3  batched survey: 64x64x48 cells, same layering plus 10 random blocks;
       16 frequencies log-spaced 1e-3..1e3 Hz; 25x25 receivers at 200 m
   c4  mixed precision: 128x128x80 cells, log-normal random conductivity
@@ -113,13 +115,16 @@ def make(name: str) -> Workload:
         layers = [Layer(0.0, 0.01)]
         m = layered_model(x, x, z, layers, blocks=[(-200, 200, -200, 200, -400, -100, 1.0)])
         return Workload(name, m, np.array([1.0]), _grid_receivers(5, 100.0))
-    if name in ("c2", "c3"):
-        if name == "c2":
+    if name in ("c2", "c2s", "c3"):
+        if name in ("c2", "c2s"):
             x = padded_lines(50.0, 76, 10, 1.4)
             z = z_lines(50.0, 44, 10, 1.4, 10, 1.4)
             nblocks, core_xy, core_z, seed = 20, 76, 44, 2
             freqs = np.array([0.1])
             rec = _grid_receivers(5, 100.0)
+            if name == "c2s":   # the c2 mesh under a 16-frequency survey
+                freqs = np.logspace(-3, 3, 16)
+                rec = _grid_receivers(15, 200.0)
         else:
             x = padded_lines(100.0, 48, 8, 1.4)
             z = z_lines(100.0, 32, 8, 1.4, 8, 1.4)
