@@ -499,8 +499,9 @@ def survey_run(args):
 
 def profile_run(args):
     """A short fixed run for ncu: the device assembly, one COCR context,
-    10 SpMV launches and 30 COCR iterations (ends with the iteration-limit
-    code, which is expected here)."""
+    10 SpMV launches and 30 COCR iterations, then the batched solver on
+    --systems systems: 10 SpMV launches and 30 iterations (both end with the
+    iteration-limit code, which is expected here)."""
     import torch
     from mtcalc_with_dfp_cocr_gb300 import assembly, workloads
     from mtcalc_with_dfp_cocr_gb300 import build as B
@@ -522,19 +523,24 @@ def profile_run(args):
     x = torch.zeros_like(rhs[0])
     code, st = ctx.solve(rhs[0], x, eps=1e-8, maxiter=30)
     ctx.close()
-    # the batched double-float solver on two systems of the same frequency
+    # the batched double-float solver on the workload's systems (all of them
+    # with --systems 0, else the first S)
     from mtcalc_with_dfp_cocr_gb300 import survey
-    rhs2 = torch.empty(2, 2 * w.mesh.nb, dtype=torch.float64, device="cuda")
-    A.rhs([nu, nu], [1, 0], t[0], np.stack([t[1], t[1]]), np.stack([t[2], t[2]]), rhs2)
-    sv = survey.Survey(A, [nu, nu], stream)
+    systems = w.systems if args.systems <= 0 else w.systems[:args.systems]
+    nus = [f for f, _ in systems]
+    tabs = tables
+    rhs2 = torch.empty(len(systems), 2 * w.mesh.nb, dtype=torch.float64, device="cuda")
+    A.rhs(nus, [a for _, a in systems], t[0], np.stack([tabs[f][1] for f in nus]),
+          np.stack([tabs[f][2] for f in nus]), rhs2)
+    sv = survey.Survey(A, nus, stream)
     ms2 = sv.spmv_timed(10)
     x2 = torch.zeros_like(rhs2)
     code2, st2 = sv.solve(rhs2, x2, eps=1e-8, maxiter=30, verify=False)
     sv.close()
     torch.cuda.synchronize()
     print(json.dumps({"profile": args.workload, "spmv_fp64_ms": ms / 10, "code": code,
-                      "iterations": st.iterations, "spmv_batched_ms": ms2 / 10,
-                      "code_batched": code2}))
+                      "iterations": st.iterations, "systems": len(systems),
+                      "spmv_batched_ms": ms2 / 10, "code_batched": code2}))
     A.close()
 
 
@@ -548,6 +554,8 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="short fixed run for ncu captures (see profile_run)")
     ap.add_argument("--workload", default=None, help="workload of --profile (default c3)")
+    ap.add_argument("--systems", type=int, default=2,
+                    help="systems of the batched solve in --profile (0: all of the workload)")
     ap.add_argument("--survey", default=None, metavar="WORKLOAD",
                     help="time a whole survey in one batch (e.g. c2s, c3); see survey_run")
     args = ap.parse_args()
