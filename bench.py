@@ -320,15 +320,16 @@ def gpu_arm(args):
 
 
 # --------------------------------------------------------------- CPU baseline
-def cpu_sample(slae, mesh, key, target_seconds=12.0, fallback_iterations=None):
+def cpu_sample(slae, mesh, key, target_seconds=15.0, fallback_iterations=None):
     """The oracle restatement of COCR_FP with all host threads: set-up plus
     a bounded number of iterations, extrapolated to the reference's
     iteration count for this system."""
     from oracle import pyoracle as O
     cores = os.cpu_count() or 1
     _, _, s1 = O.pcocr(slae, mesh, nthreads=cores, iter_limit=3)
-    per_guess = max(s1.seconds / 6.0, 1e-3)
-    n2 = int(min(2000, max(20, target_seconds / per_guess)))
+    _, _, s0 = O.pcocr(slae, mesh, nthreads=cores, iter_limit=23)
+    per_guess = max((s0.seconds - s1.seconds) / 20.0, 1e-4)
+    n2 = int(min(3000, max(50, (target_seconds - s1.seconds) / per_guess)))
     _, _, s2 = O.pcocr(slae, mesh, nthreads=cores, iter_limit=n2)
     per_iter = (s2.seconds - s1.seconds) / (n2 - 3)
     setup = max(0.0, s1.seconds - 3 * per_iter)
@@ -533,6 +534,7 @@ def profile_run(args):
     A.rhs(nus, [a for _, a in systems], t[0], np.stack([tabs[f][1] for f in nus]),
           np.stack([tabs[f][2] for f in nus]), rhs2)
     sv = survey.Survey(A, nus, stream)
+    tuning = sv.tuning()
     ms2 = sv.spmv_timed(10)
     x2 = torch.zeros_like(rhs2)
     code2, st2 = sv.solve(rhs2, x2, eps=1e-8, maxiter=30, verify=False)
@@ -540,7 +542,8 @@ def profile_run(args):
     torch.cuda.synchronize()
     print(json.dumps({"profile": args.workload, "spmv_fp64_ms": ms / 10, "code": code,
                       "iterations": st.iterations, "systems": len(systems),
-                      "spmv_batched_ms": ms2 / 10, "code_batched": code2}))
+                      "spmv_batched_ms": ms2 / 10, "spmv_variant": tuning[0],
+                      "spmv_variant_ms": tuning[1], "code_batched": code2}))
     A.close()
 
 

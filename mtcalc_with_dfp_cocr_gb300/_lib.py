@@ -100,6 +100,8 @@ SIGNATURES = {
     "mtgpu_survey_solve": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int, C.c_int,
                                      C.POINTER(SurveyStats)]),
     "mtgpu_survey_spmv_timed": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_float)]),
+    "mtgpu_survey_tuning": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_float)]),
+    "mtgpu_survey_set_spmv_variant": (C.c_int, [_vp, C.c_int]),
     "mtgpu_survey_destroy": (None, [_vp]),
     "mtgpu_receivers_create": (C.c_int, [_vp, C.c_int, _d, C.POINTER(_vp)]),
     "mtgpu_receivers_info": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), _vp]),

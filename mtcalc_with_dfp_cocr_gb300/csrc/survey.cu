@@ -28,6 +28,9 @@
 #include "survey.cuh"
 #include "dfloat.cuh"
 
+#include <algorithm>
+#include <climits>
+
 namespace mtgpu {
 
 using namespace dfl;
@@ -44,6 +47,8 @@ void Survey::release()
     dev_free(b); dev_free(x); dev_free(r); dev_free(s); dev_free(p); dev_free(a);
     dev_free(z); dev_free(w); dev_free(sm); dev_free(h);
     dev_free(b64); dev_free(xacc); dev_free(all_on);
+    dev_free(uoff); dev_free(ucol); dev_free(lc); dev_free(lr);
+    ntiles = 0;
     dev_free(partials);
     if (hsys) cudaFreeHost(hsys);
     hsys = nullptr;
@@ -65,11 +70,11 @@ __device__ __forceinline__ dfc from_d2(double2 v) { return dfc{from_double(v.x),
 // Per-system FP64 sums of a block: lanes k, k+SP, ... of a warp hold system
 // k.  The block that finishes last adds all block partials in block order
 // and returns true, with the totals in tot[n][k].
-template <int SP, int N>
+template <int SP, int N, int NT = kB>
 __device__ bool sys_grid_sum(double (&v)[N], double *partials, unsigned int *ticket,
                              double (*tot)[32])
 {
-    __shared__ double smem[N][kB / 32][SP];
+    __shared__ double smem[N][NT / 32][SP];
     __shared__ bool last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -83,7 +88,7 @@ __device__ bool sys_grid_sum(double (&v)[N], double *partials, unsigned int *tic
 #pragma unroll
         for (int n = 0; n < N; n++) {
             double acc = 0.0;
-            for (int q = 0; q < kB / 32; q++) acc += smem[n][q][threadIdx.x];
+            for (int q = 0; q < NT / 32; q++) acc += smem[n][q][threadIdx.x];
             partials[((size_t)n * gridDim.x + blockIdx.x) * SP + threadIdx.x] = acc;
         }
     }
@@ -413,29 +418,18 @@ k_update(int n, const float4 *__restrict__ p, const float4 *__restrict__ a,
     }
 }
 
-// z = A s, MRS update of s_m, ||s_m||, (z, s) -> stop test and beta.
-// mode 0 (set-up): z = A s and (z, s) only.
-template <int SP, int CH>
-__global__ void __launch_bounds__(kB, 3)
-k_spmv(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict__ s,
-       const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
-       SysState *sys, double *partials, int mode)
-{
-    const int k = threadIdx.x % SP;
-    const bool on = sys[k].status == kRun;
-    const df om = d2f(omega[k]);
-    const int mm = mode ? sys[k].mrs_mode : 0;
-    const df wm = from_double(sys[k].mrs_w);
+// Per-row tail of the SpMV kernels: store z = A s, accumulate (z, s), update
+// the MRS-smoothed residual s_m and accumulate ||s_m||^2.
+struct SpmvTail {
     acc zsr, zsi, nn;
-    const int rpb = kB / SP;
-    for (int row = blockIdx.x * rpb + threadIdx.x / SP; row < nb; row += gridDim.x * rpb) {
-        if (!on) continue;
-        const long long i = (long long)row * SP + k;
-        const float4 sv4 = __ldg(s + i);
+    int mm;
+    df wm;
+    __device__ __forceinline__ void row(long long i, dfc y, float4 sv4, const float4 *__restrict__ r,
+                                        float4 *__restrict__ z, float4 *__restrict__ sm)
+    {
         float4 rv4 = make_float4(0.f, 0.f, 0.f, 0.f), smo4 = rv4;
         if (mm != 0) rv4 = __ldg(r + i);
         if (mm == 2) smo4 = sm[i];
-        const dfc y = spmv_row<SP, CH>(A, row, k, om, s);
         z[i] = to4(y);
         const dfc sv = from4(sv4);
         zsr.mac(y.re, sv.re); zsr.mac(neg(y.im), sv.im);
@@ -456,27 +450,261 @@ k_spmv(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict
             nn.mac(smv.im, smv.im);
         }
     }
-    double v[3] = {zsr.to_double(), zsi.to_double(), nn.to_double()};
-    __shared__ double tot[3][32];
-    if (sys_grid_sum<SP, 3>(v, partials, &sys[0].ticket[3], tot) && threadIdx.x < SP) {
-        SysState &q = sys[threadIdx.x];
-        if (q.status == kRun) {
-            const double2 zs_new = make_double2(tot[0][threadIdx.x], tot[1][threadIdx.x]);
-            if (mode == 0) {
-                q.zs = zs_new;
-            } else {
-                if (q.mrs_mode != 0) q.residual = sqrt(tot[2][threadIdx.x]);
-                q.residual_rel = q.residual / q.r_old;
-                q.beta = cdiv(zs_new, q.zs);
-                q.zs = zs_new;
-                if (q.residual_rel < q.eps_k) {
-                    q.status = MTGPU_OK;
+    // grid totals -> stop test and beta (the last block only)
+    template <int SP, int NT = kB>
+    __device__ __forceinline__ void finish(SysState *sys, double *partials, int mode)
+    {
+        double v[3] = {zsr.to_double(), zsi.to_double(), nn.to_double()};
+        __shared__ double tot[3][32];
+        if (sys_grid_sum<SP, 3, NT>(v, partials, &sys[0].ticket[3], tot) && threadIdx.x < SP) {
+            SysState &q = sys[threadIdx.x];
+            if (q.status == kRun) {
+                const double2 zs_new = make_double2(tot[0][threadIdx.x], tot[1][threadIdx.x]);
+                if (mode == 0) {
+                    q.zs = zs_new;
                 } else {
-                    q.iter += 1;
-                    if (q.iter > q.maxiter) q.status = MTGPU_MAXITER;
+                    if (q.mrs_mode != 0) q.residual = sqrt(tot[2][threadIdx.x]);
+                    q.residual_rel = q.residual / q.r_old;
+                    q.beta = cdiv(zs_new, q.zs);
+                    q.zs = zs_new;
+                    if (q.residual_rel < q.eps_k) {
+                        q.status = MTGPU_OK;
+                    } else {
+                        q.iter += 1;
+                        if (q.iter > q.maxiter) q.status = MTGPU_MAXITER;
+                    }
                 }
             }
         }
+    }
+};
+
+// z = A s, MRS update of s_m, ||s_m||, (z, s) -> stop test and beta.
+// mode 0 (set-up): z = A s and (z, s) only.  x gathers straight from global
+// memory, CH slots in flight per thread.
+template <int SP, int CH>
+__global__ void __launch_bounds__(kB, 3)
+k_spmv(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict__ s,
+       const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
+       SysState *sys, double *partials, int mode)
+{
+    const int k = threadIdx.x % SP;
+    const bool on = sys[k].status == kRun;
+    const df om = d2f(omega[k]);
+    SpmvTail tail;
+    tail.mm = mode ? sys[k].mrs_mode : 0;
+    tail.wm = from_double(sys[k].mrs_w);
+    const int rpb = kB / SP;
+    for (int row = blockIdx.x * rpb + threadIdx.x / SP; row < nb; row += gridDim.x * rpb) {
+        if (!on) continue;
+        const long long i = (long long)row * SP + k;
+        const float4 sv4 = __ldg(s + i);
+        tail.row(i, spmv_row<SP, CH>(A, row, k, om, s), sv4, r, z, sm);
+    }
+    tail.finish<SP>(sys, partials, mode);
+}
+
+// ------------------------------------------------ tiled SpMV (x staged)
+// A tile is T consecutive SELL slices (32 T rows).  Its distinct columns
+// (about 260 per 32-row slice on these meshes, against 1,030 slot reads) are
+// listed once, and every slot carries its column's 16-bit index in that
+// list.  The kernel copies the tile's x segments (SP lanes each) and the
+// tile's matrix slots into shared memory with asynchronous copies, then
+// every (row, system) thread runs its row from shared memory: each x
+// segment crosses L2 once per tile instead of once per use, and no
+// dependent global load is left in the row loop.
+struct TileMat {
+    const int *wc, *wr;
+    const long long *pc, *pr;
+    const float2 *kc, *mc, *kr;
+    const unsigned short *lc, *lr;
+    const int *uoff, *ucol;
+    int T, ntiles, nslices;
+};
+
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gsrc) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+// shared-memory bytes of a tile: x segments, then K, M, K_real, local indices
+__host__ __device__ __forceinline__ long long tile_bytes(int nu, int SP, long long nc, long long nr)
+{
+    return (long long)nu * SP * 16 + nc * 8 * 2 + nr * 8 + nc * 2 + nr * 2;
+}
+
+// threads of the x-staged SpMV block: a tile of T slices in whole passes
+template <int SP>
+struct TileCfg {
+    static constexpr int NT = SP >= 32 ? 1024 : (SP == 1 ? 256 : 512);
+    // slices per tile
+    static constexpr int T = SP >= 16 ? 1 : (SP == 1 ? 8 : (16 / SP < 8 ? 16 / SP : 8));
+};
+
+template <int SP>
+__global__ void __launch_bounds__(TileCfg<SP>::NT)
+k_spmv_t(int nb, TileMat A, const float2 *__restrict__ omega, const float4 *__restrict__ s,
+         const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
+         SysState *sys, double *partials, int mode)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int k = threadIdx.x % SP;
+    const bool on = sys[k].status == kRun;
+    const df om = d2f(omega[k]);
+    SpmvTail tail;
+    tail.mm = mode ? sys[k].mrs_mode : 0;
+    tail.wm = from_double(sys[k].mrs_w);
+    for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
+        const int s0 = t * A.T, s1 = min(s0 + A.T, A.nslices);
+        const long long c0 = A.pc[s0], nc = A.pc[s1] - c0, q0 = A.pr[s0], nr = A.pr[s1] - q0;
+        const int u0 = A.uoff[t], nu = A.uoff[t + 1] - u0;
+        float4 *xs = reinterpret_cast<float4 *>(smem);
+        float2 *skc = reinterpret_cast<float2 *>(xs + (long long)nu * SP);
+        float2 *smc = skc + nc;
+        float2 *skr = smc + nc;
+        unsigned short *slc = reinterpret_cast<unsigned short *>(skr + nr);
+        unsigned short *slr = slc + nc;
+        __syncthreads();   // the previous tile's readers are done
+        constexpr int NT = TileCfg<SP>::NT;
+        for (int i = threadIdx.x; i < nu * SP; i += NT)
+            cp_async16(xs + i, s + (long long)__ldg(A.ucol + u0 + i / SP) * SP + i % SP);
+        // slot counts are multiples of 32: whole 16-byte chunks, 16-byte aligned
+        for (long long i = threadIdx.x; i < nc / 2; i += NT) {
+            cp_async16(reinterpret_cast<float4 *>(skc) + i, reinterpret_cast<const float4 *>(A.kc + c0) + i);
+            cp_async16(reinterpret_cast<float4 *>(smc) + i, reinterpret_cast<const float4 *>(A.mc + c0) + i);
+        }
+        for (long long i = threadIdx.x; i < nr / 2; i += NT)
+            cp_async16(reinterpret_cast<float4 *>(skr) + i, reinterpret_cast<const float4 *>(A.kr + q0) + i);
+        for (long long i = threadIdx.x; i < nc / 8; i += NT)
+            cp_async16(reinterpret_cast<float4 *>(slc) + i, reinterpret_cast<const float4 *>(A.lc + c0) + i);
+        for (long long i = threadIdx.x; i < nr / 8; i += NT)
+            cp_async16(reinterpret_cast<float4 *>(slr) + i, reinterpret_cast<const float4 *>(A.lr + q0) + i);
+        cp_async_wait_all();
+        __syncthreads();
+        if (!on) continue;
+        for (int rr = threadIdx.x / SP; rr < (s1 - s0) * 32; rr += NT / SP) {
+            const int row = s0 * 32 + rr;
+            if (row >= nb) break;
+            const int sl = s0 + (rr >> 5), l = rr & 31;
+            acc kr_, ki_, mr_, mi_;
+            {
+                const int b = (int)(A.pc[sl] - c0) + l, n = A.wc[sl];
+#pragma unroll 4
+                for (int q = 0; q < n; q++) {
+                    const int t2 = b + 32 * q;
+                    const float4 xv = xs[slc[t2] * SP + k];
+                    const df kd = d2f(skc[t2]), md = d2f(smc[t2]);
+                    const df xr{xv.x, xv.y}, xi{xv.z, xv.w};
+                    kr_.mac(kd, xr);
+                    ki_.mac(kd, xi);
+                    mr_.mac(md, xr);
+                    mi_.mac(md, xi);
+                }
+            }
+            {
+                const int b = (int)(A.pr[sl] - q0) + l, n = A.wr[sl];
+#pragma unroll 4
+                for (int q = 0; q < n; q++) {
+                    const int t2 = b + 32 * q;
+                    const float4 xv = xs[slr[t2] * SP + k];
+                    const df kd = d2f(skr[t2]);
+                    kr_.mac(kd, df{xv.x, xv.y});
+                    ki_.mac(kd, df{xv.z, xv.w});
+                }
+            }
+            const df mxr = mr_.get(), mxi = mi_.get();
+            kr_.mac(neg(om), mxi);
+            ki_.mac(om, mxr);
+            const long long i = (long long)row * SP + k;
+            tail.row(i, dfc{kr_.get(), ki_.get()}, __ldg(s + i), r, z, sm);
+        }
+    }
+    tail.finish<SP, TileCfg<SP>::NT>(sys, partials, mode);
+}
+
+// ---- tile set-up: sorted distinct columns of every tile, local indices
+constexpr int kTileThreads = 1024;
+constexpr int kTileMaxKeys = 16384;
+
+// pass 0 (write == 0): count[t] = distinct columns of tile t; pass 1: the
+// distinct columns to ucol[uoff[t]..] and every slot's local index.  A tile
+// with more than kTileMaxKeys slots sets *overflow.
+__global__ void __launch_bounds__(kTileThreads)
+k_tile_cols(int nslices, int T, const long long *pc, const long long *pr, const int *col_c,
+            const int *col_r, const int *uoff, int *count, int *ucol, unsigned short *lc,
+            unsigned short *lr, int *overflow, int write)
+{
+    extern __shared__ int keys[];              // [kTileMaxKeys], then unique [kTileMaxKeys]
+    int *uniq = keys + kTileMaxKeys;
+    __shared__ int part[kTileThreads];
+    const int t = blockIdx.x;
+    const int s0 = t * T, s1 = min(s0 + T, nslices);
+    const long long c0 = pc[s0], nc = pc[s1] - c0, q0 = pr[s0], nr = pr[s1] - q0;
+    const long long n = nc + nr;
+    if (n > kTileMaxKeys) {
+        if (threadIdx.x == 0) atomicExch(overflow, 1);
+        return;
+    }
+    int np2 = 1;
+    while (np2 < n) np2 <<= 1;
+    for (int i = threadIdx.x; i < np2; i += blockDim.x)
+        keys[i] = i < nc ? col_c[c0 + i] : (i < n ? col_r[q0 + i - nc] : INT_MAX);
+    __syncthreads();
+    // bitonic sort
+    for (int size = 2; size <= np2; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int i = threadIdx.x; i < np2; i += blockDim.x) {
+                const int j = i ^ stride;
+                if (j > i) {
+                    const bool up = (i & size) == 0;
+                    const int a = keys[i], b = keys[j];
+                    if ((a > b) == up) {
+                        keys[i] = b;
+                        keys[j] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    // distinct values: a contiguous chunk per thread, then a scan of the chunk counts
+    const int chunk = (int)((n + blockDim.x - 1) / blockDim.x);
+    const int a0 = threadIdx.x * chunk, a1 = min((long long)a0 + chunk, n);
+    int cnt = 0;
+    for (int i = a0; i < a1; i++) cnt += (i == 0 || keys[i] != keys[i - 1]);
+    part[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+        const int v = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    const int total = part[blockDim.x - 1];
+    if (!write) {
+        if (threadIdx.x == 0) count[t] = total;
+        return;
+    }
+    int pos = part[threadIdx.x] - cnt;
+    for (int i = a0; i < a1; i++)
+        if (i == 0 || keys[i] != keys[i - 1]) uniq[pos++] = keys[i];
+    __syncthreads();
+    for (int i = threadIdx.x; i < total; i += blockDim.x) ucol[uoff[t] + i] = uniq[i];
+    // local index of every slot: binary search in uniq
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+        const int c = i < nc ? col_c[c0 + i] : col_r[q0 + i - nc];
+        int lo = 0, hi = total - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (uniq[mid] < c) lo = mid + 1; else hi = mid;
+        }
+        if (i < nc) lc[c0 + i] = (unsigned short)lo;
+        else lr[q0 + i - nc] = (unsigned short)lo;
     }
 }
 
@@ -718,9 +946,20 @@ struct Impl {
         const ParamMatrix &P = *V.P;
         return Mat{P.d_wc, P.d_wr, P.d_pc, P.d_pr, P.d_col_c, P.d_col_r, V.kc, V.mc, V.kr};
     }
+    static TileMat tmat(const Survey &V)
+    {
+        const ParamMatrix &P = *V.P;
+        return TileMat{P.d_wc, P.d_wr, P.d_pc, P.d_pr, V.kc, V.mc, V.kr, V.lc, V.lr,
+                       V.uoff, V.ucol, V.tile_T, V.ntiles, P.nslices};
+    }
     static void spmv(Survey &V, int mode)
     {
         const Mat A = mat(V);
+        if (V.ch == 0) {
+            k_spmv_t<SP><<<V.g_spmv_t, TileCfg<SP>::NT, V.tile_smem, V.st>>>(
+                V.nb, tmat(V), V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode);
+            return;
+        }
         switch (V.ch) {
         case 2: k_spmv<SP, 2><<<V.g_spmv, kB, 0, V.st>>>(V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode); break;
         case 8: k_spmv<SP, 8><<<V.g_spmv, kB, 0, V.st>>>(V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode); break;
@@ -788,6 +1027,20 @@ struct Impl {
         const void *fs = V.ch == 2 ? (const void *)k_spmv<SP, 2>
                          : V.ch == 8 ? (const void *)k_spmv<SP, 8> : (const void *)k_spmv<SP, 4>;
         V.g_spmv = g(fs, V.grid_rows);
+        if (V.ntiles > 0) {
+            int b = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (const void *)k_spmv_t<SP>,
+                                                              TileCfg<SP>::NT, V.tile_smem) !=
+                    cudaSuccess || b < 1)
+                b = 1;
+            V.g_spmv_t = std::max(1, std::min(b * nsm, V.ntiles));
+        }
+    }
+    static void tile_slices_of(int *T) { *T = TileCfg<SP>::T; }
+    static void tile_attr(Survey &V, cudaError_t *e)
+    {
+        *e = cudaFuncSetAttribute((const void *)k_spmv_t<SP>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, V.tile_smem);
     }
 };
 
@@ -806,6 +1059,82 @@ int sync_sys(Survey &V)
     MTGPU_TRY(cudaMemcpyAsync(V.hsys, V.sys, sizeof(SysState) * 32, cudaMemcpyDeviceToHost, V.st));
     MTGPU_TRY(cudaStreamSynchronize(V.st));
     return MTGPU_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// Tiles of the x-staged SpMV: TileCfg<SP>::T slices per tile, covered by
+// a block of TileCfg<SP>::NT threads in whole passes.  Leaves
+// V.ntiles = 0 (variant unavailable) when a tile does not fit the set-up
+// sort or the shared memory of a block.
+int build_tiles(Survey &V, int nsm)
+{
+    const ParamMatrix &P = *V.P;
+    MTGPU_SP_DISPATCH(V.SP, tile_slices_of(&V.tile_T));
+    const int nt = ceil_div(P.nslices, V.tile_T);
+    int *d_count = nullptr, *d_over = nullptr;
+    int rc;
+    if ((rc = dev_alloc(&d_count, nt)) || (rc = dev_alloc(&d_over, 1)) ||
+        (rc = dev_alloc(&V.uoff, nt + 1)) || (rc = dev_alloc(&V.lc, P.len_c)) ||
+        (rc = dev_alloc(&V.lr, P.len_r))) {
+        dev_free(d_count);
+        dev_free(d_over);
+        return rc;
+    }
+    auto done = [&](int code) {
+        dev_free(d_count);
+        dev_free(d_over);
+        return code;
+    };
+    const int sort_smem = 2 * kTileMaxKeys * (int)sizeof(int);
+    MTGPU_TRY(cudaFuncSetAttribute((const void *)k_tile_cols,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, sort_smem));
+    MTGPU_TRY(cudaMemsetAsync(d_over, 0, sizeof(int), V.st));
+    k_tile_cols<<<nt, kTileThreads, sort_smem, V.st>>>(P.nslices, V.tile_T, P.d_pc, P.d_pr,
+                                                      P.d_col_c, P.d_col_r, V.uoff, d_count,
+                                                      nullptr, V.lc, V.lr, d_over, 0);
+    note_launches(1);
+    MTGPU_TRY(cudaGetLastError());
+    std::vector<int> count(nt), off(nt + 1, 0);
+    std::vector<long long> pc(P.nslices + 1), pr(P.nslices + 1);
+    int over = 0;
+    MTGPU_TRY(cudaMemcpyAsync(&over, d_over, sizeof(int), cudaMemcpyDeviceToHost, V.st));
+    MTGPU_TRY(cudaMemcpyAsync(count.data(), d_count, sizeof(int) * nt, cudaMemcpyDeviceToHost, V.st));
+    MTGPU_TRY(cudaMemcpyAsync(pc.data(), P.d_pc, sizeof(long long) * pc.size(), cudaMemcpyDeviceToHost, V.st));
+    MTGPU_TRY(cudaMemcpyAsync(pr.data(), P.d_pr, sizeof(long long) * pr.size(), cudaMemcpyDeviceToHost, V.st));
+    MTGPU_TRY(cudaStreamSynchronize(V.st));
+    if (over) return done(MTGPU_OK);
+    long long smem = 0;
+    for (int t = 0; t < nt; t++) {
+        off[t + 1] = off[t] + count[t];
+        const int s0 = t * V.tile_T, s1 = std::min(s0 + V.tile_T, P.nslices);
+        smem = std::max(smem, tile_bytes(count[t], V.SP, pc[s1] - pc[s0], pr[s1] - pr[s0]));
+    }
+    int max_smem = 0;
+    int dev = 0;
+    MTGPU_TRY(cudaGetDevice(&dev));
+    MTGPU_TRY(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    if (smem > max_smem - 26 * 1024) return done(MTGPU_OK);   // too large (with the static reduction buffers): variant off
+    if ((rc = dev_alloc(&V.ucol, std::max(off[nt], 1)))) return done(rc);
+    MTGPU_TRY(cudaMemcpyAsync(V.uoff, off.data(), sizeof(int) * (nt + 1), cudaMemcpyHostToDevice, V.st));
+    k_tile_cols<<<nt, kTileThreads, sort_smem, V.st>>>(P.nslices, V.tile_T, P.d_pc, P.d_pr,
+                                                      P.d_col_c, P.d_col_r, V.uoff, d_count,
+                                                      V.ucol, V.lc, V.lr, d_over, 1);
+    note_launches(1);
+    MTGPU_TRY(cudaGetLastError());
+    MTGPU_TRY(cudaStreamSynchronize(V.st));
+    V.tile_smem = (int)smem;
+    cudaError_t e = cudaSuccess;
+    MTGPU_SP_DISPATCH(V.SP, tile_attr(V, &e));
+    if (e != cudaSuccess) {
+        cudaGetLastError();   // clear it: the variant is just unavailable
+        return done(MTGPU_OK);
+    }
+    V.ntiles = nt;
+    MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+    return done(MTGPU_OK);
 }
 
 }  // namespace
@@ -886,12 +1215,14 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
     MTGPU_TRY(cudaGetLastError());
     MTGPU_TRY(cudaStreamSynchronize(st));
     note_launches(8);
-    // autotune the SpMV slot batch: time each candidate, keep the fastest
+    if ((rc = build_tiles(V, nsm))) return rc;
+    // autotune the SpMV variant: time each candidate, keep the fastest
     {
-        const int cand[3] = {2, 4, 8};
+        const int cand[4] = {0, 2, 4, 8};
         float best = 1e30f;
         int best_ch = 4;
-        for (int c = 0; c < 3; c++) {
+        for (int c = 0; c < 4; c++) {
+            if (cand[c] == 0 && V.ntiles == 0) continue;
             V.ch = cand[c];
             MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
             float ms = 0.f;
@@ -906,6 +1237,19 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
         V.ch = best_ch;
         MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
     }
+    return MTGPU_OK;
+}
+
+int survey_set_variant(Survey &V, int variant)
+{
+    int dev = 0, nsm = 0;
+    MTGPU_TRY(cudaGetDevice(&dev));
+    MTGPU_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    V.ch = variant;
+    MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+    if (V.graph) cudaGraphExecDestroy(V.graph);   // captured with the old variant
+    V.graph = nullptr;
+    V.graph_iters = 0;
     return MTGPU_OK;
 }
 

@@ -29,8 +29,12 @@ struct Survey {
     int nb = 0, S = 0, SP = 1;
     int grid_rows = 0, grid_nodes = 0;           // work bounds (blocks that have rows)
     int g_init = 0, g_node = 0, g_edge = 0, g_update = 0, g_spmv = 0, g_true = 0;  // launch grids
-    int ch = 4;                                  // SpMV slot batch (autotuned at set-up)
-    float tune_ms[3] = {0.f, 0.f, 0.f};          // SpMV times of the batch sizes 2, 4, 8
+    int ch = 4;    // SpMV variant: 0 tiled (x staged in shared memory), else slots in flight (2, 4, 8); autotuned
+    // SpMV tiles: T consecutive SELL slices, their distinct columns, per-slot local indices
+    int tile_T = 1, ntiles = 0, tile_smem = 0, g_spmv_t = 0;
+    int *uoff = nullptr, *ucol = nullptr;
+    unsigned short *lc = nullptr, *lr = nullptr;
+    float tune_ms[4] = {0.f, 0.f, 0.f, 0.f};     // SpMV times of the variants tiled, 2, 4, 8
     Folded G;                                    // pattern of G and G^T
     float2 *kc = nullptr, *mc = nullptr, *kr = nullptr;   // double-float K and M per slot
     float *gv32 = nullptr, *tv32 = nullptr;      // values of G and G^T (+-1/2, exact in FP32)
@@ -58,5 +62,6 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
 int survey_solve(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, double eps,
                  int maxiter, int verify, int iters_per_launch, mtgpu_survey_stats *stats);
 int survey_spmv_timed(Survey &V, int reps, float *ms);
+int survey_set_variant(Survey &V, int variant);
 
 }  // namespace mtgpu

@@ -51,6 +51,20 @@ class Survey:
                    "mtgpu_survey_spmv_timed")
         return ms.value
 
+    def tuning(self):
+        """(chosen SpMV variant, {variant: ms per launch}) of the set-up
+        autotuning; variant 0 stages x in shared memory per tile."""
+        v = C.c_int()
+        ms = (C.c_float * 4)()
+        _lib.check(_lib.lib().mtgpu_survey_tuning(self._h, C.byref(v), ms),
+                   "mtgpu_survey_tuning")
+        return v.value, {c: ms[i] for i, c in enumerate((0, 2, 4, 8)) if ms[i] > 0}
+
+    def set_spmv_variant(self, variant):
+        """Pin the SpMV variant (0 tiled, 2, 4, 8) instead of the autotuned one."""
+        _lib.check(_lib.lib().mtgpu_survey_set_spmv_variant(self._h, int(variant)),
+                   "mtgpu_survey_set_spmv_variant")
+
     def solve(self, b, x, eps=1e-8, maxiter=20000, verify=True):
         """b, x: torch CUDA float64 tensors shaped (S, 2 nb); x: initial
         guesses in, solutions out.  Returns (code, stats dict)."""
