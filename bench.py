@@ -498,6 +498,85 @@ def survey_run(args):
     A.close()
 
 
+def adjoint_run(args):
+    """The adjoint gradient on the c5 case (--adjoint): 48x48x32 cells,
+    8 frequencies x 2 polarisations, 15x15 receivers.  Observed impedances
+    come from the model with 5 seeded blocks perturbed by +-0.3 in
+    log10(sigma).  Times the misfit + gradient with the batched solver and
+    with the FP64 solver, compares the two gradients, and checks both
+    against central differences (step 1e-4 in ln sigma) of the FP64 forward
+    solve on 20 seed-chosen cells among those whose FP64 gradient is at
+    least 1 % of the largest (cells with a negligible gradient have no
+    meaningful relative error)."""
+    import torch
+    from mtcalc_with_dfp_cocr_gb300 import adjoint, workloads
+    from mtcalc_with_dfp_cocr_gb300 import build as B
+    B.build()
+    torch.cuda.set_device(0)
+    w = workloads.make("c5")
+    m = w.mesh
+    m0 = np.log(np.asarray(m.cell_sigma, np.float64))
+    rng = np.random.default_rng(55)
+    xyz = m.xyz()
+    nodes = m.cell_nodes()
+    c = 0.5 * (xyz[nodes[:, 0]] + xyz[nodes[:, 7]])
+    m_true = m0.copy()
+    for _ in range(5):
+        lo = rng.uniform([-1500.0, -1500.0, -1500.0], [1000.0, 1000.0, -300.0])
+        size = rng.uniform([200.0, 200.0, 200.0], [600.0, 600.0, 500.0])
+        box = np.all((c >= lo) & (c <= lo + size), axis=1) & (c[:, 2] < 0)
+        m_true[box] += 0.3 * np.log(10.0) * rng.choice([-1.0, 1.0])
+    freqs = w.freqs
+    p64 = adjoint.ImpedanceProblem(m, freqs, w.receivers, solver="fp64", eps=1e-10,
+                                   maxiter=50000)
+    resp, _ = p64.forward(m_true)
+    z_obs = adjoint.impedances(resp).cpu().numpy()
+    p64.set_observed(z_obs)
+    pb = adjoint.ImpedanceProblem(m, freqs, w.receivers, z_obs=z_obs, solver="batched",
+                                  eps=1e-8, maxiter=50000)
+
+    def timed(problem):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        J, st = problem.misfit(m0)
+        t1 = time.perf_counter()
+        g = problem.gradient(st)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        return J, g.cpu().numpy(), t1 - t0, t2 - t1
+
+    timed(pb)   # warm-up (library load, first-touch allocations)
+    Jb, gb, tfb, tgb = timed(pb)
+    J64, g64, tf64, tg64 = timed(p64)
+    earth = np.asarray(m.cell_sigma0) > 1e-6
+    err_b = float(np.linalg.norm((gb - g64)[earth]) / np.linalg.norm(g64[earth]))
+    fd_problem = p64
+    strong = np.nonzero(earth & (np.abs(g64) >= 0.01 * np.abs(g64[earth]).max()))[0]
+    cells = rng.choice(strong, min(20, len(strong)), replace=False)
+    h = 1e-4
+    fd, e64, eb = [], [], []
+    for cell in cells:
+        mp, mm = m0.copy(), m0.copy()
+        mp[cell] += h
+        mm[cell] -= h
+        d = (fd_problem.misfit(mp)[0] - fd_problem.misfit(mm)[0]) / (2 * h)
+        fd.append(d)
+        e64.append(abs(g64[cell] - d) / abs(d))
+        eb.append(abs(gb[cell] - d) / abs(d))
+    out = {"adjoint": "c5", "nb": m.nb, "cells": m.kpar, "systems": 2 * len(freqs),
+           "receivers": len(w.receivers), "misfit_batched": Jb, "misfit_fp64": J64,
+           "batched": {"forward_s": tfb, "gradient_s": tgb},
+           "fp64": {"forward_s": tf64, "gradient_s": tg64},
+           "speedup_forward_plus_gradient": (tf64 + tg64) / (tfb + tgb),
+           "gradient_rel_err_batched_vs_fp64_earth": err_b,
+           "fd": {"cells": [int(x) for x in cells], "step_ln_sigma": h,
+                  "rel_err_fp64_max": float(max(e64)), "rel_err_fp64_median": float(np.median(e64)),
+                  "rel_err_batched_max": float(max(eb)),
+                  "rel_err_batched_median": float(np.median(eb)),
+                  "cell_selection": "seeded among earth cells with |grad| >= 1% of max"}}
+    print(json.dumps(out), flush=True)
+
+
 def profile_run(args):
     """A short fixed run for ncu: the device assembly, one COCR context,
     10 SpMV launches and 30 COCR iterations, then the batched solver on
@@ -561,7 +640,12 @@ def main():
                     help="systems of the batched solve in --profile (0: all of the workload)")
     ap.add_argument("--survey", default=None, metavar="WORKLOAD",
                     help="time a whole survey in one batch (e.g. c2s, c3); see survey_run")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="adjoint gradient on c5: timing and finite-difference check")
     args = ap.parse_args()
+    if args.adjoint:
+        adjoint_run(args)
+        return
     if args.survey:
         args.steps = min(args.steps, 1) if args.steps else 1
         args.warmup = min(args.warmup, 1)

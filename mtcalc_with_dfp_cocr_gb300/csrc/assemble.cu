@@ -251,14 +251,38 @@ __global__ void k_bnode(int nbnd, const int *bnd, unsigned char *bnode)
     if (i < nbnd) bnode[bnd[i]] = 1;
 }
 
+// A0 as edge values of every system: the 1-D field of the system's
+// frequency at the edge midpoint times (alfa, 1 - alfa, 0), dotted with
+// J t = (h_d / 2) e_d (T_Brick.cpp:1463-1495).  h_d is the edge's length
+// (the cell size along d).  a0[k][e] = (sin, cos) parts.
+__global__ void k_a0(int nb, int S, const int *alfa, int n1d, const double *z1d,
+                     const double *usin, const double *ucos, const int *edges, const double *xyz,
+                     double2 *a0)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = blockIdx.y;
+    if (e >= nb || k >= S) return;
+    const int n1 = edges[2 * e], n2 = edges[2 * e + 1];
+    const double dx = xyz[3 * n2] - xyz[3 * n1], dy = xyz[3 * n2 + 1] - xyz[3 * n1 + 1];
+    const int d = dx != 0.0 ? 0 : (dy != 0.0 ? 1 : 2);
+    double as = 0.0, ac = 0.0;
+    if (d != 2) {
+        const double h = d == 0 ? dx : dy;
+        const double wx = alfa[k] ? 1.0 : 0.0;
+        const double wd = d == 0 ? wx : 1.0 - wx;
+        const double zm = 0.5 * (xyz[3 * n1 + 2] + xyz[3 * n2 + 2]);
+        const double *us = usin + (long long)k * n1d, *uc = ucos + (long long)k * n1d;
+        as = __dmul_rn(0.5 * h, __dmul_rn(spline(zm, n1d, z1d, us), wd));
+        ac = __dmul_rn(0.5 * h, __dmul_rn(spline(zm, n1d, z1d, uc), wd));
+    }
+    a0[(long long)k * nb + e] = make_double2(as, ac);
+}
+
 // Right-hand sides of S systems: b = i omega (sigma0 - sigma) C A0 summed
 // over the row's cells (T_Brick.cpp:1361-1395), zero on Dirichlet rows.
-// A0 at the edge midpoints is the 1-D field of the system's frequency times
-// (alfa, 1 - alfa, 0), dotted with J t = (h_d / 2) e_d (T_Brick.cpp:1463-1495).
-__global__ void k_rhs(int nb, int S, const double *omega, const int *alfa, int n1d,
-                      const double *z1d, const double *usin, const double *ucos,
+__global__ void k_rhs(int nb, int S, const double *omega, const double2 *a0,
                       const int *ec_ptr, const int *ec_cell, const int *ed, int ed_stride,
-                      const int *edges, const int *nver, int nver_stride, const double *xyz,
+                      const int *nver, int nver_stride, const double *xyz,
                       const int *nvkat, const double *sig, const double *sig0,
                       const unsigned char *bedge, double2 *rhs, long long rhs_stride,
                       int interleaved)
@@ -269,8 +293,7 @@ __global__ void k_rhs(int nb, int S, const double *omega, const int *alfa, int n
     double pre = 0.0, pim = 0.0;
     if (!bedge[e]) {
         const double w = omega[k];
-        const double wx = alfa[k] ? 1.0 : 0.0, wy = 1.0 - wx;
-        const double *us = usin + (long long)k * n1d, *uc = ucos + (long long)k * n1d;
+        const double2 *ak = a0 + (long long)k * nb;
         for (int t = ec_ptr[e]; t < ec_ptr[e + 1]; t++) {
             const int cl = ec_cell[t];
             const int cell = cl >> 4, li = cl & 15;
@@ -279,20 +302,12 @@ __global__ void k_rhs(int nb, int S, const double *omega, const int *alfa, int n
             const int mat = nvkat[cell];
             const double mult = (sig0[mat] - sig[mat]) * w;
             double gre = 0.0, gim = 0.0;
-            for (int lj = 0; lj < 12; lj++) {
+            for (int lj = 0; lj < 8; lj++) {   // x and y edges: A0 has no z part
                 double b, c;
                 brick_entry(li, lj, h, b, c);
-                const int d = ldir(lj);
-                double as = 0.0, ac = 0.0;
-                if (d != 2) {
-                    const int ej = ed[(long long)cell * ed_stride + lj];
-                    const double zm = 0.5 * (xyz[3 * edges[2 * ej] + 2] + xyz[3 * edges[2 * ej + 1] + 2]);
-                    const double wd = d == 0 ? wx : wy;
-                    as = __dmul_rn(0.5 * h[d], __dmul_rn(spline(zm, n1d, z1d, us), wd));
-                    ac = __dmul_rn(0.5 * h[d], __dmul_rn(spline(zm, n1d, z1d, uc), wd));
-                }
-                gre = __dadd_rn(gre, __dmul_rn(c, as));
-                gim = __dadd_rn(gim, __dmul_rn(c, ac));
+                const double2 v = ak[ed[(long long)cell * ed_stride + lj]];
+                gre = __dadd_rn(gre, __dmul_rn(c, v.x));
+                gim = __dadd_rn(gim, __dmul_rn(c, v.y));
             }
             pre = __dadd_rn(pre, __dmul_rn(gim, -mult));
             pim = __dadd_rn(pim, __dmul_rn(gre, mult));
@@ -539,12 +554,21 @@ int param_rhs(const ParamMatrix &P, int S, const double *d_omega, const int *d_a
               long long rhs_stride, int interleaved, cudaStream_t st)
 {
     dim3 grid(ceil_div(P.nb, 128), S);
-    k_rhs<<<grid, 128, 0, st>>>(P.nb, S, d_omega, d_alfa, n1d, d_z1d, d_usin, d_ucos, P.d_ec_ptr,
-                                P.d_ec_cell, P.d_ed, P.ed_stride, P.d_edges, P.d_nver,
-                                P.nver_stride, P.d_xyz, P.d_nvkat, P.d_sig, P.d_sig0, P.d_bedge,
-                                d_rhs, rhs_stride, interleaved);
-    note_launches(1);
-    MTGPU_TRY(cudaGetLastError());
+    double2 *a0 = nullptr;
+    int rc = dev_alloc(&a0, (size_t)S * P.nb);
+    if (rc) return rc;
+    k_a0<<<grid, 128, 0, st>>>(P.nb, S, d_alfa, n1d, d_z1d, d_usin, d_ucos, P.d_edges, P.d_xyz, a0);
+    k_rhs<<<grid, 128, 0, st>>>(P.nb, S, d_omega, a0, P.d_ec_ptr, P.d_ec_cell, P.d_ed,
+                                P.ed_stride, P.d_nver, P.nver_stride, P.d_xyz, P.d_nvkat, P.d_sig,
+                                P.d_sig0, P.d_bedge, d_rhs, rhs_stride, interleaved);
+    note_launches(2);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    dev_free(a0);
+    if (e != cudaSuccess) {
+        set_last_error(e, "param_rhs", __FILE__, __LINE__);
+        return MTGPU_ERR_CUDA;
+    }
     return MTGPU_OK;
 }
 
