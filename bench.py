@@ -577,6 +577,79 @@ def adjoint_run(args):
     print(json.dumps(out), flush=True)
 
 
+def dtm_run(args):
+    """The reference's published case (--dtm): the DTM model of
+    CalculationExample on the reference RegularMeshBuilder's 625/500 m mesh
+    (tests/golden/dtm_625_500.npz), 21 periods x 2 polarisations through the
+    device assembly, the batched solver, the receiver fields and the MT
+    responses, against CalculationResults/625_500_reg_R_Z.txt.  The table
+    was produced with the reference's smoothing output path and FP32
+    impedance post-processing, so agreement is expected at the percent
+    level, not 1e-6.  The table's station coordinates are evaluated both as
+    (northing, easting) = (x, y) and as (x, -y); the example's receiver file
+    holds the mirrored set for part of the stations."""
+    import torch
+    from mtcalc_with_dfp_cocr_gb300 import assembly, mesh as M, normal1d, receivers, survey
+    from mtcalc_with_dfp_cocr_gb300 import build as B
+    B.build()
+    torch.cuda.set_device(0)
+    g = np.load(os.path.join(ROOT, "tests", "golden", "dtm_625_500.npz"))
+    cm = g["cell_mat"].astype(np.int64)
+    layers = [M.Layer(float(t), float(s)) for t, s in zip(g["layer_tops"], g["layer_sigma"])]
+    m = M.RegularMesh(g["x"], g["y"], g["z"], layers, g["mat_sigma"][cm], g["mat_sigma0"][cm])
+    freqs = 1.0 / g["periods"]
+    st = g["stations"]
+    pts = np.concatenate([np.c_[st[:, 0], st[:, 1], np.zeros(len(st))],
+                          np.c_[st[:, 0], -st[:, 1], np.zeros(len(st))]])
+    A = assembly.Assembly(m)
+    R = receivers.Receivers(A, pts)
+    tops = [l.top for l in layers]
+    sig = [l.sigma for l in layers]
+    out = np.empty((len(freqs), len(pts), 34))
+    t_solve = 0.0
+    iters, fp64 = [], []
+    for f0 in range(0, len(freqs), 16):
+        fb = freqs[f0:f0 + 16]
+        nus = np.repeat(fb, 2)
+        alfas = np.tile([1, 0], len(fb))
+        tabs = [normal1d.solve_1d(f, tops, sig) for f in fb]
+        us = np.repeat(np.stack([t[1] for t in tabs]), 2, axis=0)
+        uc = np.repeat(np.stack([t[2] for t in tabs]), 2, axis=0)
+        b = torch.empty(len(nus), 2 * m.nb, dtype=torch.float64, device="cuda")
+        A.rhs(nus, alfas, tabs[0][0], us, uc, b)
+        x = torch.zeros_like(b)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sv = survey.Survey(A, nus)
+        code, stt = sv.solve(b, x, eps=float(args.dtm_eps), maxiter=50000, verify=True)
+        torch.cuda.synchronize()
+        t_solve += time.perf_counter() - t0
+        sv.close()
+        if code != 0:
+            raise RuntimeError(f"DTM solve failed: {stt}")
+        iters += stt["iterations"]
+        fp64 += stt["fp64_iterations"]
+        E, H, _ = R.fields(x, nus, alfas, tabs[0][0], us, uc)
+        out[f0:f0 + len(fb)] = R.mt_response(fb, np.arange(0, 2 * len(fb), 2),
+                                             np.arange(1, 2 * len(fb), 2), E, H).cpu().numpy()
+    pub = g["published"]          # [station][period][8]
+    n = len(st)
+    res = {}
+    for name, sl in (("x=northing,y=easting", slice(0, n)), ("x=northing,y=-easting", slice(n, 2 * n))):
+        o = out[:, sl].transpose(1, 0, 2)   # [station][period][34]
+        zerr = np.abs(o[..., 13:15] - pub[..., 1:3]) / pub[..., 1:3]
+        rerr = np.abs(o[..., 21:23] - pub[..., 5:7]) / pub[..., 5:7]
+        res[name] = {"Zxy_Zyx_rel_median": float(np.median(zerr)), "Zxy_Zyx_rel_p95": float(np.percentile(zerr, 95)),
+                     "Zxy_Zyx_rel_max": float(zerr.max()),
+                     "rho_xy_yx_rel_median": float(np.median(rerr)), "rho_xy_yx_rel_max": float(rerr.max()),
+                     "worst": {"station": st[int(np.argmax(zerr.max(axis=(1, 2))))].tolist()}}
+    print(json.dumps({"dtm": "625_500", "nb": m.nb, "cells": m.kpar, "periods": len(freqs),
+                      "systems": 2 * len(freqs), "stations": n, "solve_s": t_solve,
+                      "eps": float(args.dtm_eps), "iterations_max": int(max(iters)),
+                      "fp64_resolved_systems": int(sum(1 for v in fp64 if v > 0)),
+                      "vs_published": res}), flush=True)
+
+
 def profile_run(args):
     """A short fixed run for ncu: the device assembly, one COCR context,
     10 SpMV launches and 30 COCR iterations, then the batched solver on
@@ -642,7 +715,14 @@ def main():
                     help="time a whole survey in one batch (e.g. c2s, c3); see survey_run")
     ap.add_argument("--adjoint", action="store_true",
                     help="adjoint gradient on c5: timing and finite-difference check")
+    ap.add_argument("--dtm", action="store_true",
+                    help="the reference's published DTM case against its results table")
+    ap.add_argument("--dtm-eps", default=1e-8, type=float,
+                    help="relative residual of the DTM solves")
     args = ap.parse_args()
+    if args.dtm:
+        dtm_run(args)
+        return
     if args.adjoint:
         adjoint_run(args)
         return

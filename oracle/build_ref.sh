@@ -10,6 +10,7 @@
 #   COCR_FP      Code/COCR_FP/*.cpp      the reference solver (PCOCR_2x2_Folded)
 #   BuildMatrix  Code/BuildMatrix/*.cpp  the reference SLAE assembly
 #   Harm1D       Code/Harm1D/*.cpp       the reference 1-D normal field
+#   RegularMeshBuilder  Code/RegularMeshBuilder/*.cpp (two fixes streamed in, ref_fix_rmb.py)
 #   ref_receivers  Code/OutputNu/{T_Brick,OutputArbitrary,For_Solvers,in_out}.cpp
 #                plus ref_receivers_main.cpp: the receiver evaluation
 #
@@ -72,3 +73,19 @@ build_receivers() {
     echo "build_ref: $OUT/ref_receivers"
 }
 build_receivers
+
+# RegularMeshBuilder (Code/RegularMeshBuilder): main.cpp passes through
+# oracle/ref_fix_rmb.py (two compile/run fixes, streamed into the compiler;
+# no copy is written) and is built with BasicOperations.cpp.
+build_meshbuilder() {
+    local src="$REF/Code/RegularMeshBuilder"
+    local objdir="$OUT/obj_RegularMeshBuilder"
+    mkdir -p "$objdir"
+    local flags=("${COMMON[@]}" -include cmath -include cfloat -I "$src")
+    python3 "$HERE/ref_fix_rmb.py" "$REF" | "$CXX" "${flags[@]}" -x c++ -c - -o "$objdir/main.o" &
+    "$CXX" "${flags[@]}" -c "$src/BasicOperations.cpp" -o "$objdir/BasicOperations.o" &
+    wait
+    "$CXX" -o "$OUT/RegularMeshBuilder" "$objdir/main.o" "$objdir/BasicOperations.o"
+    echo "build_ref: $OUT/RegularMeshBuilder"
+}
+build_meshbuilder

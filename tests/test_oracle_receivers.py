@@ -167,3 +167,21 @@ def test_half_space_apparent_resistivity(sigma):
     assert abs(out[17]) == pytest.approx(135.0, abs=1e-4)        # phase of Zxy
     assert out[18] == pytest.approx(-45.0, abs=1e-4)             # phase of Zyx
     assert out[12] == 0.0 and out[15] == 0.0                     # Zxx = Zyy = 0
+
+
+def test_dtm_fixture_mesh():
+    """The fixture of the published DTM case rebuilds the reference
+    RegularMeshBuilder's mesh: air above z = 0, the 0.01 S/m half-space as
+    background everywhere below, the three objects' conductivities."""
+    from mtcalc_with_dfp_cocr_gb300 import mesh as M
+    g = np.load(os.path.join(GOLDEN, "dtm_625_500.npz"))
+    cm = g["cell_mat"].astype(np.int64)
+    layers = [M.Layer(float(t), float(s)) for t, s in zip(g["layer_tops"], g["layer_sigma"])]
+    m = M.RegularMesh(g["x"], g["y"], g["z"], layers, g["mat_sigma"][cm], g["mat_sigma0"][cm])
+    assert (m.nx, m.ny, m.nz) == (104, 144, 28) and m.nb == 1236064
+    zc = 0.5 * (g["z"][:-1] + g["z"][1:])
+    cz = np.repeat(zc, (m.nx - 1) * (m.ny - 1))
+    assert np.all(m.cell_sigma[cz > 0] == 1e-8)
+    assert np.all(m.cell_sigma0[cz < 0] == 0.01)
+    assert set(np.unique(m.cell_sigma[cz < 0])) == {1e-4, 1e-2, 1e-1, 1.0}
+    assert g["published"].shape == (53, 21, 8) and len(g["periods"]) == 21
