@@ -1,0 +1,124 @@
+"""Survey driver: a calculation directory in, the impedance table out.
+
+    python -m mtcalc_with_dfp_cocr_gb300.calc CASE_DIR [--out FILE]
+
+CASE_DIR holds the reference's five input files (frequencies, xyzVectorB,
+z_sig_2d, objects, settings.cfg; the reference's readme.txt documents
+them).  The driver does on one GPU what the reference's CalcStarter runs as
+separate programs per frequency and polarisation (RegularMeshBuilder,
+Harm1D, BuildMatrix, COCR_FP, OutputNu, then ImpedanceZToEdsAll and
+calcimpedance over all of them): the mesh (meshbuilder.py), the 1-D normal
+fields (normal1d.py), the device assembly, every frequency x polarisation
+through the batched solver (16 frequencies per batch), the receiver fields
+and the MT responses.
+
+The table has the layout of the reference's published results
+(CalculationResults/625_500_reg_R_Z.txt): per receiver and period,
+northing, easting, period, |Zxx| |Zxy| |Zyx| |Zyy| (Ohm) and the apparent
+resistivities Rxx Rxy Ryx Ryy (Ohm.m).  Northing is the model's x and
+easting its -y, the convention of that table.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+from . import meshbuilder, normal1d
+from .receivers import MT_RHO, MT_ZABS
+
+BATCH = 16   # frequencies per batch (x 2 polarisations = 32 systems)
+
+
+def run(case, eps=None, maxiter=None, device="cuda", log=None):
+    """Solve every frequency x polarisation of `case`; returns
+    (responses [nf][nrec][34], stats dict)."""
+    import torch
+    from .assembly import Assembly
+    from .receivers import Receivers
+    from .survey import Survey
+
+    eps = case.eps if eps is None else eps
+    maxiter = case.maxiter if maxiter is None else maxiter
+    t0 = time.perf_counter()
+    mesh = meshbuilder.build_mesh(case)
+    A = Assembly(mesh)
+    R = Receivers(A, case.receivers)
+    miss, _ = R.info()
+    tops = [l.top for l in case.layers]
+    sig = [l.sigma for l in case.layers]
+    freqs = np.asarray(case.freqs, np.float64)
+    out = np.empty((len(freqs), len(case.receivers), 34))
+    stats = {"nb": mesh.nb, "cells": mesh.kpar, "lines": [mesh.nx, mesh.ny, mesh.nz],
+             "receivers_outside_mesh": miss, "eps": eps, "systems": []}
+    for f0 in range(0, len(freqs), BATCH):
+        fb = freqs[f0:f0 + BATCH]
+        nus = np.repeat(fb, 2)
+        alfas = np.tile(np.array([1, 0], np.int32), len(fb))
+        tabs = [normal1d.solve_1d(f, tops, sig) for f in fb]
+        us = np.repeat(np.stack([t[1] for t in tabs]), 2, axis=0)
+        uc = np.repeat(np.stack([t[2] for t in tabs]), 2, axis=0)
+        b = torch.empty(len(nus), 2 * mesh.nb, dtype=torch.float64, device=device)
+        A.rhs(nus, alfas, tabs[0][0], us, uc, b)
+        x = torch.zeros_like(b)
+        sv = Survey(A, nus)
+        code, st = sv.solve(b, x, eps=eps, maxiter=maxiter, verify=True)
+        sv.close()
+        for k in range(len(nus)):
+            stats["systems"].append({
+                "nu": float(nus[k]), "polarisation": "XY"[1 - int(alfas[k])],
+                "status": st["status"][k], "iterations": st["iterations"][k],
+                "fp64_iterations": st["fp64_iterations"][k],
+                "true_residual_rel": st["true_residual_rel"][k]})
+        if log:
+            log(f"frequencies {f0 + 1}-{f0 + len(fb)} of {len(freqs)}: code {code}, "
+                f"iterations {max(st['iterations'])}")
+        E, H, _ = R.fields(x, nus, alfas, tabs[0][0], us, uc)
+        out[f0:f0 + len(fb)] = R.mt_response(
+            fb, np.arange(0, 2 * len(fb), 2), np.arange(1, 2 * len(fb), 2), E, H).cpu().numpy()
+    stats["seconds"] = time.perf_counter() - t0
+    return out, stats
+
+
+def write_table(path, case, resp):
+    """The published results' layout: one row per receiver and period
+    (periods ascending), tab-separated."""
+    freqs = np.asarray(case.freqs, np.float64)
+    order = np.argsort(1.0 / freqs)
+    with open(path, "w") as f:
+        f.write("northing (m)\teasting (m)\tperiods (s)\t\t\tZxx (Ohm)\t\t\tZxy (Ohm)\t\t\t"
+                "Zyx (Ohm)\t\t\tZyy (Ohm)\t\t\tRxx (Ohm)\t\t\tRxy (Ohm)\t\t\tRyx (Ohm)\t\t\t"
+                "Ryy (Ohm)\t\n")
+        for r, (x, y, _) in enumerate(case.receivers):
+            for i in order:
+                o = resp[i, r]
+                vals = list(o[MT_ZABS:MT_ZABS + 4]) + list(o[MT_RHO:MT_RHO + 4])
+                f.write(f"{x:g}\t\t\t{-y + 0.0:g}\t\t{1.0 / freqs[i]:e}\t\t" +
+                        "\t\t".join(f"{v:e}" for v in vals) + "\n")
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("case", help="directory with frequencies, xyzVectorB, z_sig_2d, objects, "
+                                 "settings.cfg")
+    ap.add_argument("--out", default=None, help="results table (default CASE/results_R_Z.txt)")
+    ap.add_argument("--eps", type=float, default=None,
+                    help="relative residual of the solves (default: settings.cfg's)")
+    ap.add_argument("--maxiter", type=int, default=None)
+    a = ap.parse_args(argv)
+    case = meshbuilder.read_case(a.case)
+    resp, stats = run(case, a.eps, a.maxiter, log=lambda s: print(s, file=sys.stderr))
+    out = a.out or os.path.join(a.case, "results_R_Z.txt")
+    write_table(out, case, resp)
+    with open(os.path.splitext(out)[0] + "_stats.json", "w") as f:
+        json.dump(stats, f, indent=1)
+    print(f"{out}: {len(case.receivers)} receivers x {len(case.freqs)} periods, "
+          f"{stats['seconds']:.1f} s", file=sys.stderr)
+
+
+if __name__ == "__main__":
+    main()

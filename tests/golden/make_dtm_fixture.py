@@ -13,10 +13,14 @@ what a solve needs, compactly:
   mat_sigma, mat_sigma0   conductivity and normal-field conductivity per material
   layer_tops, layer_sigma the 1-D background (bottom-up; tops, last 0)
   receivers           (53, 3), the example's xyzVectorB
+  objects, settings   the example's objects (x1 x2 y1 y2 z1 z2 sigma) and the
+                      first four rows of its settings.cfg
   stations            (53, 2): the table's (northing, easting), in table order
   periods             (21,) seconds
   published           (53, 21, 8) per station and period: |Zxx| |Zxy| |Zyx| |Zyy|
                       (Ohm), Rxx Rxy Ryx Ryy (Ohm.m)
+  ex_*                the same mesh arrays for the example's own settings.cfg
+                      (2500 m / 500 m steps)
 
 Usage (needs the reference; not run by the tests):
     python tests/golden/make_dtm_fixture.py [--ref /root/reference]
@@ -42,22 +46,17 @@ def read_settings(path):
     return rows
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
-    a = ap.parse_args()
-    subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), a.ref])
-    ex = os.path.join(a.ref, "CalculationExample")
-    s = read_settings(os.path.join(ex, "settings.cfg"))
+def run_builder(ex, s, steps):
+    """The reference RegularMeshBuilder on the example's inputs with the given
+    (lateral, vertical) steps, the other settings as in the example:
+    (x, y, z lines, 0-based cell materials, material table [index, sigma, sigma0])."""
     d = tempfile.mkdtemp(prefix="dtm_")
     try:
         for n in ("objects", "z_sig_2d", "xyzVectorB"):
             shutil.copy(os.path.join(ex, n), d)
-        # the published run: 625 m lateral, 500 m vertical steps; the other
-        # settings as in the example
         with open(os.path.join(d, "RegularMeshBuilderSettings.cfg"), "w") as f:
-            f.write(f"625 500\n{s[1][0]} {s[1][1]}\n{s[2][0]} {s[2][1]}\n{s[3][0]} {s[3][1]}\n"
-                    f"X\n1\n1\n{s[4][0]}\n{s[5][0]}\n")
+            f.write(f"{steps[0]} {steps[1]}\n{s[1][0]} {s[1][1]}\n{s[2][0]} {s[2][1]}\n"
+                    f"{s[3][0]} {s[3][1]}\nX\n1\n1\n{s[4][0]}\n{s[5][0]}\n")
         subprocess.check_call([os.path.join(REF_BIN, "RegularMeshBuilder")], cwd=d,
                               stdout=subprocess.DEVNULL)
         xyz = np.fromfile(os.path.join(d, "xyz.dat")).reshape(-1, 3)
@@ -65,15 +64,32 @@ def main():
         assert len(x) * len(y) * len(z) == len(xyz)
         nvkat = np.fromfile(os.path.join(d, "nvkat.dat"), "<i4") - 1
         sig = np.loadtxt(os.path.join(d, "Sig3d"))
-        mats = sig[np.argsort(sig[:, 0])]
-        with open(os.path.join(d, "z_sig_2d")) as f:
-            n = int(f.readline())
-            lay = np.array([list(map(float, f.readline().split())) for _ in range(n)])
-        with open(os.path.join(d, "xyzVectorB")) as f:
-            nr = int(f.readline())
-            rec = np.array([list(map(float, f.readline().split())) for _ in range(nr)])
     finally:
         shutil.rmtree(d, ignore_errors=True)
+    return x, y, z, nvkat, sig[np.argsort(sig[:, 0])]
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    a = ap.parse_args()
+    subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), a.ref])
+    ex = os.path.join(a.ref, "CalculationExample")
+    s = read_settings(os.path.join(ex, "settings.cfg"))
+    # the published run: 625 m lateral, 500 m vertical steps
+    x, y, z, nvkat, mats = run_builder(ex, s, ("625", "500"))
+    # the example's own settings
+    x2, y2, z2, nvkat2, mats2 = run_builder(ex, s, (s[0][0], s[0][1]))
+    with open(os.path.join(ex, "z_sig_2d")) as f:
+        n = int(f.readline())
+        lay = np.array([list(map(float, f.readline().split())) for _ in range(n)])
+    with open(os.path.join(ex, "xyzVectorB")) as f:
+        nr = int(f.readline())
+        rec = np.array([list(map(float, f.readline().split())) for _ in range(nr)])
+    with open(os.path.join(ex, "objects")) as f:
+        no = int(f.readline())
+        objects = np.array([list(map(float, f.readline().split())) for _ in range(no)])
+    settings = np.array([[float(v) for v in row[:2]] for row in s[:4]])
     tab = np.loadtxt(os.path.join(a.ref, "CalculationResults", "625_500_reg_R_Z.txt"), skiprows=1)
     periods = np.unique(tab[:, 2])
     # the table's own stations (northing, easting), in first-appearance order;
@@ -95,7 +111,8 @@ def main():
         os.path.join(HERE, "dtm_625_500.npz"), x=x, y=y, z=z, cell_mat=nvkat.astype(np.uint8),
         mat_sigma=mats[:, 1], mat_sigma0=mats[:, 2], layer_tops=lay[:, 0],
         layer_sigma=lay[:, 1], receivers=rec, stations=stations, periods=periods,
-        published=pub)
+        published=pub, objects=objects, settings=settings, ex_x=x2, ex_y=y2, ex_z=z2, ex_cell_mat=nvkat2.astype(np.uint8),
+        ex_mat_sigma=mats2[:, 1], ex_mat_sigma0=mats2[:, 2])
     print("mesh", len(x), len(y), len(z), "cells", len(nvkat), "materials", len(mats),
           "receivers", len(rec), "periods", len(periods))
 

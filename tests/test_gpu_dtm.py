@@ -1,50 +1,63 @@
 """The reference's published DTM results (CalculationResults/625_500_reg_R_Z.txt)
-reproduced end to end on the GPU: the reference RegularMeshBuilder's mesh of
-the example model (tests/golden/dtm_625_500.npz), device assembly, batched
-solve, receiver fields and MT responses.  The table was computed with the
-reference's smoothing output path and FP32 post-processing, so the check is
-at the percent level.  The table's easting axis is the model's -y."""
+reproduced end to end on the GPU through the survey driver: the reference's
+input files of the example model (written from tests/golden/dtm_625_500.npz)
+with 625/500 m steps, the mesh builder, device assembly, batched solves,
+receiver fields, MT responses and the results table.  The table was computed
+with the reference's smoothing output path and FP32 post-processing, so the
+check is at the percent level."""
 import os
 
 import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from mtcalc_with_dfp_cocr_gb300 import assembly, mesh as M, normal1d, receivers, survey
+from mtcalc_with_dfp_cocr_gb300 import calc
 
 pytestmark = pytest.mark.gpu
 
+PICK = [4, 8, 12, 16]   # periods 1, 10, 100, 1000 s
 
-def test_dtm_impedances_match_published_table(gpu):
-    torch = gpu
-    g = np.load(os.path.join(GOLDEN, "dtm_625_500.npz"))
-    cm = g["cell_mat"].astype(np.int64)
-    layers = [M.Layer(float(t), float(s)) for t, s in zip(g["layer_tops"], g["layer_sigma"])]
-    m = M.RegularMesh(g["x"], g["y"], g["z"], layers, g["mat_sigma"][cm], g["mat_sigma0"][cm])
-    periods = g["periods"]
-    pick = [4, 8, 12, 16]                      # 1, 10, 100, 1000 s
-    fb = 1.0 / periods[pick]
+
+def _f(v):
+    return repr(float(v))
+
+
+def write_case(d, g, periods, eps):
     st = g["stations"]
-    pts = np.c_[st[:, 0], -st[:, 1], np.zeros(len(st))]
-    A = assembly.Assembly(m)
-    R = receivers.Receivers(A, pts)
-    tops, sig = [l.top for l in layers], [l.sigma for l in layers]
-    nus = np.repeat(fb, 2)
-    alfas = np.tile([1, 0], len(fb))
-    tabs = [normal1d.solve_1d(f, tops, sig) for f in fb]
-    us = np.repeat(np.stack([t[1] for t in tabs]), 2, axis=0)
-    uc = np.repeat(np.stack([t[2] for t in tabs]), 2, axis=0)
-    b = torch.empty(len(nus), 2 * m.nb, dtype=torch.float64, device="cuda")
-    A.rhs(nus, alfas, tabs[0][0], us, uc, b)
-    x = torch.zeros_like(b)
-    code, stt = survey.Survey(A, nus).solve(b, x, eps=1e-8, maxiter=50000, verify=True)
-    assert code == 0 and max(stt["true_residual_rel"]) < 1e-8
-    E, H, _ = R.fields(x, nus, alfas, tabs[0][0], us, uc)
-    out = R.mt_response(fb, np.arange(0, 2 * len(fb), 2), np.arange(1, 2 * len(fb), 2),
-                        E, H).cpu().numpy().transpose(1, 0, 2)
-    pub = g["published"][:, pick]
-    z_err = np.abs(out[..., 13:15] - pub[..., 1:3]) / pub[..., 1:3]
-    r_err = np.abs(out[..., 21:23] - pub[..., 5:7]) / pub[..., 5:7]
+    with open(os.path.join(d, "frequencies"), "w") as f:
+        f.write(f"{len(periods)}\n" + "".join(f"{_f(1.0 / p)}\n" for p in periods))
+    with open(os.path.join(d, "xyzVectorB"), "w") as f:
+        # the table's easting is the model's -y
+        f.write(f"{len(st)}\n" + "".join(f"{_f(n)} {_f(-e + 0.0)} 0\n" for n, e in st))
+    with open(os.path.join(d, "z_sig_2d"), "w") as f:
+        f.write(f"{len(g['layer_tops'])}\n" +
+                "".join(f"{_f(t)} {_f(s)}\n" for t, s in zip(g["layer_tops"], g["layer_sigma"])))
+    with open(os.path.join(d, "objects"), "w") as f:
+        f.write(f"{len(g['objects'])}\n" +
+                "".join(" ".join(_f(v) for v in o) + "\n" for o in g["objects"]))
+    s = g["settings"]
+    with open(os.path.join(d, "settings.cfg"), "w") as f:
+        f.write(f"625 500\n{_f(s[1][0])} {_f(s[1][1])}\n{_f(s[2][0])} {_f(s[2][1])}\n"
+                f"{_f(s[3][0])} {_f(s[3][1])}\n{_f(eps)}\n50000\n")
+
+
+def test_dtm_through_the_driver_matches_published_table(gpu, tmp_path):
+    g = np.load(os.path.join(GOLDEN, "dtm_625_500.npz"))
+    periods = g["periods"][PICK]
+    write_case(str(tmp_path), g, periods, 1e-8)
+    out = str(tmp_path / "results.txt")
+    calc.main([str(tmp_path), "--out", out])
+    tab = np.loadtxt(out, skiprows=1)
+    assert tab.shape == (len(g["stations"]) * len(periods), 11)
+    pub = g["published"][:, PICK]
+    z_err, r_err = [], []
+    for row in tab:
+        r = np.nonzero((g["stations"][:, 0] == row[0]) & (g["stations"][:, 1] == row[1]))[0]
+        p = np.nonzero(np.isclose(periods, row[2], rtol=1e-6))[0]
+        assert len(r) == 1 and len(p) == 1
+        ref = pub[r[0], p[0]]
+        z_err += list(np.abs(row[4:6] - ref[1:3]) / ref[1:3])
+        r_err += list(np.abs(row[8:10] - ref[5:7]) / ref[5:7])
     assert np.median(z_err) < 0.005
-    assert z_err.max() < 0.03
-    assert r_err.max() < 0.06
+    assert max(z_err) < 0.03
+    assert max(r_err) < 0.06

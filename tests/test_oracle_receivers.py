@@ -185,3 +185,44 @@ def test_dtm_fixture_mesh():
     assert np.all(m.cell_sigma0[cz < 0] == 0.01)
     assert set(np.unique(m.cell_sigma[cz < 0])) == {1e-4, 1e-2, 1e-1, 1.0}
     assert g["published"].shape == (53, 21, 8) and len(g["periods"]) == 21
+
+
+@pytest.mark.parametrize("prefix,steps", [("", (625.0, 500.0)), ("ex_", None)])
+def test_meshbuilder_matches_reference_builder(prefix, steps):
+    """meshbuilder.build_mesh on the reference's example inputs reproduces
+    the reference RegularMeshBuilder's mesh lines bit for bit and its cell
+    conductivities, at the published run's 625/500 m steps and at the
+    example's own settings."""
+    from mtcalc_with_dfp_cocr_gb300 import meshbuilder as MB
+    g = np.load(os.path.join(GOLDEN, "dtm_625_500.npz"))
+    case = MB.Case(
+        freqs=1.0 / g["periods"], receivers=g["receivers"],
+        layers=[MB.Layer(float(t), float(s)) for t, s in zip(g["layer_tops"], g["layer_sigma"])],
+        objects=g["objects"], steps=steps or tuple(g["settings"][0]),
+        sparse=tuple(g["settings"][1]), gap=tuple(g["settings"][2]),
+        far=tuple(g["settings"][3]), eps=1e-4, maxiter=10000)
+    m = MB.build_mesh(case)
+    for a, b in ((m.x, g[prefix + "x"]), (m.y, g[prefix + "y"]), (m.z, g[prefix + "z"])):
+        np.testing.assert_array_equal(a, b)
+    cm = g[prefix + "cell_mat"].astype(np.int64)
+    np.testing.assert_array_equal(m.cell_sigma, g[prefix + "mat_sigma"][cm])
+    np.testing.assert_array_equal(m.cell_sigma0, g[prefix + "mat_sigma0"][cm])
+
+
+def test_driver_table_layout(tmp_path):
+    """The survey driver's results table has the published table's layout:
+    per receiver and ascending period, northing = x, easting = -y, |Z| and
+    rho_a of the four components."""
+    from mtcalc_with_dfp_cocr_gb300 import calc, meshbuilder as MB
+    case = MB.Case(freqs=np.array([0.1, 10.0]), receivers=np.array([[1.0, 2.0, 0.0]]),
+                   layers=[MB.Layer(0.0, 0.01)], objects=np.zeros((0, 7)),
+                   steps=(100.0, 100.0), sparse=(1.5, 1.5), gap=(100.0, 100.0),
+                   far=(1000.0, 1000.0), eps=1e-8, maxiter=10)
+    resp = np.zeros((2, 1, 34))
+    resp[:, 0, 12:16] = [[1, 2, 3, 4], [5, 6, 7, 8]]
+    resp[:, 0, 20:24] = [[9, 10, 11, 12], [13, 14, 15, 16]]
+    out = str(tmp_path / "t.txt")
+    calc.write_table(out, case, resp)
+    tab = np.loadtxt(out, skiprows=1)
+    np.testing.assert_allclose(tab[0], [1, -2, 0.1, 5, 6, 7, 8, 13, 14, 15, 16])
+    np.testing.assert_allclose(tab[1], [1, -2, 10.0, 1, 2, 3, 4, 9, 10, 11, 12])
