@@ -265,16 +265,17 @@ int mtgpu_survey_solve(mtgpu_survey *s, const double *d_b, double *d_x, double e
  * CUDA events on the survey's stream; *ms receives the total. */
 int mtgpu_survey_spmv_timed(mtgpu_survey *s, int reps, float *ms);
 
-/* The SpMV variant the set-up autotuning chose (0: x staged in shared memory
- * per tile of slices; 2, 4, 8: slots in flight per thread, gathers from
- * global memory) and the times (ms per launch) it measured for the variants
- * 0, 2, 4, 8 (ms[4]; 0 where a variant was not available). */
+/* The SpMV variant the set-up autotuning chose (0: x segments and matrix
+ * slots staged in shared memory per tile of slices; 1: x segments staged
+ * only; 2, 4, 8: slots in flight per thread, gathers from global memory) and
+ * the times (ms per launch) it measured for the variants 0, 1, 2, 4, 8
+ * (ms[5]; 0 where a variant was not available). */
 int mtgpu_survey_tuning(const mtgpu_survey *s, int *variant, float *ms);
 
-/* Pins the SpMV variant (0, 2, 4 or 8) instead of the autotuned choice; all
- * variants give bitwise the same products.  MTGPU_ERR_ARG if the variant is
- * unknown or unavailable for this survey (variant 0 needs its tiles to fit
- * shared memory). */
+/* Pins the SpMV variant (0, 1, 2, 4 or 8) instead of the autotuned choice;
+ * all variants sum the same products in the same order.  MTGPU_ERR_ARG if
+ * the variant is unknown or unavailable for this survey (0 and 1 need their
+ * tiles to fit shared memory). */
 int mtgpu_survey_set_spmv_variant(mtgpu_survey *s, int variant);
 
 void mtgpu_survey_destroy(mtgpu_survey *s);

@@ -262,17 +262,17 @@ int mtgpu_survey_tuning(const mtgpu_survey *s, int *variant, float *ms)
     MTGPU_CHECK_ARG(s != nullptr, "null survey");
     if (variant) *variant = s->V.ch;
     if (ms)
-        for (int i = 0; i < 4; i++) ms[i] = s->V.tune_ms[i];
+        for (int i = 0; i < 5; i++) ms[i] = s->V.tune_ms[i];
     return MTGPU_OK;
 }
 
 int mtgpu_survey_set_spmv_variant(mtgpu_survey *s, int variant)
 {
     MTGPU_CHECK_ARG(s != nullptr, "null survey");
-    MTGPU_CHECK_ARG(variant == 0 || variant == 2 || variant == 4 || variant == 8,
-                    "SpMV variant must be 0, 2, 4 or 8");
-    MTGPU_CHECK_ARG(variant != 0 || s->V.ntiles > 0,
-                    "the tiled SpMV variant is not available for this survey");
+    MTGPU_CHECK_ARG(variant == 0 || variant == 1 || variant == 2 || variant == 4 || variant == 8,
+                    "SpMV variant must be 0, 1, 2, 4 or 8");
+    MTGPU_CHECK_ARG(variant > 1 || s->V.ntiles > 0,
+                    "the tiled SpMV variants are not available for this survey");
     return survey_set_variant(s->V, variant);
 }
 

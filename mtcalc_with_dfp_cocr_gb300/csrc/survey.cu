@@ -387,19 +387,32 @@ k_update(int n, const float4 *__restrict__ p, const float4 *__restrict__ a,
     const dfc nal{neg(al.re), neg(al.im)};
     acc su, uu;
     const int rpb = kB / SP;
-    for (int e = blockIdx.x * rpb + threadIdx.x / SP; e < n; e += gridDim.x * rpb) {
+    const int stride = gridDim.x * rpb;
+    // two elements per pass, all 14 loads issued before any store
+    for (int e = blockIdx.x * rpb + threadIdx.x / SP; e < n; e += 2 * stride) {
         if (!on) continue;
-        const long long idx = (long long)e * SP + k;
-        const float4 pv = __ldg(p + idx), av = __ldg(a + idx), wv = __ldg(w + idx),
-                     smv = __ldg(sm + idx), xv = x[idx], rv = r[idx], sv = s[idx];
-        const dfc rn = caxpy(from4(rv), nal, from4(av));
-        x[idx] = to4(caxpy(from4(xv), al, from4(pv)));
-        r[idx] = to4(rn);
-        s[idx] = to4(caxpy(from4(sv), nal, from4(wv)));
-        const dfc smd = from4(smv);
-        const df ur = add(rn.re, neg(smd.re)), ui = add(rn.im, neg(smd.im));
-        su.mac(smd.re, ur); su.mac(smd.im, ui);
-        uu.mac(ur, ur); uu.mac(ui, ui);
+        const bool two = e + stride < n;
+        float4 v[2][7];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            if (u == 1 && !two) break;
+            const long long idx = (long long)(e + u * stride) * SP + k;
+            v[u][0] = __ldg(p + idx); v[u][1] = __ldg(a + idx); v[u][2] = __ldg(w + idx);
+            v[u][3] = __ldg(sm + idx); v[u][4] = x[idx]; v[u][5] = r[idx]; v[u][6] = s[idx];
+        }
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            if (u == 1 && !two) break;
+            const long long idx = (long long)(e + u * stride) * SP + k;
+            const dfc rn = caxpy(from4(v[u][5]), nal, from4(v[u][1]));
+            x[idx] = to4(caxpy(from4(v[u][4]), al, from4(v[u][0])));
+            r[idx] = to4(rn);
+            s[idx] = to4(caxpy(from4(v[u][6]), nal, from4(v[u][2])));
+            const dfc smd = from4(v[u][3]);
+            const df ur = add(rn.re, neg(smd.re)), ui = add(rn.im, neg(smd.im));
+            su.mac(smd.re, ur); su.mac(smd.im, ui);
+            uu.mac(ur, ur); uu.mac(ui, ui);
+        }
     }
     double v[2] = {su.to_double(), uu.to_double()};
     __shared__ double tot[2][32];
@@ -539,6 +552,13 @@ __host__ __device__ __forceinline__ long long tile_bytes(int nu, int SP, long lo
     return (long long)nu * SP * 16 + nc * 8 * 2 + nr * 8 + nc * 2 + nr * 2;
 }
 
+// a value from shared memory (plain load) or from global memory (read-only path)
+template <class T>
+__device__ __forceinline__ T ldv(const T *p, bool shared)
+{
+    return shared ? *p : __ldg(p);
+}
+
 // threads of the x-staged SpMV block: a tile of T slices in whole passes
 template <int SP>
 struct TileCfg {
@@ -547,7 +567,9 @@ struct TileCfg {
     static constexpr int T = SP >= 16 ? 1 : (SP == 1 ? 8 : (16 / SP < 8 ? 16 / SP : 8));
 };
 
-template <int SP>
+// MAT: also stage the tile's matrix slots (else they stream from global
+// memory, each used once)
+template <int SP, bool MAT>
 __global__ void __launch_bounds__(TileCfg<SP>::NT)
 k_spmv_t(int nb, TileMat A, const float2 *__restrict__ omega, const float4 *__restrict__ s,
          const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
@@ -565,26 +587,34 @@ k_spmv_t(int nb, TileMat A, const float2 *__restrict__ omega, const float4 *__re
         const long long c0 = A.pc[s0], nc = A.pc[s1] - c0, q0 = A.pr[s0], nr = A.pr[s1] - q0;
         const int u0 = A.uoff[t], nu = A.uoff[t + 1] - u0;
         float4 *xs = reinterpret_cast<float4 *>(smem);
-        float2 *skc = reinterpret_cast<float2 *>(xs + (long long)nu * SP);
-        float2 *smc = skc + nc;
-        float2 *skr = smc + nc;
-        unsigned short *slc = reinterpret_cast<unsigned short *>(skr + nr);
-        unsigned short *slr = slc + nc;
+        // matrix slots: shared memory after x, or global memory from the tile's start
+        const float2 *skc, *smc, *skr;
+        const unsigned short *slc, *slr;
         __syncthreads();   // the previous tile's readers are done
         constexpr int NT = TileCfg<SP>::NT;
         for (int i = threadIdx.x; i < nu * SP; i += NT)
             cp_async16(xs + i, s + (long long)__ldg(A.ucol + u0 + i / SP) * SP + i % SP);
-        // slot counts are multiples of 32: whole 16-byte chunks, 16-byte aligned
-        for (long long i = threadIdx.x; i < nc / 2; i += NT) {
-            cp_async16(reinterpret_cast<float4 *>(skc) + i, reinterpret_cast<const float4 *>(A.kc + c0) + i);
-            cp_async16(reinterpret_cast<float4 *>(smc) + i, reinterpret_cast<const float4 *>(A.mc + c0) + i);
+        if (MAT) {
+            float2 *kc2 = reinterpret_cast<float2 *>(xs + (long long)nu * SP);
+            float2 *mc2 = kc2 + nc;
+            float2 *kr2 = mc2 + nc;
+            unsigned short *lc2 = reinterpret_cast<unsigned short *>(kr2 + nr);
+            unsigned short *lr2 = lc2 + nc;
+            // slot counts are multiples of 32: whole 16-byte chunks, 16-byte aligned
+            for (long long i = threadIdx.x; i < nc / 2; i += NT) {
+                cp_async16(reinterpret_cast<float4 *>(kc2) + i, reinterpret_cast<const float4 *>(A.kc + c0) + i);
+                cp_async16(reinterpret_cast<float4 *>(mc2) + i, reinterpret_cast<const float4 *>(A.mc + c0) + i);
+            }
+            for (long long i = threadIdx.x; i < nr / 2; i += NT)
+                cp_async16(reinterpret_cast<float4 *>(kr2) + i, reinterpret_cast<const float4 *>(A.kr + q0) + i);
+            for (long long i = threadIdx.x; i < nc / 8; i += NT)
+                cp_async16(reinterpret_cast<float4 *>(lc2) + i, reinterpret_cast<const float4 *>(A.lc + c0) + i);
+            for (long long i = threadIdx.x; i < nr / 8; i += NT)
+                cp_async16(reinterpret_cast<float4 *>(lr2) + i, reinterpret_cast<const float4 *>(A.lr + q0) + i);
+            skc = kc2; smc = mc2; skr = kr2; slc = lc2; slr = lr2;
+        } else {
+            skc = A.kc + c0; smc = A.mc + c0; skr = A.kr + q0; slc = A.lc + c0; slr = A.lr + q0;
         }
-        for (long long i = threadIdx.x; i < nr / 2; i += NT)
-            cp_async16(reinterpret_cast<float4 *>(skr) + i, reinterpret_cast<const float4 *>(A.kr + q0) + i);
-        for (long long i = threadIdx.x; i < nc / 8; i += NT)
-            cp_async16(reinterpret_cast<float4 *>(slc) + i, reinterpret_cast<const float4 *>(A.lc + c0) + i);
-        for (long long i = threadIdx.x; i < nr / 8; i += NT)
-            cp_async16(reinterpret_cast<float4 *>(slr) + i, reinterpret_cast<const float4 *>(A.lr + q0) + i);
         cp_async_wait_all();
         __syncthreads();
         if (!on) continue;
@@ -598,8 +628,8 @@ k_spmv_t(int nb, TileMat A, const float2 *__restrict__ omega, const float4 *__re
 #pragma unroll 4
                 for (int q = 0; q < n; q++) {
                     const int t2 = b + 32 * q;
-                    const float4 xv = xs[slc[t2] * SP + k];
-                    const df kd = d2f(skc[t2]), md = d2f(smc[t2]);
+                    const float4 xv = xs[ldv(slc + t2, MAT) * SP + k];
+                    const df kd = d2f(ldv(skc + t2, MAT)), md = d2f(ldv(smc + t2, MAT));
                     const df xr{xv.x, xv.y}, xi{xv.z, xv.w};
                     kr_.mac(kd, xr);
                     ki_.mac(kd, xi);
@@ -612,8 +642,8 @@ k_spmv_t(int nb, TileMat A, const float2 *__restrict__ omega, const float4 *__re
 #pragma unroll 4
                 for (int q = 0; q < n; q++) {
                     const int t2 = b + 32 * q;
-                    const float4 xv = xs[slr[t2] * SP + k];
-                    const df kd = d2f(skr[t2]);
+                    const float4 xv = xs[ldv(slr + t2, MAT) * SP + k];
+                    const df kd = d2f(ldv(skr + t2, MAT));
                     kr_.mac(kd, df{xv.x, xv.y});
                     ki_.mac(kd, df{xv.z, xv.w});
                 }
@@ -956,7 +986,12 @@ struct Impl {
     {
         const Mat A = mat(V);
         if (V.ch == 0) {
-            k_spmv_t<SP><<<V.g_spmv_t, TileCfg<SP>::NT, V.tile_smem, V.st>>>(
+            k_spmv_t<SP, true><<<V.g_spmv_t, TileCfg<SP>::NT, V.tile_smem, V.st>>>(
+                V.nb, tmat(V), V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode);
+            return;
+        }
+        if (V.ch == 1) {
+            k_spmv_t<SP, false><<<V.g_spmv_tx, TileCfg<SP>::NT, V.tile_smem_x, V.st>>>(
                 V.nb, tmat(V), V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode);
             return;
         }
@@ -1029,18 +1064,26 @@ struct Impl {
         V.g_spmv = g(fs, V.grid_rows);
         if (V.ntiles > 0) {
             int b = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (const void *)k_spmv_t<SP>,
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (const void *)k_spmv_t<SP, true>,
                                                               TileCfg<SP>::NT, V.tile_smem) !=
                     cudaSuccess || b < 1)
                 b = 1;
             V.g_spmv_t = std::max(1, std::min(b * nsm, V.ntiles));
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (const void *)k_spmv_t<SP, false>,
+                                                              TileCfg<SP>::NT, V.tile_smem_x) !=
+                    cudaSuccess || b < 1)
+                b = 1;
+            V.g_spmv_tx = std::max(1, std::min(b * nsm, V.ntiles));
         }
     }
     static void tile_slices_of(int *T) { *T = TileCfg<SP>::T; }
     static void tile_attr(Survey &V, cudaError_t *e)
     {
-        *e = cudaFuncSetAttribute((const void *)k_spmv_t<SP>,
+        *e = cudaFuncSetAttribute((const void *)k_spmv_t<SP, true>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, V.tile_smem);
+        if (*e == cudaSuccess)
+            *e = cudaFuncSetAttribute((const void *)k_spmv_t<SP, false>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, V.tile_smem_x);
     }
 };
 
@@ -1106,11 +1149,12 @@ int build_tiles(Survey &V, int nsm)
     MTGPU_TRY(cudaMemcpyAsync(pr.data(), P.d_pr, sizeof(long long) * pr.size(), cudaMemcpyDeviceToHost, V.st));
     MTGPU_TRY(cudaStreamSynchronize(V.st));
     if (over) return done(MTGPU_OK);
-    long long smem = 0;
+    long long smem = 0, smem_x = 0;
     for (int t = 0; t < nt; t++) {
         off[t + 1] = off[t] + count[t];
         const int s0 = t * V.tile_T, s1 = std::min(s0 + V.tile_T, P.nslices);
         smem = std::max(smem, tile_bytes(count[t], V.SP, pc[s1] - pc[s0], pr[s1] - pr[s0]));
+        smem_x = std::max(smem_x, tile_bytes(count[t], V.SP, 0, 0));
     }
     int max_smem = 0;
     int dev = 0;
@@ -1126,6 +1170,7 @@ int build_tiles(Survey &V, int nsm)
     MTGPU_TRY(cudaGetLastError());
     MTGPU_TRY(cudaStreamSynchronize(V.st));
     V.tile_smem = (int)smem;
+    V.tile_smem_x = (int)smem_x;
     cudaError_t e = cudaSuccess;
     MTGPU_SP_DISPATCH(V.SP, tile_attr(V, &e));
     if (e != cudaSuccess) {
@@ -1218,11 +1263,11 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
     if ((rc = build_tiles(V, nsm))) return rc;
     // autotune the SpMV variant: time each candidate, keep the fastest
     {
-        const int cand[4] = {0, 2, 4, 8};
+        const int cand[5] = {0, 1, 2, 4, 8};
         float best = 1e30f;
         int best_ch = 4;
-        for (int c = 0; c < 4; c++) {
-            if (cand[c] == 0 && V.ntiles == 0) continue;
+        for (int c = 0; c < 5; c++) {
+            if (cand[c] <= 1 && V.ntiles == 0) continue;
             V.ch = cand[c];
             MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
             float ms = 0.f;

@@ -29,12 +29,14 @@ struct Survey {
     int nb = 0, S = 0, SP = 1;
     int grid_rows = 0, grid_nodes = 0;           // work bounds (blocks that have rows)
     int g_init = 0, g_node = 0, g_edge = 0, g_update = 0, g_spmv = 0, g_true = 0;  // launch grids
-    int ch = 4;    // SpMV variant: 0 tiled (x staged in shared memory), else slots in flight (2, 4, 8); autotuned
+    // SpMV variant (autotuned): 0 x and matrix slots staged in shared memory per
+    // tile, 1 x staged only, 2/4/8 gathers from global memory with that many slots in flight
+    int ch = 4;
     // SpMV tiles: T consecutive SELL slices, their distinct columns, per-slot local indices
-    int tile_T = 1, ntiles = 0, tile_smem = 0, g_spmv_t = 0;
+    int tile_T = 1, ntiles = 0, tile_smem = 0, tile_smem_x = 0, g_spmv_t = 0, g_spmv_tx = 0;
     int *uoff = nullptr, *ucol = nullptr;
     unsigned short *lc = nullptr, *lr = nullptr;
-    float tune_ms[4] = {0.f, 0.f, 0.f, 0.f};     // SpMV times of the variants tiled, 2, 4, 8
+    float tune_ms[5] = {0.f, 0.f, 0.f, 0.f, 0.f};  // SpMV times of the variants 0, 1, 2, 4, 8
     Folded G;                                    // pattern of G and G^T
     float2 *kc = nullptr, *mc = nullptr, *kr = nullptr;   // double-float K and M per slot
     float *gv32 = nullptr, *tv32 = nullptr;      // values of G and G^T (+-1/2, exact in FP32)

@@ -53,15 +53,16 @@ class Survey:
 
     def tuning(self):
         """(chosen SpMV variant, {variant: ms per launch}) of the set-up
-        autotuning; variant 0 stages x in shared memory per tile."""
+        autotuning; variants 0 and 1 stage x in shared memory per tile."""
         v = C.c_int()
-        ms = (C.c_float * 4)()
+        ms = (C.c_float * 5)()
         _lib.check(_lib.lib().mtgpu_survey_tuning(self._h, C.byref(v), ms),
                    "mtgpu_survey_tuning")
-        return v.value, {c: ms[i] for i, c in enumerate((0, 2, 4, 8)) if ms[i] > 0}
+        return v.value, {c: ms[i] for i, c in enumerate((0, 1, 2, 4, 8)) if ms[i] > 0}
 
     def set_spmv_variant(self, variant):
-        """Pin the SpMV variant (0 tiled, 2, 4, 8) instead of the autotuned one."""
+        """Pin the SpMV variant (0 x and matrix staged, 1 x staged, 2, 4, 8
+        slots in flight) instead of the autotuned one."""
         _lib.check(_lib.lib().mtgpu_survey_set_spmv_variant(self._h, int(variant)),
                    "mtgpu_survey_set_spmv_variant")
 
