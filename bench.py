@@ -49,6 +49,9 @@ sys.path.insert(0, ROOT)
 METRIC = "time/solve to rel-res 1e-8: batched mixed vs plain FP64 GPU; SpMV HBM GB/s"
 UNIT = "s/solve"
 WORKLOAD = "c2"
+# DRAM bytes of one launch of the batched SpMV on c2 (two lanes), from the
+# ncu capture summarised in profiles/spmv_batched_c2_s2.md
+SPMV_TRAFFIC_C2 = 957.0e6
 
 
 def load_peaks():
@@ -299,7 +302,10 @@ def gpu_arm(args):
         "roofline": {"bound": "hbm", "kernel": "k_spmv<SP> (batched double-float SELL-32 SpMV, S systems)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": f"{peak_kind} hbm_gbs",
-                     "bytes_per_launch": spmv_bytes, "ms_per_launch": spmv_ms, "traffic": None},
+                     "bytes_per_launch": spmv_bytes, "ms_per_launch": spmv_ms,
+                     "traffic": SPMV_TRAFFIC_C2 if WORKLOAD == "c2" else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
+                                       "k_spmv<2,4> on c2, profiles/spmv_batched_c2_s2.md"},
         "roofline_fp64_spmv": {"bound": "fp64 pipe (GB300 FP64 = FP32/64)",
                                "achieved": achieved64, "peak": peak, "unit": "GB/s",
                                "frac": achieved64 / peak, "bytes_per_launch": spmv64_bytes,
