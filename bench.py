@@ -135,6 +135,36 @@ def dist_init():
     return world, rank, local
 
 
+def max_over_ranks(value, device):
+    """The largest of every rank's value (the job's time is its slowest
+    rank's); the value itself without a process group."""
+    import torch
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return value
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_seconds_per_solve(ms, steps, systems_per_rank, world):
+    """Replicas: every rank solves its own copy of the workload, so the job
+    solves steps x systems x world systems in the slowest rank's time."""
+    return (ms / 1e3) / (steps * systems_per_rank * world)
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
 def make_inputs(w):
     from mtcalc_with_dfp_cocr_gb300 import normal1d
     tops = [l.top for l in w.mesh.layers]
@@ -211,12 +241,7 @@ def gpu_arm(args):
             fn()
         ev1.record(stream)
         barrier()
-        ms = ev0.elapsed_time(ev1)
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return max_over_ranks(ev0.elapsed_time(ev1), "cuda")
 
     # headline: the batched double-float solver
     for _ in range(args.warmup):
@@ -226,7 +251,7 @@ def gpu_arm(args):
         ms = timed(step_batched, args.steps)
     launches = _lib.kernel_launches() - launches0
     ms_per_step = ms / args.steps
-    value = (ms / 1e3) / (args.steps * S * world)
+    value = whole_job_seconds_per_solve(ms, args.steps, S, world)
     batched = info["batched"]
 
     # comparison: the plain FP64 COCR (the reference's algorithm) on the GPU
@@ -339,9 +364,16 @@ def cpu_sample(slae, mesh, key, target_seconds=15.0, fallback_iterations=None):
     _, _, s2 = O.pcocr(slae, mesh, nthreads=cores, iter_limit=n2)
     per_iter = (s2.seconds - s1.seconds) / (n2 - 3)
     setup = max(0.0, s1.seconds - 3 * per_iter)
+    # one thread (the reference's default nthreads.txt): a shorter sample
+    _, _, t1 = O.pcocr(slae, mesh, nthreads=1, iter_limit=3)
+    _, _, t2 = O.pcocr(slae, mesh, nthreads=1, iter_limit=13)
+    per_iter_1 = (t2.seconds - t1.seconds) / 10
+    setup_1 = max(0.0, t1.seconds - 3 * per_iter_1)
     pinned = ref_iterations()
     n_ref = pinned[key] if pinned else fallback_iterations
     return {"value": setup + per_iter * n_ref, "unit": UNIT, "cores": cores, "kind": "port",
+            "cpu_model": cpu_model(),
+            "value_1_thread": setup_1 + per_iter_1 * n_ref,
             "sample": f"oracle COCR_FP restatement, {cores} threads: set-up + {n2} iterations "
                       f"on the {key[0]} Hz / {'XY'[1 - key[1]]} system "
                       f"({s2.seconds:.1f} s), extrapolated to " +
