@@ -523,6 +523,8 @@ def survey_run(args):
         "speedup": t_p / t_b,
         "iterations_batched": {lab(f, a): it for (f, a), it in zip(systems, res["batched"]["iterations"])},
         "iterations_fp64": {lab(f, a): plain[k][0] for k, (f, a) in enumerate(systems)},
+        "fp64_resolve_iterations_batched": {lab(f, a): it for (f, a), it in
+                                            zip(systems, res["batched"]["fp64_iterations"]) if it},
         "true_rel_res_batched_max": max(res["batched"]["true_residual_rel"]),
         "true_rel_res_fp64_max": max(v[1] for v in plain.values()),
         "impedance_error_vs_fp64": {

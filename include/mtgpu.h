@@ -74,8 +74,8 @@ typedef struct {
     /* iterations per CUDA-graph launch between host status checks (0: 16) */
     int iterations_per_launch;
     /* 1: run the same algorithm in double-float arithmetic on the FP32 pipes
-     * (the batched survey solver with one system; if its smoothed residual
-     * stalls, the system is solved again in FP64 from x = 0); 0: FP64. */
+     * (the batched survey solver with one system; a system it cannot
+     * finish continues in FP64, see the survey solver); 0: FP64. */
     int double_float;
 } mtgpu_solve_opts;
 
@@ -231,8 +231,9 @@ void mtgpu_assembly_destroy(mtgpu_assembly *a);
  * FP64 (group updates every 16 iterations) and true residuals are evaluated
  * in FP64 from the FP64 matrix.  A system the double-float iteration cannot
  * finish (its smoothed residual stalls: very low frequencies on fine meshes,
- * where omega sigma_air is ~1e-13 of the curl-curl scale) is solved again by
- * the FP64 COCR from x = 0.  No counterpart in the reference,
+ * where omega sigma_air is ~1e-13 of the curl-curl scale) is finished by the
+ * FP64 COCR: from its double-float solution when that is within 100 eps of
+ * the target, else from x = 0.  No counterpart in the reference,
  * which solves the systems one by one in FP64.
  * ---------------------------------------------------------------------- */
 typedef struct mtgpu_survey_s mtgpu_survey;

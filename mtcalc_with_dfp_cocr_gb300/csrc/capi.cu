@@ -361,17 +361,18 @@ int mtgpu_pcocr_2x2_folded_ex(int n, const int *ig, const int *jg, const int *id
                                               kpar, n_nodes_c, nvkat, nver14, sigma3d, edges2,
                                               ig_t, jg_t, gg_t, is_node_bound,
                                               opts->stop_on_true_residual, &sd);
-        // a system the double-float iteration cannot finish (its smoothed
-        // residual stalls) is solved again in FP64 from x = 0: the stalled
-        // iterate's errors in the air's gradient components are not a start
-        // the FP64 iteration recovers from
+        // a system the double-float iteration cannot finish continues in FP64:
+        // from its double-float solution when that is within 100 eps of the
+        // target, else from x = 0 (a stalled iterate's errors in the air's
+        // gradient components are not a start the FP64 iteration recovers from)
         if (r != MTGPU_MAXITER || sd.iterations >= maxiter) {
             if (stats) *stats = sd;
             return r;
         }
         df_iters = sd.iterations;
         maxiter -= df_iters;
-        for (int i = 0; i < n; i++) x[i] = 0.0;
+        if (!(sd.true_residual_rel >= 0.0 && sd.true_residual_rel < 100.0 * eps))
+            for (int i = 0; i < n; i++) x[i] = 0.0;
     }
     mtgpu_cocr *c = nullptr;
     int rc = mtgpu_cocr_create(nb, 0, ig, jg, idi, ijg, di, gg, 0, kpar, n_nodes_c, nvkat,

@@ -227,10 +227,11 @@ int mtgpu_survey_solve(mtgpu_survey *s, const double *d_b, double *d_x, double e
     int rc = survey_solve(s->V, (const double2 *)d_b, (double2 *)d_x, eps, maxiter, verify, 16,
                           st);
     if (rc <= MTGPU_ERR_ARG) return rc;
-    // systems the double-float iteration could not finish: FP64 COCR from a
-    // zero initial guess, with the iterations left (the stalled double-float
-    // iterate carries large errors in the air's gradient components, from
-    // which the FP64 iteration does not recover)
+    // systems the double-float iteration could not finish: FP64 COCR with the
+    // iterations left.  A double-float solution within 100 eps of the target
+    // is the FP64 iteration's start; a stalled one (far above: very low
+    // frequencies, large errors in the air's gradient components, from which
+    // the FP64 iteration does not recover) is discarded for x = 0.
     const long long nb = s->V.nb;
     int worst = MTGPU_OK;
     for (int k = 0; k < s->V.S; k++) {
@@ -241,7 +242,9 @@ int mtgpu_survey_solve(mtgpu_survey *s, const double *d_b, double *d_x, double e
             if (r2) return r2;
             mtgpu_solve_opts opts{verify, 0, 0};
             mtgpu_solve_stats s64{};
-            MTGPU_TRY(cudaMemsetAsync(d_x + 2 * nb * k, 0, sizeof(double) * 2 * nb, s->st));
+            const double tr = st->true_residual_rel[k];
+            if (!(tr >= 0.0 && tr < 100.0 * eps))
+                MTGPU_TRY(cudaMemsetAsync(d_x + 2 * nb * k, 0, sizeof(double) * 2 * nb, s->st));
             MTGPU_TRY(cudaStreamSynchronize(s->st));
             r2 = mtgpu_cocr_solve(c, d_b + 2 * nb * k, d_x + 2 * nb * k, eps, left, &opts, &s64);
             mtgpu_cocr_destroy(c);

@@ -1360,7 +1360,10 @@ int survey_solve(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, do
     V.eps = eps;
     if (iters_per_launch <= 0) iters_per_launch = 16;
     constexpr int kMaxContinue = 4;      // continuations after the first stop
-    constexpr int kStallWindow = 1000;   // iterations without halving the smoothed residual
+    // stalled: the smoothed residual has not halved for max(kStallWindow,
+    // iterations before its last halving) iterations (COCR plateaus that
+    // end are shorter than the way down to them)
+    constexpr int kStallWindow = 1000;
     for (int k = 0; k < 32; k++) {
         SysState s{};
         s.status = k < V.S ? kRun : MTGPU_OK;
@@ -1440,7 +1443,7 @@ int survey_solve(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, do
                 if (q.residual_rel < 0.5 * best[k]) {
                     best[k] = q.residual_rel;
                     best_it[k] = q.iter;
-                } else if (q.iter - best_it[k] > kStallWindow) {
+                } else if (q.iter - best_it[k] > std::max(kStallWindow, best_it[k])) {
                     q.status = MTGPU_MAXITER;   // stalled
                     stalled[k] = 1;
                     changed = true;
