@@ -624,10 +624,10 @@ def dtm_run(args):
     device assembly, the batched solver, the receiver fields and the MT
     responses, against CalculationResults/625_500_reg_R_Z.txt.  The table
     was produced with the reference's smoothing output path and FP32
-    impedance post-processing, so agreement is expected at the percent
-    level, not 1e-6.  The table's station coordinates are evaluated both as
-    (northing, easting) = (x, y) and as (x, -y); the example's receiver file
-    holds the mirrored set for part of the stations."""
+    impedance post-processing.  The direct output is evaluated at the
+    table's station coordinates taken both as (northing, easting) = (x, y)
+    and as (x, -y) (the example's receiver file holds the mirrored set for
+    part of the stations); the smoothing output at (x, -y)."""
     import torch
     from mtcalc_with_dfp_cocr_gb300 import assembly, mesh as M, normal1d, receivers, survey
     from mtcalc_with_dfp_cocr_gb300 import build as B
@@ -643,6 +643,11 @@ def dtm_run(args):
                           np.c_[st[:, 0], -st[:, 1], np.zeros(len(st))]])
     A = assembly.Assembly(m)
     R = receivers.Receivers(A, pts)
+    # the reference's default output (subdomain smoothing) at the table's
+    # receivers, (northing, -easting)
+    Rs = receivers.Receivers(A, pts[len(st):], output="smooth")
+    out_s = np.empty((len(freqs), len(st), 34))
+    t_smooth = 0.0
     tops = [l.top for l in layers]
     sig = [l.sigma for l in layers]
     out = np.empty((len(freqs), len(pts), 34))
@@ -672,11 +677,19 @@ def dtm_run(args):
         E, H, _ = R.fields(x, nus, alfas, tabs[0][0], us, uc)
         out[f0:f0 + len(fb)] = R.mt_response(fb, np.arange(0, 2 * len(fb), 2),
                                              np.arange(1, 2 * len(fb), 2), E, H).cpu().numpy()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        E, H, _ = Rs.fields(x, nus, alfas, tabs[0][0], us, uc)
+        torch.cuda.synchronize()
+        t_smooth += time.perf_counter() - t0
+        out_s[f0:f0 + len(fb)] = Rs.mt_response(fb, np.arange(0, 2 * len(fb), 2),
+                                                np.arange(1, 2 * len(fb), 2), E, H).cpu().numpy()
     pub = g["published"]          # [station][period][8]
     n = len(st)
     res = {}
-    for name, sl in (("x=northing,y=easting", slice(0, n)), ("x=northing,y=-easting", slice(n, 2 * n))):
-        o = out[:, sl].transpose(1, 0, 2)   # [station][period][34]
+    for name, o in (("x=northing,y=easting", out[:, :n]), ("x=northing,y=-easting", out[:, n:]),
+                    ("smoothing output, x=northing,y=-easting", out_s)):
+        o = o.transpose(1, 0, 2)            # [station][period][34]
         zerr = np.abs(o[..., 13:15] - pub[..., 1:3]) / pub[..., 1:3]
         rerr = np.abs(o[..., 21:23] - pub[..., 5:7]) / pub[..., 5:7]
         res[name] = {"Zxy_Zyx_rel_median": float(np.median(zerr)), "Zxy_Zyx_rel_p95": float(np.percentile(zerr, 95)),
@@ -687,6 +700,7 @@ def dtm_run(args):
                       "systems": 2 * len(freqs), "stations": n, "solve_s": t_solve,
                       "eps": float(args.dtm_eps), "iterations_max": int(max(iters)),
                       "fp64_resolved_systems": int(sum(1 for v in fp64 if v > 0)),
+                      "smoothing": dict(Rs.smoothing_info(), seconds_all_periods=t_smooth),
                       "vs_published": res}), flush=True)
 
 

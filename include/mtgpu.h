@@ -302,6 +302,35 @@ int mtgpu_receivers_create(const mtgpu_assembly *a, int nrec, const double *xyz_
  * every receiver (host [nrec]). */
 int mtgpu_receivers_info(const mtgpu_receivers *r, int *nrec, int *n_unlocated, int *elem);
 
+/* How mtgpu_receivers_fields obtains A and curl A at the receivers:
+ *  MTGPU_OUTPUT_DIRECT (the default after create): the edge basis of the
+ *    receiver's brick evaluated at the receiver, the reference's direct
+ *    output (GPDocSettings.vfem_direct_output, give_out_vec_mt.cpp:109-198);
+ *  MTGPU_OUTPUT_SMOOTH: the reference's default output, subdomain L2-
+ *    projection smoothing (give_out_vec_mt.cpp:200-237; OutputResultant3d.cpp
+ *    :76-199, 293-450; Subdomain.cpp:132-661): the brick-centre values of A
+ *    (per material, air skipped) and of curl A (all materials) in the
+ *    receivers' bricks grown `levels` times (the reference uses 5) by the
+ *    bricks sharing a node are projected onto nodal trilinear functions, and
+ *    the projection is interpolated at the receiver.  Receivers are located
+ *    with boxes grown by 1e-6; a receiver with no non-air brick gets A = 0.
+ *    The reference solves each projection with PARDISO; here all value types
+ *    of all systems are solved together on the device by conjugate gradients
+ *    to a relative residual of 1e-14.  Conforming hexahedral meshes only.
+ * The assembly `a` must be the one the receivers were created on and must
+ * outlive them while the output is smoothed.  The adjoint functions accept
+ * the direct output only. */
+#define MTGPU_OUTPUT_DIRECT 0
+#define MTGPU_OUTPUT_SMOOTH 1
+int mtgpu_receivers_set_output(mtgpu_receivers *r, const mtgpu_assembly *a, int mode, int levels);
+
+/* Smoothing subdomains (at most max_sub reported): subdomain 0 smooths
+ * curl A over all materials (material -1), the others A over one material
+ * each; their bricks and nodes, and the conjugate-gradient iterations of the
+ * last mtgpu_receivers_fields call. */
+int mtgpu_receivers_smoothing_info(const mtgpu_receivers *r, int max_sub, int *nsub, int *material,
+                                   int *cells, int *nodes, int *iterations);
+
 /* Total fields of S systems at the receivers: E = -i omega A + E_1d and
  * H = curl A / MU_0 + H_1d, the 1-D part on x and y only, with A the
  * anomalous potential d_x [S][2 nb] (device, re/im interleaved, e.g. the

@@ -109,6 +109,9 @@ SIGNATURES = {
                                          _vp, _vp]),
     "mtgpu_mt_response": (C.c_int, [_vp, C.c_int, _d, _i, _i, C.c_int, _vp, _vp, _vp]),
     "mtgpu_receivers_destroy": (None, [_vp]),
+    "mtgpu_receivers_set_output": (C.c_int, [_vp, _vp, C.c_int, C.c_int]),
+    "mtgpu_receivers_smoothing_info": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), _vp, _vp,
+                                                 _vp, C.POINTER(C.c_int)]),
     "mtgpu_adjoint_source": (C.c_int, [_vp, C.c_int, _d, _i, _i, C.c_int, _vp, _vp, _vp, _vp,
                                        C.POINTER(C.c_double)]),
     "mtgpu_adjoint_gradient": (C.c_int, [_vp, C.c_int, _d, _i, C.c_int, _d, _d, _d, _vp, _vp,

@@ -10,7 +10,9 @@ Harm1D, BuildMatrix, COCR_FP, OutputNu, then ImpedanceZToEdsAll and
 calcimpedance over all of them): the mesh (meshbuilder.py), the 1-D normal
 fields (normal1d.py), the device assembly, every frequency x polarisation
 through the batched solver (16 frequencies per batch), the receiver fields
-and the MT responses.
+(by default through the reference's default output, subdomain smoothing;
+--output direct evaluates the edge basis at the receivers) and the MT
+responses.
 
 The table has the layout of the reference's published results
 (CalculationResults/625_500_reg_R_Z.txt): per receiver and period,
@@ -34,9 +36,11 @@ from .receivers import MT_RHO, MT_ZABS
 BATCH = 16   # frequencies per batch (x 2 polarisations = 32 systems)
 
 
-def run(case, eps=None, maxiter=None, device="cuda", log=None):
+def run(case, eps=None, maxiter=None, device="cuda", log=None, output="smooth"):
     """Solve every frequency x polarisation of `case`; returns
-    (responses [nf][nrec][34], stats dict)."""
+    (responses [nf][nrec][34], stats dict).  output: "smooth", the
+    reference's default receiver output (subdomain smoothing), or "direct"
+    (receivers.py)."""
     import torch
     from .assembly import Assembly
     from .receivers import Receivers
@@ -47,14 +51,14 @@ def run(case, eps=None, maxiter=None, device="cuda", log=None):
     t0 = time.perf_counter()
     mesh = meshbuilder.build_mesh(case)
     A = Assembly(mesh)
-    R = Receivers(A, case.receivers)
+    R = Receivers(A, case.receivers, output=output)
     miss, _ = R.info()
     tops = [l.top for l in case.layers]
     sig = [l.sigma for l in case.layers]
     freqs = np.asarray(case.freqs, np.float64)
     out = np.empty((len(freqs), len(case.receivers), 34))
     stats = {"nb": mesh.nb, "cells": mesh.kpar, "lines": [mesh.nx, mesh.ny, mesh.nz],
-             "receivers_outside_mesh": miss, "eps": eps, "systems": []}
+             "receivers_outside_mesh": miss, "eps": eps, "output": output, "systems": []}
     for f0 in range(0, len(freqs), BATCH):
         fb = freqs[f0:f0 + BATCH]
         nus = np.repeat(fb, 2)
@@ -80,6 +84,8 @@ def run(case, eps=None, maxiter=None, device="cuda", log=None):
         E, H, _ = R.fields(x, nus, alfas, tabs[0][0], us, uc)
         out[f0:f0 + len(fb)] = R.mt_response(
             fb, np.arange(0, 2 * len(fb), 2), np.arange(1, 2 * len(fb), 2), E, H).cpu().numpy()
+    if output == "smooth":
+        stats["smoothing"] = R.smoothing_info()
     stats["seconds"] = time.perf_counter() - t0
     return out, stats
 
@@ -109,9 +115,13 @@ def main(argv=None):
     ap.add_argument("--eps", type=float, default=None,
                     help="relative residual of the solves (default: settings.cfg's)")
     ap.add_argument("--maxiter", type=int, default=None)
+    ap.add_argument("--output", choices=["smooth", "direct"], default="smooth",
+                    help="receiver output: the reference's default subdomain smoothing, or the "
+                         "direct evaluation of the edge basis at the receiver")
     a = ap.parse_args(argv)
     case = meshbuilder.read_case(a.case)
-    resp, stats = run(case, a.eps, a.maxiter, log=lambda s: print(s, file=sys.stderr))
+    resp, stats = run(case, a.eps, a.maxiter, log=lambda s: print(s, file=sys.stderr),
+                      output=a.output)
     out = a.out or os.path.join(a.case, "results_R_Z.txt")
     write_table(out, case, resp)
     with open(os.path.splitext(out)[0] + "_stats.json", "w") as f:

@@ -277,6 +277,8 @@ int mtgpu_adjoint_source(mtgpu_receivers *r, int nf, const double *nu, const int
 {
     MTGPU_CHECK_ARG(r && nu && sys_x && sys_y && d_e && d_h && d_zobs && d_src,
                     "null argument");
+    MTGPU_CHECK_ARG(r->output == MTGPU_OUTPUT_DIRECT,
+                    "the adjoint source differentiates the direct receiver output only");
     MTGPU_CHECK_ARG(nf > 0 && nf <= 65535 && S > 0 && S <= 65535, "bad nf or S");
     std::vector<int> used(S, 0);
     for (int f = 0; f < nf; f++) {

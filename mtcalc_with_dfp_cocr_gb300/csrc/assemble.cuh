@@ -57,6 +57,7 @@ struct mtgpu_assembly_s {
     cudaStream_t st = nullptr;
     // host copies of what the folded preconditioner set-up reads
     std::vector<int> nver, nvkat, edges, bound;
+    std::vector<double> xyz;
     std::vector<double> sigflag;
     std::vector<int> ig_t;
     int nver_stride = 14;

@@ -40,6 +40,7 @@ int mtgpu_assembly_create(const mtgpu_fem_mesh *mesh, mtgpu_assembly **out)
     a->nver_stride = m.nver_stride;
     a->nver.assign(m.nver, m.nver + (size_t)m.kpar * m.nver_stride);
     a->nvkat.assign(m.nvkat, m.nvkat + m.kpar);
+    a->xyz.assign(m.xyz, m.xyz + (size_t)3 * m.kuzlov);
     a->edges.assign(m.edges, m.edges + (size_t)2 * m.nb);
     a->bound.assign(m.kuzlov, 0);
     for (int i = 0; i < m.n_bound; i++) a->bound[m.bound_nodes[i]] = 1;

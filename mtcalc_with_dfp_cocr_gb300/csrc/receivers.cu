@@ -9,6 +9,7 @@
 // kernel runs in FP64 with one thread per (receiver, system) or (receiver,
 // frequency); the only sizeable step is the one-off receiver location, a
 // scan of all bricks against the receiver list staged in shared memory.
+#include "rcv_eval.cuh"
 #include "receivers.cuh"
 
 #include <climits>
@@ -17,9 +18,7 @@
 namespace mtgpu {
 namespace {
 
-constexpr double kPi = 3.1415926535897932384626433832795;   // OutputNu/stdafx.h:32
-constexpr double kMu0 = 1.25663706143591729e-6;              // OutputNu/stdafx.h:31
-constexpr double kMu0_1d = 4.0 * 3.1415926535897932 * 1e-7;  // Harm1D/divgrad_1d.cpp:288
+using rcv::kPi;
 constexpr int kLocChunk = 256;                               // receivers per shared-memory pass
 
 __global__ void k_rcv_init(int nrec, int *elem)
@@ -28,22 +27,26 @@ __global__ void k_rcv_init(int nrec, int *elem)
     if (r < nrec) elem[r] = INT_MAX;
 }
 
-// elem[r] = the lowest brick index whose closed box [vertex 0, vertex 7]
-// holds receiver r (OutputArbitrary.cpp:385-500 keeps the first one found
-// in index order).  One thread per brick; receivers pass through shared
-// memory in chunks.
+// elem[r] = the lowest brick index whose closed box [vertex 0, vertex 7],
+// grown by `grow` on every side, holds receiver r.  The direct output keeps
+// the first brick found in index order with no growth
+// (OutputArbitrary.cpp:385-500); the smoothing output grows the boxes by
+// 1e-6 and, for A, skips the bricks of material 0, the air
+// (OutputResultant3d.cpp:293-450): nvkat != NULL selects that.  One thread
+// per brick; receivers pass through shared memory in chunks.
 __global__ void __launch_bounds__(kThreads)
 k_rcv_locate(int kpar, const int *__restrict__ nver, int nver_stride,
-             const double *__restrict__ xyz, int nrec, const double *__restrict__ rec, int *elem)
+             const double *__restrict__ xyz, int nrec, const double *__restrict__ rec, double grow,
+             const int *__restrict__ nvkat, int *elem)
 {
     __shared__ double sx[kLocChunk], sy[kLocChunk], sz[kLocChunk];
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     double lo[3] = {0, 0, 0}, hi[3] = {-1, -1, -1};   // empty box for idle threads
-    if (e < kpar) {
+    if (e < kpar && !(nvkat && nvkat[e] == 0)) {
         const int v0 = nver[(long long)e * nver_stride], v7 = nver[(long long)e * nver_stride + 7];
         for (int d = 0; d < 3; d++) {
-            lo[d] = xyz[3 * v0 + d];
-            hi[d] = xyz[3 * v7 + d];
+            lo[d] = xyz[3 * v0 + d] - grow;
+            hi[d] = xyz[3 * v7 + d] + grow;
         }
     }
     for (int base = 0; base < nrec; base += kLocChunk) {
@@ -92,54 +95,8 @@ __global__ void k_rcv_prepare(int nrec, int *elem, const int *__restrict__ nver,
     hsz[r] = make_double4(h[0], h[1], h[2], 0.0);
 }
 
-// Harm1D's table interpolation (divgrad_1d.cpp:50-88): the first interval
-// [z_i, z_i+1] holding x, constant beyond the ends
-__device__ double table_value(double x, int n, const double *z, const double *v)
-{
-    if (x < z[0]) return v[0];
-    if (x > z[n - 1]) return v[n - 1];
-    int lo = 0, hi = n - 2;
-    while (lo < hi) {   // smallest t with x <= z[t+1]
-        const int mid = (lo + hi) >> 1;
-        if (x <= z[mid + 1]) hi = mid; else lo = mid + 1;
-    }
-    const double t = (x - z[lo]) / (z[lo + 1] - z[lo]);
-    return (1.0 - t) * v[lo] + t * v[lo + 1];
-}
-
-// Harm1D's table derivative (divgrad_1d.cpp:90-138): end slopes outside
-// [z_1, z_n-2]; inside, node slopes (weighted means of the adjacent interval
-// slopes) interpolated over the interval ending at the first z_i >= x
-__device__ double table_slope(double x, int n, const double *z, const double *v)
-{
-    if (x < z[1]) return (v[1] - v[0]) / (z[1] - z[0]);
-    if (x > z[n - 2]) return (v[n - 1] - v[n - 2]) / (z[n - 1] - z[n - 2]);
-    int lo = 1, hi = n - 1;
-    while (lo < hi) {   // smallest i >= 1 with x <= z[i]
-        const int mid = (lo + hi) >> 1;
-        if (x <= z[mid]) hi = mid; else lo = mid + 1;
-    }
-    const int i = lo;
-    if (i < 2 || i + 1 >= n) return (v[i] - v[i - 1]) / (z[i] - z[i - 1]);
-    const double w0 = (z[i - 1] - z[i - 2]) / (z[i] - z[i - 2]);
-    const double d0 = (v[i - 1] - v[i - 2]) / (z[i - 1] - z[i - 2]) * (1.0 - w0) +
-                      (v[i] - v[i - 1]) / (z[i] - z[i - 1]) * w0;
-    const double w1 = (z[i] - z[i - 1]) / (z[i + 1] - z[i - 1]);
-    const double d1 = (v[i] - v[i - 1]) / (z[i] - z[i - 1]) * (1.0 - w1) +
-                      (v[i + 1] - v[i]) / (z[i + 1] - z[i]) * w1;
-    const double t = (x - z[i - 1]) / (z[i] - z[i - 1]);
-    return (1.0 - t) * d0 + t * d1;
-}
-
-__device__ __forceinline__ double lin0(double t) { return 0.5 * (1.0 - t); }
-__device__ __forceinline__ double lin1(double t) { return 0.5 * (1.0 + t); }
-
-// One thread per (receiver, system).  A from the 12 edge DOFs of the
-// receiver's brick (edge i of direction d carries (2/h_d) l_a l_b in the two
-// other local coordinates, T_Brick.cpp:980-1137), curl A from l0' = -1/2,
-// l1' = 1/2 (T_Brick.cpp:1484-1618, 1842-1918).  E = -i omega A plus the 1-D
-// field on x and y; H = curl A / mu0 plus the 1-D field on x and y
-// (give_out_vec_mt.cpp:135-195, 232-266; Harm1D divgrad_1d.cpp:290-330).
+// One thread per (receiver, system): A and curl A at the receiver from the
+// 12 edge values of its brick, then the total fields.
 __global__ void k_rcv_fields(int nrec, int S, long long x_stride, const double2 *__restrict__ x,
                              const double *__restrict__ omega, const int *__restrict__ alfa,
                              int n1d, const double *__restrict__ z1d,
@@ -151,77 +108,18 @@ __global__ void k_rcv_fields(int nrec, int S, long long x_stride, const double2 
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     const int k = blockIdx.y;
     if (r >= nrec || k >= S) return;
-    const double w = omega[k];
     double2 A[3] = {}, C[3] = {};
     if (elem[r] >= 0) {
         const double4 L = loc[r], Hs = hsz[r];
-        const double xi = L.x, et = L.y, ze = L.z, hx = Hs.x, hy = Hs.y, hz = Hs.z;
         const double2 *xs = x + (long long)k * x_stride;
         double2 v[12];
 #pragma unroll
         for (int i = 0; i < 12; i++) v[i] = xs[edge[12 * r + i]];
-        const double cx[4] = {lin0(et) * lin0(ze), lin1(et) * lin0(ze), lin0(et) * lin1(ze),
-                              lin1(et) * lin1(ze)};
-        const double cy[4] = {lin0(ze) * lin0(xi), lin1(ze) * lin0(xi), lin0(ze) * lin1(xi),
-                              lin1(ze) * lin1(xi)};
-        const double cz[4] = {lin0(xi) * lin0(et), lin1(xi) * lin0(et), lin0(xi) * lin1(et),
-                              lin1(xi) * lin1(et)};
-        const double sx = 2.0 / hx, sy = 2.0 / hy, sz = 2.0 / hz;
-        const double rx = 2.0 / (hy * hz), ry = 2.0 / (hx * hz), rz = 2.0 / (hx * hy);
-#define MTGPU_PART(f)                                                                         \
-        {                                                                                     \
-            A[0].f = sx * (v[0].f * cx[0] + v[1].f * cx[1] + v[2].f * cx[2] + v[3].f * cx[3]); \
-            A[1].f = sy * (v[4].f * cy[0] + v[5].f * cy[1] + v[6].f * cy[2] + v[7].f * cy[3]); \
-            A[2].f = sz * (v[8].f * cz[0] + v[9].f * cz[1] + v[10].f * cz[2] + v[11].f * cz[3]); \
-            C[0].f = rx * (lin0(xi) * (v[4].f - v[5].f - v[8].f + v[10].f) +                  \
-                           lin1(xi) * (v[6].f - v[7].f - v[9].f + v[11].f));                  \
-            C[1].f = ry * (lin0(et) * (v[2].f - v[0].f + v[8].f - v[9].f) +                   \
-                           lin1(et) * (v[3].f - v[1].f + v[10].f - v[11].f));                 \
-            C[2].f = rz * (lin0(ze) * (v[0].f - v[1].f - v[4].f + v[6].f) +                   \
-                           lin1(ze) * (v[2].f - v[3].f - v[5].f + v[7].f));                   \
-        }
-        MTGPU_PART(x)
-        MTGPU_PART(y)
-#undef MTGPU_PART
+        rcv::brick_eval(v, L.x, L.y, L.z, Hs.x, Hs.y, Hs.z, A, C);
     }
-    double2 E[3], H[3];
-    for (int d = 0; d < 3; d++) {
-        E[d] = make_double2(w * A[d].y, -w * A[d].x);
-        H[d] = make_double2(C[d].x / kMu0, C[d].y / kMu0);
-    }
-    // 1-D normal field at the receiver depth
-    {
-        const double z = loc[r].w;
-        const double a = alfa[k] ? 1.0 : 0.0;
-        const double *us = usin + (long long)k * n1d, *uc = ucos + (long long)k * n1d;
-        double ds = kMu0_1d, dc = 0.0;
-        if (z < 0.0) {
-            ds = table_slope(z, n1d, z1d, us);
-            dc = table_slope(z, n1d, z1d, uc);
-        }
-        const double zz = z > 0.0 ? 0.0 : z;
-        const double fs = table_value(zz, n1d, z1d, us), fc = table_value(zz, n1d, z1d, uc);
-        E[0].x += w * a * fc;
-        E[0].y += -w * a * fs;
-        E[1].x += w * (1.0 - a) * fc;
-        E[1].y += w * (a - 1.0) * fs;
-        H[0].x += (a - 1.0) * ds / kMu0;
-        H[0].y += (a - 1.0) * dc / kMu0;
-        H[1].x += a * ds / kMu0;
-        H[1].y += a * dc / kMu0;
-    }
-    const long long o = ((long long)k * nrec + r) * 3;
-    for (int d = 0; d < 3; d++) {
-        e_out[o + d] = E[d];
-        h_out[o + d] = H[d];
-    }
-    // give_out_vec_mt.cpp:247-264: moduli of the real and imaginary parts
-    const double ere = sqrt(E[0].x * E[0].x + E[1].x * E[1].x + E[2].x * E[2].x);
-    const double eim = sqrt(E[0].y * E[0].y + E[1].y * E[1].y + E[2].y * E[2].y);
-    const double hre = sqrt(H[0].x * H[0].x + H[1].x * H[1].x + H[2].x * H[2].x);
-    const double him = sqrt(H[0].y * H[0].y + H[1].y * H[1].y + H[2].y * H[2].y);
-    const double q = sqrt(ere * ere + eim * eim) / sqrt(hre * hre + him * him);
-    scal[(long long)k * nrec + r] = make_double2(q * q / (w * kMu0), q);
+    const long long o = (long long)k * nrec + r;
+    rcv::total_fields(A, C, omega[k], alfa[k], loc[r].w, n1d, z1d, usin + (long long)k * n1d,
+                      ucos + (long long)k * n1d, e_out + 3 * o, h_out + 3 * o, scal + o);
 }
 
 // calcimpedance.for:163-171: quadrant rule, then the near-axis overrides in
@@ -323,6 +221,19 @@ __global__ void k_mt_response(int nrec, int nf, const double *__restrict__ omega
 }
 
 }  // namespace
+
+int locate_receivers(const ParamMatrix &P, int nrec, const double *d_rec, double grow,
+                     bool skip_air, int *d_elem, cudaStream_t st)
+{
+    k_rcv_init<<<ceil_div(nrec, kThreads), kThreads, 0, st>>>(nrec, d_elem);
+    k_rcv_locate<<<ceil_div(P.kpar, kThreads), kThreads, 0, st>>>(
+        P.kpar, P.d_nver, P.nver_stride, P.d_xyz, nrec, d_rec, grow,
+        skip_air ? P.d_nvkat : nullptr, d_elem);
+    note_launches(2);
+    MTGPU_TRY(cudaGetLastError());
+    return MTGPU_OK;
+}
+
 }  // namespace mtgpu
 
 using namespace mtgpu;
@@ -345,6 +256,10 @@ void mtgpu_receivers_destroy(mtgpu_receivers *r)
     dev_free(r->d_touch_ptr);
     dev_free(r->d_touch_edge);
     dev_free(r->d_touch_slot);
+    if (r->sm) {
+        r->sm->release();
+        delete r->sm;
+    }
     if (r->st) cudaStreamDestroy(r->st);
     delete r;
 }
@@ -358,6 +273,7 @@ int mtgpu_receivers_create(const mtgpu_assembly *a, int nrec, const double *xyz_
     auto *r = new mtgpu_receivers_s();
     r->nrec = nrec;
     r->nb = a->P.nb;
+    r->rec.assign(xyz_rec, xyz_rec + (size_t)3 * nrec);
     int rc = MTGPU_OK;
     double *d_rec = nullptr;
     do {
@@ -388,7 +304,7 @@ int mtgpu_receivers_create(const mtgpu_assembly *a, int nrec, const double *xyz_
         const ParamMatrix &P = a->P;
         k_rcv_init<<<ceil_div(nrec, kThreads), kThreads, 0, r->st>>>(nrec, r->d_elem);
         k_rcv_locate<<<ceil_div(P.kpar, kThreads), kThreads, 0, r->st>>>(
-            P.kpar, P.d_nver, P.nver_stride, P.d_xyz, nrec, d_rec, r->d_elem);
+            P.kpar, P.d_nver, P.nver_stride, P.d_xyz, nrec, d_rec, 0.0, nullptr, r->d_elem);
         k_rcv_prepare<<<ceil_div(nrec, kThreads), kThreads, 0, r->st>>>(
             nrec, r->d_elem, P.d_nver, P.nver_stride, P.d_ed, P.ed_stride, P.d_xyz, d_rec,
             r->d_edge, r->d_loc, r->d_h);
@@ -425,6 +341,54 @@ int mtgpu_receivers_info(const mtgpu_receivers *r, int *nrec, int *n_unlocated, 
     return MTGPU_OK;
 }
 
+int mtgpu_receivers_set_output(mtgpu_receivers *r, const mtgpu_assembly *a, int mode, int levels)
+{
+    MTGPU_CHECK_ARG(r != nullptr, "null receivers");
+    MTGPU_CHECK_ARG(mode == MTGPU_OUTPUT_DIRECT || mode == MTGPU_OUTPUT_SMOOTH, "unknown mode");
+    if (mode == MTGPU_OUTPUT_DIRECT) {
+        r->output = mode;
+        return MTGPU_OK;
+    }
+    MTGPU_CHECK_ARG(a != nullptr, "the smoothing output needs the assembly");
+    MTGPU_CHECK_ARG(a->P.nb == r->nb, "the assembly is not the receivers' mesh");
+    MTGPU_CHECK_ARG(levels >= 0 && levels <= 64, "levels must be in [0, 64]");
+    MTGPU_CHECK_ARG(a->nver_stride >= 8 && !a->xyz.empty(), "the assembly has no host mesh");
+    if (r->sm) {
+        r->sm->release();
+        delete r->sm;
+        r->sm = nullptr;
+    }
+    r->output = MTGPU_OUTPUT_DIRECT;
+    auto *sm = new Smoothing();
+    sm->levels = levels;
+    int rc = smoothing_build(*sm, *a, r->nrec, r->rec.data(), r->st);
+    if (rc) {
+        sm->release();
+        delete sm;
+        return rc;
+    }
+    r->sm = sm;
+    r->asm_ = a;
+    r->output = mode;
+    return MTGPU_OK;
+}
+
+int mtgpu_receivers_smoothing_info(const mtgpu_receivers *r, int max_sub, int *nsub, int *material,
+                                   int *cells, int *nodes, int *iterations)
+{
+    MTGPU_CHECK_ARG(r != nullptr, "null receivers");
+    MTGPU_CHECK_ARG(r->output == MTGPU_OUTPUT_SMOOTH && r->sm, "the output is not smoothed");
+    const Smoothing &sm = *r->sm;
+    if (nsub) *nsub = sm.nsub;
+    for (int s = 0; s < sm.nsub && s < max_sub; s++) {
+        if (material) material[s] = sm.sub_material[s];
+        if (cells) cells[s] = sm.sub_cells[s];
+        if (nodes) nodes[s] = sm.sub_nodes[s];
+    }
+    if (iterations) *iterations = sm.iterations;
+    return MTGPU_OK;
+}
+
 int mtgpu_receivers_fields(mtgpu_receivers *r, int S, const double *nu, const int *alfa, int n1d,
                            const double *z1d, const double *usin, const double *ucos,
                            const double *d_x, double *d_e, double *d_h, double *d_rho_imp)
@@ -454,13 +418,21 @@ int mtgpu_receivers_fields(mtgpu_receivers *r, int S, const double *nu, const in
                               r->st));
     MTGPU_TRY(cudaMemcpyAsync(d_uc, ucos, sizeof(double) * S * n1d, cudaMemcpyHostToDevice,
                               r->st));
-    dim3 grid(ceil_div(r->nrec, 128), S);
-    k_rcv_fields<<<grid, 128, 0, r->st>>>(r->nrec, S, r->nb, (const double2 *)d_x, r->d_omega,
-                                          r->d_int, n1d, d_z1d, d_us, d_uc, r->d_elem,
-                                          r->d_edge, r->d_loc, r->d_h, (double2 *)d_e,
-                                          (double2 *)d_h, (double2 *)d_rho_imp);
-    note_launches(1);
-    MTGPU_TRY(cudaGetLastError());
+    if (r->output == MTGPU_OUTPUT_SMOOTH) {
+        int rc2 = smoothing_fields(*r->sm, r->asm_->P, r->nrec, S, r->nb, (const double2 *)d_x,
+                                   r->d_omega, r->d_int, n1d, d_z1d, d_us, d_uc, r->d_loc,
+                                   (double2 *)d_e, (double2 *)d_h, (double2 *)d_rho_imp, r->st);
+        if (rc2) return rc2;
+    } else {
+        dim3 grid(ceil_div(r->nrec, 128), S);
+        k_rcv_fields<<<grid, 128, 0, r->st>>>(r->nrec, S, r->nb, (const double2 *)d_x,
+                                              r->d_omega, r->d_int, n1d, d_z1d, d_us, d_uc,
+                                              r->d_elem, r->d_edge, r->d_loc, r->d_h,
+                                              (double2 *)d_e, (double2 *)d_h,
+                                              (double2 *)d_rho_imp);
+        note_launches(1);
+        MTGPU_TRY(cudaGetLastError());
+    }
     MTGPU_TRY(cudaStreamSynchronize(r->st));
     return MTGPU_OK;
 }

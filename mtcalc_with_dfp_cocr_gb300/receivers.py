@@ -1,9 +1,12 @@
 """Receiver fields and MT responses on the GPU (over libmtgpu).
 
-    Receivers(assembly, points)     locate the receivers in the mesh
+    Receivers(assembly, points, output="direct" | "smooth", levels=5)
+                                    locate the receivers in the mesh
     .fields(x, nus, alfas, ...)     E, H at the receivers for S solutions, as
-                                    the reference's OutputNu direct path and
-                                    Harm1D's normal field give them
+                                    the reference's OutputNu gives them (its
+                                    direct evaluation, or its default
+                                    subdomain smoothing) plus Harm1D's
+                                    normal field
     .mt_response(nus, sys_x, sys_y, E, H)
                                     impedance tensor, tipper, apparent
                                     resistivities and phases per frequency
@@ -27,15 +30,46 @@ MT_Z, MT_W, MT_ZABS, MT_ZPHASE, MT_RHO, MT_RHOPHASE, MT_RHOEFF, MT_WABS = (
     0, 8, 12, 16, 20, 24, 28, 30)
 
 
+OUTPUTS = {"direct": 0, "smooth": 1}   # MTGPU_OUTPUT_DIRECT / MTGPU_OUTPUT_SMOOTH
+
+
 class Receivers:
-    def __init__(self, assembly, points):
+    """output="direct": the edge basis evaluated at the receiver (the
+    reference's direct output); output="smooth": the reference's default
+    output, subdomain L2-projection smoothing over `levels` neighbour levels
+    (include/mtgpu.h, mtgpu_receivers_set_output).  The assembly must outlive
+    a smoothed Receivers."""
+
+    def __init__(self, assembly, points, output="direct", levels=5):
         pts = np.ascontiguousarray(np.reshape(points, (-1, 3)), np.float64)
+        if output not in OUTPUTS:
+            raise ValueError(f"output must be one of {sorted(OUTPUTS)}")
         h = C.c_void_p()
         rc = _lib.lib().mtgpu_receivers_create(assembly._h, len(pts), pts, C.byref(h))
         _lib.check(rc, "mtgpu_receivers_create")
         self._h = h
         self.nrec = len(pts)
         self.points = pts
+        self.output = output
+        self._assembly = assembly   # kept alive for the smoothing output
+        if output != "direct":
+            rc = _lib.lib().mtgpu_receivers_set_output(h, assembly._h, OUTPUTS[output], levels)
+            _lib.check(rc, "mtgpu_receivers_set_output")
+
+    def smoothing_info(self):
+        """Per smoothing subdomain (0: curl A, all materials; then A per
+        material): material, bricks, nodes; and the conjugate-gradient
+        iterations of the last fields() call."""
+        n, it = C.c_int(), C.c_int()
+        mx = 64
+        mat, cells, nodes = (np.zeros(mx, np.int32) for _ in range(3))
+        rc = _lib.lib().mtgpu_receivers_smoothing_info(
+            self._h, mx, C.byref(n), mat.ctypes.data_as(C.c_void_p),
+            cells.ctypes.data_as(C.c_void_p), nodes.ctypes.data_as(C.c_void_p), C.byref(it))
+        _lib.check(rc, "mtgpu_receivers_smoothing_info")
+        k = min(n.value, mx)
+        return {"material": mat[:k].tolist(), "cells": cells[:k].tolist(),
+                "nodes": nodes[:k].tolist(), "iterations": it.value}
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:

@@ -13,6 +13,11 @@
 #   RegularMeshBuilder  Code/RegularMeshBuilder/*.cpp (two fixes streamed in, ref_fix_rmb.py)
 #   ref_receivers  Code/OutputNu/{T_Brick,OutputArbitrary,For_Solvers,in_out}.cpp
 #                plus ref_receivers_main.cpp: the receiver evaluation
+#   ref_smoothing  Code/OutputNu/{OutputResultant3d,Subdomain,Hex_Local_Matrix,
+#                Portret,ElemNeib,FormatConverter,T_Brick,For_Solvers,in_out,
+#                iobinary}.cpp (Subdomain.cpp through ref_fix_subdomain.py)
+#                plus ref_smoothing_main.cpp and ref_shim/pardiso_shim.cpp:
+#                the default (smoothing) receiver output
 #
 # Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
 set -euo pipefail
@@ -73,6 +78,37 @@ build_receivers() {
     echo "build_ref: $OUT/ref_receivers"
 }
 build_receivers
+
+# Receiver output by subdomain smoothing (the reference's default path):
+# the OutputNu classes it needs, built as for Windows' 4-byte `long`
+# (llp64.h: Subdomain passes int arrays through `long*`), with PARDISO
+# replaced by oracle/ref_shim/pardiso_shim.cpp.  iobinary.cpp defines both
+# the int and the long binary readers, so it is built without llp64.h.
+build_smoothing() {
+    local src="$REF/Code/OutputNu"
+    local objdir="$OUT/obj_OutputNu_smoothing"
+    mkdir -p "$objdir"
+    local flags=("${COMMON[@]}" -include "$SHIM/llp64.h" -I "$SHIM/mkl" -I "$src")
+    local objs=()
+    for n in OutputResultant3d Hex_Local_Matrix Portret ElemNeib FormatConverter T_Brick \
+             For_Solvers in_out; do
+        "$CXX" "${flags[@]}" -c "$src/$n.cpp" -o "$objdir/$n.o" &
+        objs+=("$objdir/$n.o")
+    done
+    python3 "$HERE/ref_fix_subdomain.py" "$REF" |
+        "$CXX" "${flags[@]}" -x c++ -c - -o "$objdir/Subdomain.o" &
+    objs+=("$objdir/Subdomain.o")
+    "$CXX" "${COMMON[@]}" -I "$SHIM/mkl" -I "$src" -c "$src/iobinary.cpp" -o "$objdir/iobinary.o" &
+    objs+=("$objdir/iobinary.o")
+    "$CXX" "${flags[@]}" -c "$SHIM/pardiso_shim.cpp" -o "$objdir/pardiso_shim.o" &
+    objs+=("$objdir/pardiso_shim.o")
+    "$CXX" "${flags[@]}" -c "$HERE/ref_smoothing_main.cpp" -o "$objdir/main.o" &
+    objs+=("$objdir/main.o")
+    wait
+    "$CXX" -fopenmp -o "$OUT/ref_smoothing" "${objs[@]}"
+    echo "build_ref: $OUT/ref_smoothing"
+}
+build_smoothing
 
 # RegularMeshBuilder (Code/RegularMeshBuilder): main.cpp passes through
 # oracle/ref_fix_rmb.py (two compile/run fixes, streamed into the compiler;

@@ -2,9 +2,11 @@
 reproduced end to end on the GPU through the survey driver: the reference's
 input files of the example model (written from tests/golden/dtm_625_500.npz)
 with 625/500 m steps, the mesh builder, device assembly, batched solves,
-receiver fields, MT responses and the results table.  The table was computed
-with the reference's smoothing output path and FP32 post-processing, so the
-check is at the percent level."""
+receiver fields by the reference's default output (subdomain smoothing), MT
+responses and the results table.  The table holds FP32 post-processing
+printed to 7 digits; the direct output (evaluation at the receiver, no
+smoothing) differs from it at the percent level, the smoothing output at
+the 1e-4 level."""
 import os
 
 import numpy as np
@@ -41,12 +43,13 @@ def write_case(d, g, periods, eps):
                 f"{_f(s[3][0])} {_f(s[3][1])}\n{_f(eps)}\n50000\n")
 
 
-def test_dtm_through_the_driver_matches_published_table(gpu, tmp_path):
+@pytest.mark.parametrize("output", ["smooth", "direct"])
+def test_dtm_through_the_driver_matches_published_table(gpu, tmp_path, output):
     g = np.load(os.path.join(GOLDEN, "dtm_625_500.npz"))
     periods = g["periods"][PICK]
     write_case(str(tmp_path), g, periods, 1e-8)
     out = str(tmp_path / "results.txt")
-    calc.main([str(tmp_path), "--out", out])
+    calc.main([str(tmp_path), "--out", out, "--output", output])
     tab = np.loadtxt(out, skiprows=1)
     assert tab.shape == (len(g["stations"]) * len(periods), 11)
     pub = g["published"][:, PICK]
@@ -58,6 +61,11 @@ def test_dtm_through_the_driver_matches_published_table(gpu, tmp_path):
         ref = pub[r[0], p[0]]
         z_err += list(np.abs(row[4:6] - ref[1:3]) / ref[1:3])
         r_err += list(np.abs(row[8:10] - ref[5:7]) / ref[5:7])
-    assert np.median(z_err) < 0.005
-    assert max(z_err) < 0.03
-    assert max(r_err) < 0.06
+    if output == "smooth":
+        assert np.median(z_err) < 3e-4
+        assert max(z_err) < 0.005
+        assert max(r_err) < 0.01
+    else:
+        assert np.median(z_err) < 0.005
+        assert max(z_err) < 0.03
+        assert max(r_err) < 0.06
