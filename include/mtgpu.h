@@ -268,15 +268,23 @@ int mtgpu_survey_spmv_timed(mtgpu_survey *s, int reps, float *ms);
 
 /* The SpMV variant the set-up autotuning chose (0: x segments and matrix
  * slots staged in shared memory per tile of slices; 1: x segments staged
- * only; 2, 4, 8: slots in flight per thread, gathers from global memory) and
- * the times (ms per launch) it measured for the variants 0, 1, 2, 4, 8
- * (ms[5]; 0 where a variant was not available). */
+ * only; 2, 4, 8: slots in flight per thread, gathers from global memory;
+ * 18, 20: two-system batches only, one thread per row for both systems with
+ * 2 or 4 slots in flight; 32: matrix-free, tensor meshes only: the curl-curl
+ * part as D^T F D (edge -> face circulations, face mass matrix) and the mass
+ * part regenerated from six weights per cell instead of the stored matrix)
+ * and the times (ms per launch) it measured for the variants 0, 1, 2, 4, 8,
+ * 18, 20, 32 (ms[8]; 0 where a variant was not available). */
 int mtgpu_survey_tuning(const mtgpu_survey *s, int *variant, float *ms);
 
-/* Pins the SpMV variant (0, 1, 2, 4 or 8) instead of the autotuned choice;
- * all variants sum the same products in the same order.  MTGPU_ERR_ARG if
- * the variant is unknown or unavailable for this survey (0 and 1 need their
- * tiles to fit shared memory). */
+/* Pins the SpMV variant (0, 1, 2, 4, 8, 18, 20 or 32) instead of the
+ * autotuned choice.  The stored-matrix variants sum the same products in the
+ * same order; the matrix-free one computes the same operator in another
+ * order (it is enabled only where a set-up product agrees with the stored
+ * matrix's to 1e-9).  MTGPU_ERR_ARG if the variant is unknown or unavailable
+ * for this survey (0 and 1 need their tiles to fit shared memory, 18 and 20
+ * two systems, 32 a survey created from an assembly of a tensor mesh with
+ * RegularMeshBuilder's numbering and all outer nodes Dirichlet). */
 int mtgpu_survey_set_spmv_variant(mtgpu_survey *s, int variant);
 
 void mtgpu_survey_destroy(mtgpu_survey *s);

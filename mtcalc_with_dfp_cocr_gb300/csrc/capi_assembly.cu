@@ -207,7 +207,7 @@ int mtgpu_survey_create(mtgpu_assembly *a, int S, const double *nu, void *stream
     mtgpu_mesh_desc mesh{a->P.kpar, a->P.nb, a->P.kuzlov, a->nvkat.data(), a->nver.data(),
                          a->sigflag.data(), a->edges.data(), a->ig_t.data(), a->ig_t.data(),
                          nullptr, a->bound.data(), a->nver_stride};
-    int rc = survey_setup(a->P, mesh, S, om.data(), s->V, s->st);
+    int rc = survey_setup(a->P, mesh, S, om.data(), s->V, s->st, a);
     if (rc) {
         mtgpu_survey_destroy(s);
         return rc;
@@ -266,17 +266,15 @@ int mtgpu_survey_tuning(const mtgpu_survey *s, int *variant, float *ms)
     MTGPU_CHECK_ARG(s != nullptr, "null survey");
     if (variant) *variant = s->V.ch;
     if (ms)
-        for (int i = 0; i < 5; i++) ms[i] = s->V.tune_ms[i];
+        for (int i = 0; i < kSpmvVariants; i++) ms[i] = s->V.tune_ms[i];
     return MTGPU_OK;
 }
 
 int mtgpu_survey_set_spmv_variant(mtgpu_survey *s, int variant)
 {
     MTGPU_CHECK_ARG(s != nullptr, "null survey");
-    MTGPU_CHECK_ARG(variant == 0 || variant == 1 || variant == 2 || variant == 4 || variant == 8,
-                    "SpMV variant must be 0, 1, 2, 4 or 8");
-    MTGPU_CHECK_ARG(variant > 1 || s->V.ntiles > 0,
-                    "the tiled SpMV variants are not available for this survey");
+    MTGPU_CHECK_ARG(spmv_variant_available(s->V, variant),
+                    "unknown SpMV variant, or not available for this survey");
     return survey_set_variant(s->V, variant);
 }
 

@@ -53,6 +53,16 @@ void Survey::release()
     if (hsys) cudaFreeHost(hsys);
     hsys = nullptr;
     G.release();
+    mf.release();
+}
+
+void MatFree::release()
+{
+    dev_free(rb);
+    dev_free(code);
+    dev_free(w);
+    dev_free(f);
+    on = false;
 }
 
 namespace {
@@ -468,6 +478,14 @@ struct SpmvTail {
     __device__ __forceinline__ void finish(SysState *sys, double *partials, int mode)
     {
         double v[3] = {zsr.to_double(), zsi.to_double(), nn.to_double()};
+        finish_v<SP, NT>(v, sys, partials, mode);
+    }
+    // the same from this thread's (z, s) re, im and ||s_m||^2 of system
+    // threadIdx.x % SP
+    template <int SP, int NT = kB>
+    static __device__ __forceinline__ void finish_v(double (&v)[3], SysState *sys,
+                                                    double *partials, int mode)
+    {
         __shared__ double tot[3][32];
         if (sys_grid_sum<SP, 3, NT>(v, partials, &sys[0].ticket[3], tot) && threadIdx.x < SP) {
             SysState &q = sys[threadIdx.x];
@@ -515,6 +533,401 @@ k_spmv(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict
         tail.row(i, spmv_row<SP, CH>(A, row, k, om, s), sv4, r, z, sm);
     }
     tail.finish<SP>(sys, partials, mode);
+}
+
+// y_k = (K + i omega_k M) x_k of one row for all SP systems in one thread:
+// the row's column indices and matrix values are loaded once and serve
+// every system (SP = 2: the x values of a column for both systems are one
+// contiguous 32-byte pair).  Per system the products are summed in the same
+// slot order as spmv_row.
+template <int SP, int CH>
+__device__ __forceinline__ void spmv_row_all(const Mat &A, int row, const df (&om)[SP],
+                                             const float4 *__restrict__ x, dfc (&y)[SP])
+{
+    const int sl = row >> 5, l = row & 31;
+    acc kr_[SP], ki_[SP], mr_[SP], mi_[SP];
+    {
+        const long long b0 = A.pc[sl] + l;
+        const int *__restrict__ cc = A.col_c + b0;
+        const float2 *__restrict__ kk = A.kc + b0;
+        const float2 *__restrict__ mm = A.mc + b0;
+        const int n = A.wc[sl];
+        for (int q = 0; q < n; q += CH) {
+            int c[CH];
+            float2 kv[CH], mv[CH];
+            float4 xv[CH][SP];
+#pragma unroll
+            for (int j = 0; j < CH; j++) {
+                const bool in = q + j < n;
+                c[j] = in ? __ldg(cc + kSlice * (q + j)) : -1;
+                kv[j] = in ? __ldg(kk + kSlice * (q + j)) : make_float2(0.f, 0.f);
+                mv[j] = in ? __ldg(mm + kSlice * (q + j)) : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int j = 0; j < CH; j++)
+#pragma unroll
+                for (int k = 0; k < SP; k++)
+                    xv[j][k] = c[j] >= 0 ? __ldg(x + (long long)c[j] * SP + k)
+                                         : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int j = 0; j < CH; j++) {
+                if (c[j] < 0) break;
+                const df kd = d2f(kv[j]), md = d2f(mv[j]);
+#pragma unroll
+                for (int k = 0; k < SP; k++) {
+                    const df xr{xv[j][k].x, xv[j][k].y}, xi{xv[j][k].z, xv[j][k].w};
+                    kr_[k].mac(kd, xr);
+                    ki_[k].mac(kd, xi);
+                    mr_[k].mac(md, xr);
+                    mi_[k].mac(md, xi);
+                }
+            }
+        }
+    }
+    {
+        const long long b0 = A.pr[sl] + l;
+        const int *__restrict__ cc = A.col_r + b0;
+        const float2 *__restrict__ kk = A.kr + b0;
+        const int n = A.wr[sl];
+        for (int q = 0; q < n; q += 2 * CH) {
+            int c[2 * CH];
+            float2 kv[2 * CH];
+            float4 xv[2 * CH][SP];
+#pragma unroll
+            for (int j = 0; j < 2 * CH; j++) {
+                const bool in = q + j < n;
+                c[j] = in ? __ldg(cc + kSlice * (q + j)) : -1;
+                kv[j] = in ? __ldg(kk + kSlice * (q + j)) : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int j = 0; j < 2 * CH; j++)
+#pragma unroll
+                for (int k = 0; k < SP; k++)
+                    xv[j][k] = c[j] >= 0 ? __ldg(x + (long long)c[j] * SP + k)
+                                         : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int j = 0; j < 2 * CH; j++) {
+                if (c[j] < 0) break;
+                const df kd = d2f(kv[j]);
+#pragma unroll
+                for (int k = 0; k < SP; k++) {
+                    kr_[k].mac(kd, df{xv[j][k].x, xv[j][k].y});
+                    ki_[k].mac(kd, df{xv[j][k].z, xv[j][k].w});
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < SP; k++) {
+        const df mxr = mr_[k].get(), mxi = mi_[k].get();
+        kr_[k].mac(neg(om[k]), mxi);
+        ki_[k].mac(om[k], mxr);
+        y[k] = dfc{kr_[k].get(), ki_[k].get()};
+    }
+}
+
+// The SpMV with one thread per row serving both systems of a two-system
+// batch (variants 16 + CH): half the matrix-slot loads of k_spmv, twice the
+// independent work per thread.  Before the grid reduction every lane pair
+// swaps partial sums so that lane l carries system l % 2, the layout
+// sys_grid_sum expects.
+template <int CH>
+__global__ void __launch_bounds__(kB, 2)
+k_spmv_r2(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict__ s,
+          const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
+          SysState *sys, double *partials, int mode)
+{
+    constexpr int SP = 2;
+    bool on[SP];
+    df om[SP];
+    SpmvTail tail[SP];
+#pragma unroll
+    for (int k = 0; k < SP; k++) {
+        on[k] = sys[k].status == kRun;
+        om[k] = d2f(omega[k]);
+        tail[k].mm = mode ? sys[k].mrs_mode : 0;
+        tail[k].wm = from_double(sys[k].mrs_w);
+    }
+    if (on[0] || on[1]) {
+        for (int row = blockIdx.x * kB + threadIdx.x; row < nb; row += gridDim.x * kB) {
+            dfc y[SP];
+            spmv_row_all<SP, CH>(A, row, om, s, y);
+#pragma unroll
+            for (int k = 0; k < SP; k++) {
+                if (!on[k]) continue;
+                const long long i = (long long)row * SP + k;
+                tail[k].row(i, y[k], __ldg(s + i), r, z, sm);
+            }
+        }
+    }
+    const bool odd = threadIdx.x & 1;
+    double v[3];
+    const double a0[3] = {tail[0].zsr.to_double(), tail[0].zsi.to_double(), tail[0].nn.to_double()};
+    const double a1[3] = {tail[1].zsr.to_double(), tail[1].zsi.to_double(), tail[1].nn.to_double()};
+#pragma unroll
+    for (int n = 0; n < 3; n++) {
+        const double mine = odd ? a1[n] : a0[n], give = odd ? a0[n] : a1[n];
+        v[n] = mine + __shfl_xor_sync(0xffffffffu, give, 1);
+    }
+    SpmvTail::finish_v<SP>(v, sys, partials, mode);
+}
+
+// ------------------------------------------------ matrix-free SpMV (tensor meshes)
+// On a tensor mesh with RegularMeshBuilder's numbering the brick matrices
+// factor: the curl-curl matrix B = D^T F D with D the 6 x 12 edge -> face
+// circulation operator (entries +-1) and F block diagonal, per direction d
+// (2 h_d / (h_t1 h_t2)) m, m = [[2/3, 1/3], [1/3, 2/3]] coupling the two
+// faces of normal d; the edge mass matrix C is, per direction,
+// (h_t1 h_t2 / h_d) m (x) m over the 4 parallel edges (both from the brick
+// matrices of T_Brick.cpp:1361-1395 as oracle/mtcalc_oracle.c restates
+// them).  So A s = D^T F_g D s + i omega M s with F_g, M regenerated from
+// six weights per cell (wF / 3 and sigma wM / 9, double-float; the 1/3 and
+// 1/9 make the remaining multipliers 1, 2, 4, exact) instead of 33 stored
+// slots per row.  Two passes: the circulation of every face
+// (k_mf_faces), then per edge the 4 faces through it, their neighbours
+// along the normal and the 3 x 3 parallel edges of the 4 cells around it
+// (k_mf_edges, with the SpMV tail).  Dirichlet edges (both nodes on the
+// boundary) read as 0 and map to themselves, as in the assembled matrix.
+struct MF {
+    int nx, ny, nz;
+    long long nfx, nfy, nfz, ncell;
+    const int *rb;
+    const unsigned *code;
+    const float2 *w;
+    const unsigned char *bedge;
+    float4 *f;
+};
+
+// edge of direction d leaving node (i, j, k): the node's first edge
+// rb + i (1 + [j < ny-1] + [k < nz-1]), then +x, +y, +z as present
+__device__ __forceinline__ long long mf_edge(const MF &M, int d, int i, int j, int k)
+{
+    const int ey = j < M.ny - 1, ex = i < M.nx - 1;
+    long long e = (long long)__ldg(M.rb + k * M.ny + j) + (long long)i * (1 + ey + (k < M.nz - 1));
+    if (d >= 1) e += ex;
+    if (d == 2) e += ey;
+    return e;
+}
+
+// face of normal n at (i, j, k): line index along n, cell indices across
+__device__ __forceinline__ long long mf_face(const MF &M, int n, int i, int j, int k)
+{
+    if (n == 0) return ((long long)k * (M.ny - 1) + j) * M.nx + i;
+    if (n == 1) return M.nfx + ((long long)k * M.ny + j) * (M.nx - 1) + i;
+    return M.nfx + M.nfy + ((long long)k * (M.ny - 1) + j) * (M.nx - 1) + i;
+}
+
+template <int SP>
+__device__ __forceinline__ dfc mf_x(const MF &M, const float4 *__restrict__ x, long long e, int k)
+{
+    if (__ldg(M.bedge + e)) return dfc{df{0.f, 0.f}, df{0.f, 0.f}};
+    return from4(__ldg(x + e * SP + k));
+}
+
+// f = D s: x(e0) + x(e1) - x(e2) - x(e3) around every face (counterclockwise
+// seen from +n: y then z for n = x, z then x for n = y, x then y for n = z)
+template <int SP>
+__global__ void __launch_bounds__(kB)
+k_mf_faces(MF M, const float4 *__restrict__ x, const SysState *sys)
+{
+    const int k = threadIdx.x % SP;
+    if (sys[k].status != kRun) return;
+    const long long nf = M.nfx + M.nfy + M.nfz;
+    const int rpb = kB / SP;
+    for (long long t = (long long)blockIdx.x * rpb + threadIdx.x / SP; t < nf;
+         t += (long long)gridDim.x * rpb) {
+        long long q = t;
+        int n, i, j, kk;
+        if (q < M.nfx) {
+            n = 0;
+            i = (int)(q % M.nx);
+            q /= M.nx;
+            j = (int)(q % (M.ny - 1));
+            kk = (int)(q / (M.ny - 1));
+        } else if ((q -= M.nfx) < M.nfy) {
+            n = 1;
+            i = (int)(q % (M.nx - 1));
+            q /= (M.nx - 1);
+            j = (int)(q % M.ny);
+            kk = (int)(q / M.ny);
+        } else {
+            q -= M.nfy;
+            n = 2;
+            i = (int)(q % (M.nx - 1));
+            q /= (M.nx - 1);
+            j = (int)(q % (M.ny - 1));
+            kk = (int)(q / (M.ny - 1));
+        }
+        long long e0, e1, e2, e3;
+        if (n == 0) {
+            e0 = mf_edge(M, 1, i, j, kk);
+            e1 = mf_edge(M, 2, i, j + 1, kk);
+            e2 = mf_edge(M, 1, i, j, kk + 1);
+            e3 = mf_edge(M, 2, i, j, kk);
+        } else if (n == 1) {
+            e0 = mf_edge(M, 2, i, j, kk);
+            e1 = mf_edge(M, 0, i, j, kk + 1);
+            e2 = mf_edge(M, 2, i + 1, j, kk);
+            e3 = mf_edge(M, 0, i, j, kk);
+        } else {
+            e0 = mf_edge(M, 0, i, j, kk);
+            e1 = mf_edge(M, 1, i + 1, j, kk);
+            e2 = mf_edge(M, 0, i, j + 1, kk);
+            e3 = mf_edge(M, 1, i, j, kk);
+        }
+        const dfc a = mf_x<SP>(M, x, e0, k), b = mf_x<SP>(M, x, e1, k);
+        const dfc c = mf_x<SP>(M, x, e2, k), d = mf_x<SP>(M, x, e3, k);
+        acc fr, fi;
+        fr.add(a.re); fr.add(b.re); fr.add(neg(c.re)); fr.add(neg(d.re));
+        fi.add(a.im); fi.add(b.im); fi.add(neg(c.im)); fi.add(neg(d.im));
+        M.f[t * SP + k] = to4(dfc{fr.get(), fi.get()});
+    }
+}
+
+__device__ __forceinline__ df scale(df a, float s) { return df{a.h * s, a.l * s}; }   // s = +-1, 2, 4
+
+// one non-Dirichlet edge of direction d at lattice position p (p[d] the
+// cell index along d, the others line indices): (K + i omega M) s.
+// Positions are kept as three scalars moved along the unit steps of t1 and
+// t2 (no runtime-indexed arrays, which would live in local memory).
+struct Pos {
+    int x, y, z;
+};
+__device__ __forceinline__ Pos mv(Pos p, Pos u, int o) { return Pos{p.x + o * u.x, p.y + o * u.y, p.z + o * u.z}; }
+__device__ __forceinline__ Pos unit(int a) { return Pos{a == 0, a == 1, a == 2}; }
+
+template <int SP>
+__device__ __forceinline__ dfc mf_row(const MF &M, long long e, int k, df om,
+                                      const float4 *__restrict__ x)
+{
+    const unsigned c = __ldg(M.code + e);
+    const int d = (int)(c >> 30);
+    const Pos p{(int)(c & 1023u), (int)((c >> 10) & 1023u), (int)((c >> 20) & 1023u)};
+    const int t1 = d == 2 ? 0 : d + 1, t2 = d == 0 ? 2 : d - 1;
+    const Pos u1 = unit(t1), u2 = unit(t2);
+    auto cell = [&](Pos q) { return ((long long)q.z * (M.ny - 1) + q.y) * (M.nx - 1) + q.x; };
+    // weights of the 4 cells around the edge, offsets (a - 1, b - 1) along (t1, t2)
+    df w1[2][2], w2[2][2], wm[2][2];
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 2; b++) {
+            const long long cc = cell(mv(mv(p, u1, a - 1), u2, b - 1));
+            w1[a][b] = d2f(__ldg(M.w + (long long)t1 * M.ncell + cc));
+            w2[a][b] = d2f(__ldg(M.w + (long long)t2 * M.ncell + cc));
+            wm[a][b] = d2f(__ldg(M.w + (long long)(3 + d) * M.ncell + cc));
+        }
+    acc kr, ki, mr, mi;
+    // D^T F D: faces of normal t1 through the edge (t2 cells b - 1 = -1: +1,
+    // 0: -1), then faces of normal t2 (t1 cells -1: -1, 0: +1); each face's
+    // F row: wa (f_-1 + 2 f_0) + wb (2 f_0 + f_+1) over the cells before and
+    // after it along the normal
+#pragma unroll
+    for (int nn = 0; nn < 2; nn++) {
+        const int n = nn == 0 ? t1 : t2;
+        const Pos un = nn == 0 ? u1 : u2, uo = nn == 0 ? u2 : u1;
+#pragma unroll
+        for (int b = 0; b < 2; b++) {
+            const Pos q = mv(p, uo, b - 1);
+            const float sg = nn == 0 ? (b == 0 ? 1.f : -1.f) : (b == 0 ? -1.f : 1.f);
+            const df wa = nn == 0 ? w1[0][b] : w2[b][0], wb = nn == 0 ? w1[1][b] : w2[b][1];
+            const Pos qm = mv(q, un, -1), qp = mv(q, un, 1);
+            const dfc fm = from4(__ldg(M.f + mf_face(M, n, qm.x, qm.y, qm.z) * SP + k));
+            const dfc f0 = from4(__ldg(M.f + mf_face(M, n, q.x, q.y, q.z) * SP + k));
+            const dfc fp = from4(__ldg(M.f + mf_face(M, n, qp.x, qp.y, qp.z) * SP + k));
+            const df ca = scale(wa, sg), cb = scale(wb, sg), c0 = scale(add(wa, wb), 2.f * sg);
+            kr.mac(ca, fm.re); kr.mac(c0, f0.re); kr.mac(cb, fp.re);
+            ki.mac(ca, fm.im); ki.mac(c0, f0.im); ki.mac(cb, fp.im);
+        }
+    }
+    // M: the 3 x 3 parallel edges around, each cell's 4 with multipliers
+    // 4 (this edge's position), 2 (one axis off), 1 (the diagonal)
+    dfc xv[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            const Pos q = mv(mv(p, u1, a - 1), u2, b - 1);
+            xv[a][b] = mf_x<SP>(M, x, mf_edge(M, d, q.x, q.y, q.z), k);
+        }
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 2; b++)
+#pragma unroll
+            for (int a2 = 0; a2 < 2; a2++)
+#pragma unroll
+                for (int b2 = 0; b2 < 2; b2++) {
+                    // cell (a, b) holds offsets (a + a2 - 1, b + b2 - 1); this edge is at (1 - a, 1 - b)
+                    const float mult = (a2 == 1 - a ? 2.f : 1.f) * (b2 == 1 - b ? 2.f : 1.f);
+                    const df cw = scale(wm[a][b], mult);
+                    const dfc xe = xv[a + a2][b + b2];
+                    mr.mac(cw, xe.re);
+                    mi.mac(cw, xe.im);
+                }
+    const df mxr = mr.get(), mxi = mi.get();
+    kr.mac(neg(om), mxi);
+    ki.mac(om, mxr);
+    return dfc{kr.get(), ki.get()};
+}
+
+// z = A s by the matrix-free operator, with the SpMV tail of k_spmv
+template <int SP>
+__global__ void __launch_bounds__(kB, 2)
+k_mf_edges(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restrict__ s,
+           const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
+           SysState *sys, double *partials, int mode)
+{
+    const int k = threadIdx.x % SP;
+    const bool on = sys[k].status == kRun;
+    const df om = d2f(omega[k]);
+    SpmvTail tail;
+    tail.mm = mode ? sys[k].mrs_mode : 0;
+    tail.wm = from_double(sys[k].mrs_w);
+    const int rpb = kB / SP;
+    for (int row = blockIdx.x * rpb + threadIdx.x / SP; row < nb; row += gridDim.x * rpb) {
+        if (!on) continue;
+        const long long i = (long long)row * SP + k;
+        const float4 sv4 = __ldg(s + i);
+        const dfc y = __ldg(M.bedge + row) ? from4(sv4) : mf_row<SP>(M, row, k, om, s);
+        tail.row(i, y, sv4, r, z, sm);
+    }
+    tail.finish<SP>(sys, partials, mode);
+}
+
+// largest |a - b| and |b| over n float4 double-float pairs (as ordered bits
+// of non-negative doubles)
+__global__ void k_maxdiff(long long n, const float4 *__restrict__ a, const float4 *__restrict__ b,
+                          unsigned long long *out)
+{
+    double dm = 0.0, bm = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float4 u = a[i], v = b[i];
+        const double ur = (double)u.x + u.y, ui = (double)u.z + u.w;
+        const double vr = (double)v.x + v.y, vi = (double)v.z + v.w;
+        dm = fmax(dm, fmax(fabs(ur - vr), fabs(ui - vi)));
+        bm = fmax(bm, fmax(fabs(vr), fabs(vi)));
+    }
+    atomicMax(out, (unsigned long long)__double_as_longlong(dm));
+    atomicMax(out + 1, (unsigned long long)__double_as_longlong(bm));
+}
+
+// a fixed pseudo-random test vector (double-float values in [-1, 1))
+__global__ void k_pattern(long long n, float4 *v)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        unsigned h = (unsigned)i * 2654435761u + 12345u;
+        float q[4];
+        for (int t = 0; t < 4; t++) {
+            h ^= h >> 15;
+            h *= 2246822519u;
+            h ^= h >> 13;
+            q[t] = (float)(h & 0xffffffu) / 8388608.0f - 1.0f;
+        }
+        v[i] = make_float4(q[0], 0.f, q[2] * (1.f + 0.25f * q[1] * q[3]), 0.f);
+    }
 }
 
 // ------------------------------------------------ tiled SpMV (x staged)
@@ -982,9 +1395,23 @@ struct Impl {
         return TileMat{P.d_wc, P.d_wr, P.d_pc, P.d_pr, V.kc, V.mc, V.kr, V.lc, V.lr,
                        V.uoff, V.ucol, V.tile_T, V.ntiles, P.nslices};
     }
+    static MF mfd(const Survey &V)
+    {
+        const MatFree &F = V.mf;
+        return MF{F.nx, F.ny, F.nz, F.nfx, F.nfy, F.nfz,
+                  (long long)(F.nx - 1) * (F.ny - 1) * (F.nz - 1), F.rb, F.code, F.w,
+                  V.P->d_bedge, F.f};
+    }
     static void spmv(Survey &V, int mode)
     {
         const Mat A = mat(V);
+        if (V.ch == kMatFree) {
+            const MF M = mfd(V);
+            k_mf_faces<SP><<<V.g_mff, kB, 0, V.st>>>(M, V.s, V.sys);
+            k_mf_edges<SP><<<V.g_mfe, kB, 0, V.st>>>(V.nb, M, V.omega, V.s, V.r, V.z, V.sm, V.sys,
+                                                    V.partials, mode);
+            return;
+        }
         if (V.ch == 0) {
             k_spmv_t<SP, true><<<V.g_spmv_t, TileCfg<SP>::NT, V.tile_smem, V.st>>>(
                 V.nb, tmat(V), V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode);
@@ -994,6 +1421,16 @@ struct Impl {
             k_spmv_t<SP, false><<<V.g_spmv_tx, TileCfg<SP>::NT, V.tile_smem_x, V.st>>>(
                 V.nb, tmat(V), V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode);
             return;
+        }
+        if constexpr (SP == 2) {
+            if (V.ch == kRowVariant + 2) {
+                k_spmv_r2<2><<<V.g_spmv, kB, 0, V.st>>>(V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode);
+                return;
+            }
+            if (V.ch == kRowVariant + 4) {
+                k_spmv_r2<4><<<V.g_spmv, kB, 0, V.st>>>(V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode);
+                return;
+            }
         }
         switch (V.ch) {
         case 2: k_spmv<SP, 2><<<V.g_spmv, kB, 0, V.st>>>(V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode); break;
@@ -1062,6 +1499,19 @@ struct Impl {
         const void *fs = V.ch == 2 ? (const void *)k_spmv<SP, 2>
                          : V.ch == 8 ? (const void *)k_spmv<SP, 8> : (const void *)k_spmv<SP, 4>;
         V.g_spmv = g(fs, V.grid_rows);
+        if (V.mf.on) {
+            const long long nf = V.mf.nfx + V.mf.nfy + V.mf.nfz;
+            V.g_mff = g((const void *)k_mf_faces<SP>, (int)std::min<long long>(
+                                                          (nf + kB / SP - 1) / (kB / SP), INT_MAX));
+            V.g_mfe = g((const void *)k_mf_edges<SP>, V.grid_rows);
+        }
+        if constexpr (SP == 2) {
+            if (V.ch == kRowVariant + 2 || V.ch == kRowVariant + 4) {
+                const void *fr = V.ch == kRowVariant + 2 ? (const void *)k_spmv_r2<2>
+                                                         : (const void *)k_spmv_r2<4>;
+                V.g_spmv = g(fr, (V.nb + kB - 1) / kB);
+            }
+        }
         if (V.ntiles > 0) {
             int b = 0;
             if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (const void *)k_spmv_t<SP, true>,
@@ -1184,8 +1634,165 @@ int build_tiles(Survey &V, int nsm)
 
 }  // namespace
 
+namespace {
+
+// The matrix-free variant's tables, when the assembly's mesh is a tensor
+// mesh numbered as RegularMeshBuilder numbers it (nodes x fastest, cells
+// likewise, edges per node +x, +y, +z, every node of the outer surface a
+// Dirichlet node); anything else leaves the variant off.  A set-up check
+// compares one matrix-free product with the stored-matrix product and
+// leaves the variant off unless they agree to 1e-9.
+int matfree_build(Survey &V, const mtgpu_assembly_s &a, int nsm)
+{
+    MatFree &F = V.mf;
+    F.release();
+    const ParamMatrix &P = *V.P;
+    const int kuz = P.kuzlov, ns = a.nver_stride;
+    const std::vector<double> &xyz = a.xyz;
+    if ((long long)xyz.size() != 3LL * kuz || kuz < 27 || ns < 8) return MTGPU_OK;
+    int nx = 1;
+    while (nx < kuz && xyz[3 * nx + 1] == xyz[1] && xyz[3 * nx + 2] == xyz[2]) nx++;
+    int nxy = nx;
+    while (nxy < kuz && xyz[3 * nxy + 2] == xyz[2]) nxy++;
+    if (nxy % nx || kuz % nxy) return MTGPU_OK;
+    const int ny = nxy / nx, nz = kuz / nxy;
+    if (nx < 3 || ny < 3 || nz < 3 || nx > 1024 || ny > 1024 || nz > 1024) return MTGPU_OK;
+    std::vector<double> X(nx), Y(ny), Z(nz);
+    for (int i = 0; i < nx; i++) X[i] = xyz[3 * i];
+    for (int j = 0; j < ny; j++) Y[j] = xyz[3 * (j * nx) + 1];
+    for (int k = 0; k < nz; k++) Z[k] = xyz[3 * (k * nxy) + 2];
+    for (int i = 1; i < nx; i++) if (!(X[i] > X[i - 1])) return MTGPU_OK;
+    for (int j = 1; j < ny; j++) if (!(Y[j] > Y[j - 1])) return MTGPU_OK;
+    for (int k = 1; k < nz; k++) if (!(Z[k] > Z[k - 1])) return MTGPU_OK;
+    for (int k = 0, n = 0; k < nz; k++)
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++, n++) {
+                if (xyz[3 * n] != X[i] || xyz[3 * n + 1] != Y[j] || xyz[3 * n + 2] != Z[k])
+                    return MTGPU_OK;
+                const bool surf = i == 0 || j == 0 || k == 0 || i == nx - 1 || j == ny - 1 ||
+                                  k == nz - 1;
+                if (surf && !a.bound[n]) return MTGPU_OK;
+            }
+    const long long ncell = (long long)(nx - 1) * (ny - 1) * (nz - 1);
+    if (ncell != P.kpar) return MTGPU_OK;
+    for (int k = 0, c = 0; k < nz - 1; k++)
+        for (int j = 0; j < ny - 1; j++)
+            for (int i = 0; i < nx - 1; i++, c++) {
+                const int n0 = (k * ny + j) * nx + i;
+                const int want[8] = {n0, n0 + 1, n0 + nx, n0 + nx + 1,
+                                     n0 + nxy, n0 + nxy + 1, n0 + nxy + nx, n0 + nxy + nx + 1};
+                for (int t = 0; t < 8; t++)
+                    if (a.nver[(size_t)c * ns + t] != want[t]) return MTGPU_OK;
+            }
+    // edges: node order, +x, +y, +z per node
+    std::vector<int> rb((size_t)ny * nz);
+    std::vector<unsigned> code(P.nb);
+    long long e = 0;
+    for (int k = 0; k < nz; k++)
+        for (int j = 0; j < ny; j++) {
+            rb[(size_t)k * ny + j] = (int)e;
+            for (int i = 0; i < nx; i++) {
+                const int n = (k * ny + j) * nx + i;
+                const int step[3] = {1, nx, nxy};
+                const bool has[3] = {i < nx - 1, j < ny - 1, k < nz - 1};
+                for (int d = 0; d < 3; d++) {
+                    if (!has[d]) continue;
+                    if (e >= P.nb || a.edges[2 * e] != n || a.edges[2 * e + 1] != n + step[d])
+                        return MTGPU_OK;
+                    code[e] = (unsigned)i | ((unsigned)j << 10) | ((unsigned)k << 20) |
+                              ((unsigned)d << 30);
+                    e++;
+                }
+            }
+        }
+    if (e != P.nb) return MTGPU_OK;
+    // per-cell weights from the materials' mu and sigma
+    std::vector<double> mu(P.n_materials), sig(P.n_materials);
+    MTGPU_TRY(cudaMemcpyAsync(mu.data(), P.d_mu, sizeof(double) * P.n_materials,
+                              cudaMemcpyDeviceToHost, V.st));
+    MTGPU_TRY(cudaMemcpyAsync(sig.data(), P.d_sig, sizeof(double) * P.n_materials,
+                              cudaMemcpyDeviceToHost, V.st));
+    MTGPU_TRY(cudaStreamSynchronize(V.st));
+    std::vector<float2> w((size_t)6 * ncell);
+    for (int k = 0, c = 0; k < nz - 1; k++)
+        for (int j = 0; j < ny - 1; j++)
+            for (int i = 0; i < nx - 1; i++, c++) {
+                const int mat = a.nvkat[c];
+                if (mat < 0 || mat >= P.n_materials || !(mu[mat] > 0.0)) return MTGPU_OK;
+                const double h[3] = {X[i + 1] - X[i], Y[j + 1] - Y[j], Z[k + 1] - Z[k]};
+                for (int d = 0; d < 3; d++) {
+                    const int t1 = (d + 1) % 3, t2 = (d + 2) % 3;
+                    const dfl::df f = dfl::from_double(2.0 * h[d] / (h[t1] * h[t2]) / mu[mat] / 3.0);
+                    const dfl::df m = dfl::from_double(sig[mat] * h[t1] * h[t2] / h[d] / 9.0);
+                    w[(size_t)d * ncell + c] = make_float2(f.h, f.l);
+                    w[(size_t)(3 + d) * ncell + c] = make_float2(m.h, m.l);
+                }
+            }
+    F.nx = nx;
+    F.ny = ny;
+    F.nz = nz;
+    F.nfx = (long long)nx * (ny - 1) * (nz - 1);
+    F.nfy = (long long)(nx - 1) * ny * (nz - 1);
+    F.nfz = (long long)(nx - 1) * (ny - 1) * nz;
+    int rc;
+    if ((rc = dev_alloc(&F.rb, rb.size())) || (rc = dev_alloc(&F.code, code.size())) ||
+        (rc = dev_alloc(&F.w, w.size())) ||
+        (rc = dev_alloc(&F.f, (size_t)(F.nfx + F.nfy + F.nfz) * V.SP)))
+        return rc;
+    MTGPU_TRY(cudaMemcpyAsync(F.rb, rb.data(), sizeof(int) * rb.size(), cudaMemcpyHostToDevice, V.st));
+    MTGPU_TRY(cudaMemcpyAsync(F.code, code.data(), sizeof(unsigned) * code.size(),
+                              cudaMemcpyHostToDevice, V.st));
+    MTGPU_TRY(cudaMemcpyAsync(F.w, w.data(), sizeof(float2) * w.size(), cudaMemcpyHostToDevice, V.st));
+    F.on = true;
+    // set-up check against the stored-matrix SpMV on a test vector
+    const int ch = V.ch;
+    std::vector<SysState> init(32);
+    for (int k = 0; k < 32; k++) {
+        SysState q{};
+        q.status = k < V.S ? kRun : MTGPU_OK;
+        q.maxiter = 1;
+        init[k] = q;
+    }
+    const long long n = (long long)V.nb * V.SP;
+    unsigned long long *d_mx = nullptr;
+    if ((rc = dev_alloc(&d_mx, 2))) return rc;
+    MTGPU_TRY(cudaMemcpyAsync(V.sys, init.data(), sizeof(SysState) * 32, cudaMemcpyHostToDevice, V.st));
+    k_pattern<<<4 * nsm, kB, 0, V.st>>>(n, V.s);
+    V.ch = 4;
+    MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+    MTGPU_SP_DISPATCH(V.SP, spmv_only(V));
+    MTGPU_TRY(cudaMemcpyAsync(V.w, V.z, sizeof(float4) * n, cudaMemcpyDeviceToDevice, V.st));
+    MTGPU_TRY(cudaMemcpyAsync(V.sys, init.data(), sizeof(SysState) * 32, cudaMemcpyHostToDevice, V.st));
+    V.ch = kMatFree;
+    MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+    MTGPU_SP_DISPATCH(V.SP, spmv_only(V));
+    MTGPU_TRY(cudaMemsetAsync(d_mx, 0, sizeof(unsigned long long) * 2, V.st));
+    k_maxdiff<<<4 * nsm, kB, 0, V.st>>>(n, V.z, V.w, d_mx);
+    note_launches(5);
+    unsigned long long mx[2] = {0, 0};
+    cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(mx, d_mx, sizeof(mx), cudaMemcpyDeviceToHost, V.st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(V.st);
+    dev_free(d_mx);
+    V.ch = ch;
+    MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+    if (err != cudaSuccess) {
+        set_last_error(err, "matrix-free SpMV set-up check", __FILE__, __LINE__);
+        return MTGPU_ERR_CUDA;
+    }
+    double dm, bm;
+    memcpy(&dm, &mx[0], sizeof(double));
+    memcpy(&bm, &mx[1], sizeof(double));
+    F.check = bm > 0.0 ? dm / bm : 1.0;
+    if (!(F.check < 1e-9)) F.on = false;
+    return MTGPU_OK;
+}
+
+}  // namespace
+
 int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const double *omega,
-                 Survey &V, cudaStream_t st)
+                 Survey &V, cudaStream_t st, const mtgpu_assembly_s *a)
 {
     V.release();
     MTGPU_CHECK_ARG(S >= 1 && S <= 32, "a survey batch holds 1 to 32 systems");
@@ -1261,13 +1868,14 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
     MTGPU_TRY(cudaStreamSynchronize(st));
     note_launches(8);
     if ((rc = build_tiles(V, nsm))) return rc;
+    if (a && (rc = matfree_build(V, *a, nsm))) return rc;
     // autotune the SpMV variant: time each candidate, keep the fastest
     {
-        const int cand[5] = {0, 1, 2, 4, 8};
+        const int cand[kSpmvVariants] = {0, 1, 2, 4, 8, kRowVariant + 2, kRowVariant + 4, kMatFree};
         float best = 1e30f;
         int best_ch = 4;
-        for (int c = 0; c < 5; c++) {
-            if (cand[c] <= 1 && V.ntiles == 0) continue;
+        for (int c = 0; c < kSpmvVariants; c++) {
+            if (!spmv_variant_available(V, cand[c])) continue;
             V.ch = cand[c];
             MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
             float ms = 0.f;
@@ -1416,7 +2024,7 @@ int survey_solve(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, do
         MTGPU_TRY(e);
         V.graph_iters = iters_per_launch;
     }
-    const unsigned long long kpi = V.G.m > 0 ? 4 : 3;
+    const unsigned long long kpi = (V.G.m > 0 ? 4 : 3) + (V.ch == kMatFree ? 1 : 0);
     long long guard = 0;
     const long long guard_max =
         (long long)maxiter + (long long)(kMaxContinue + 1) * 4 * iters_per_launch + 64;

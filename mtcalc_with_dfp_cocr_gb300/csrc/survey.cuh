@@ -23,6 +23,25 @@ struct SysState {
     unsigned int ticket[4];  // block-completion counters (system 0 only)
 };
 
+constexpr int kRowVariant = 16;    // + slots in flight: one thread per row, both systems
+constexpr int kMatFree = 32;       // matrix-free SpMV on tensor meshes
+constexpr int kSpmvVariants = 8;   // 0, 1, 2, 4, 8, 18, 20, 32
+
+// Matrix-free SpMV of a tensor (RegularMeshBuilder) mesh: K = D^T F D with D
+// the edge -> face circulations and F the face mass matrix, M the edge mass
+// matrix, both regenerated from per-cell weights (survey.cu)
+struct MatFree {
+    bool on = false;
+    int nx = 0, ny = 0, nz = 0;      // lines per axis
+    long long nfx = 0, nfy = 0, nfz = 0;
+    int *rb = nullptr;               // [nz][ny] number of the first edge of node (0, j, k)
+    unsigned *code = nullptr;        // [nb] edge position i | j << 10 | k << 20 | direction << 30
+    float2 *w = nullptr;             // [6][cells] double-float wF/3 (x, y, z), wM/9 (x, y, z)
+    float4 *f = nullptr;             // face circulations [faces][SP]
+    double check = -1.0;             // set-up check: max |A_mf s - A s| / max |A s|
+    void release();
+};
+
 struct Survey {
     const ParamMatrix *P = nullptr;
     cudaStream_t st = nullptr;
@@ -30,13 +49,16 @@ struct Survey {
     int grid_rows = 0, grid_nodes = 0;           // work bounds (blocks that have rows)
     int g_init = 0, g_node = 0, g_edge = 0, g_update = 0, g_spmv = 0, g_true = 0;  // launch grids
     // SpMV variant (autotuned): 0 x and matrix slots staged in shared memory per
-    // tile, 1 x staged only, 2/4/8 gathers from global memory with that many slots in flight
+    // tile, 1 x staged only, 2/4/8 gathers from global memory with that many slots in flight,
+    // kRowVariant + 2/4 (two systems only) one thread per row for both systems
     int ch = 4;
     // SpMV tiles: T consecutive SELL slices, their distinct columns, per-slot local indices
     int tile_T = 1, ntiles = 0, tile_smem = 0, tile_smem_x = 0, g_spmv_t = 0, g_spmv_tx = 0;
     int *uoff = nullptr, *ucol = nullptr;
     unsigned short *lc = nullptr, *lr = nullptr;
-    float tune_ms[5] = {0.f, 0.f, 0.f, 0.f, 0.f};  // SpMV times of the variants 0, 1, 2, 4, 8
+    float tune_ms[kSpmvVariants] = {};   // SpMV times of the variants 0, 1, 2, 4, 8, 18, 20, 32
+    MatFree mf;
+    int g_mff = 0, g_mfe = 0;                    // matrix-free launch grids (faces, edges)
     Folded G;                                    // pattern of G and G^T
     float2 *kc = nullptr, *mc = nullptr, *kr = nullptr;   // double-float K and M per slot
     float *gv32 = nullptr, *tv32 = nullptr;      // values of G and G^T (+-1/2, exact in FP32)
@@ -57,8 +79,21 @@ struct Survey {
     void release();
 };
 
+// whether SpMV variant v can run on this survey: the tiled ones need their
+// tiles to fit shared memory, the row-per-thread ones a two-system batch
+inline bool spmv_variant_available(const Survey &V, int v)
+{
+    if (v == 0 || v == 1) return V.ntiles > 0;
+    if (v == 2 || v == 4 || v == 8) return true;
+    if (v == kRowVariant + 2 || v == kRowVariant + 4) return V.SP == 2;
+    if (v == kMatFree) return V.mf.on;
+    return false;
+}
+
+// a: the assembly (host mesh copies) when the survey is built from one: on a
+// tensor mesh it enables the matrix-free SpMV variant
 int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const double *omega,
-                 Survey &V, cudaStream_t st);
+                 Survey &V, cudaStream_t st, const mtgpu_assembly_s *a = nullptr);
 // b, x: system-major FP64 [S][nb] complex; x is the initial guess in and the
 // solution out.  verify: continue until the true residual is below eps too.
 int survey_solve(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, double eps,

@@ -20,6 +20,9 @@ import numpy as np
 from . import _lib
 
 
+SPMV_VARIANTS = (0, 1, 2, 4, 8, 18, 20, 32)   # include/mtgpu.h, mtgpu_survey_tuning
+
+
 class Survey:
     def __init__(self, assembly, nus, stream=None):
         """assembly: an Assembly; nus: frequency [Hz] of every system."""
@@ -53,16 +56,19 @@ class Survey:
 
     def tuning(self):
         """(chosen SpMV variant, {variant: ms per launch}) of the set-up
-        autotuning; variants 0 and 1 stage x in shared memory per tile."""
+        autotuning; variants 0 and 1 stage x in shared memory per tile,
+        18 and 20 (two systems) run one thread per row for both systems, 32
+        is the matrix-free SpMV of tensor meshes."""
         v = C.c_int()
-        ms = (C.c_float * 5)()
+        ms = (C.c_float * len(SPMV_VARIANTS))()
         _lib.check(_lib.lib().mtgpu_survey_tuning(self._h, C.byref(v), ms),
                    "mtgpu_survey_tuning")
-        return v.value, {c: ms[i] for i, c in enumerate((0, 1, 2, 4, 8)) if ms[i] > 0}
+        return v.value, {c: ms[i] for i, c in enumerate(SPMV_VARIANTS) if ms[i] > 0}
 
     def set_spmv_variant(self, variant):
         """Pin the SpMV variant (0 x and matrix staged, 1 x staged, 2, 4, 8
-        slots in flight) instead of the autotuned one."""
+        slots in flight, 18, 20 row per thread for two systems, 32
+        matrix-free) instead of the autotuned one."""
         _lib.check(_lib.lib().mtgpu_survey_set_spmv_variant(self._h, int(variant)),
                    "mtgpu_survey_set_spmv_variant")
 

@@ -96,12 +96,15 @@ def test_survey_iteration_limit(gpu):
     assert code == -3 and st["status"][0] == -3 and st["iterations"][0] == 6
 
 
-@pytest.mark.parametrize("name,S", [("c1", 4), ("small", 32)])
+@pytest.mark.parametrize("name,S", [("c1", 2), ("c1", 4), ("small", 32)])
 def test_spmv_variants_agree(gpu, name, S):
-    """Every SpMV variant (x staged in shared memory per tile, or gathered
-    with 2, 4, 8 slots in flight) sums the same products in the same order;
-    only the block grouping of the dot products differs with the launch
-    grid, so the solves agree to rounding."""
+    """Every SpMV variant (x staged in shared memory per tile, gathered with
+    2, 4, 8 slots in flight, or, for two systems, one thread per row for
+    both) sums the same products in the same order; only the block grouping
+    of the dot products differs with the launch grid, so the solves agree to
+    rounding.  The matrix-free variant (32, available on these tensor
+    meshes) computes the same operator in another order: its solves agree
+    to the same bounds."""
     torch = gpu
     w = workloads.make(name)
     freqs = np.logspace(-2, 2, S // 2)
@@ -114,7 +117,7 @@ def test_spmv_variants_agree(gpu, name, S):
           np.stack([t[2] for t in tabs]), b)
     sv = survey.Survey(A, nus)
     ref = None
-    for v in (0, 1, 2, 4, 8):
+    for v in (0, 1, 2, 4, 8, 32) + ((18, 20) if S == 2 else ()):
         sv.set_spmv_variant(v)
         x = torch.zeros_like(b)
         code, st = sv.solve(b, x, eps=1e-8, maxiter=20000, verify=True)
