@@ -700,25 +700,26 @@ struct MF {
 
 // edge of direction d leaving node (i, j, k): the node's first edge
 // rb + i (1 + [j < ny-1] + [k < nz-1]), then +x, +y, +z as present
-__device__ __forceinline__ long long mf_edge(const MF &M, int d, int i, int j, int k)
+// (32-bit: the set-up keeps edges x systems and faces x systems below 2^31)
+__device__ __forceinline__ int mf_edge(const MF &M, int d, int i, int j, int k)
 {
     const int ey = j < M.ny - 1, ex = i < M.nx - 1;
-    long long e = (long long)__ldg(M.rb + k * M.ny + j) + (long long)i * (1 + ey + (k < M.nz - 1));
+    int e = __ldg(M.rb + k * M.ny + j) + i * (1 + ey + (k < M.nz - 1));
     if (d >= 1) e += ex;
     if (d == 2) e += ey;
     return e;
 }
 
 // face of normal n at (i, j, k): line index along n, cell indices across
-__device__ __forceinline__ long long mf_face(const MF &M, int n, int i, int j, int k)
+__device__ __forceinline__ int mf_face(const MF &M, int n, int i, int j, int k)
 {
-    if (n == 0) return ((long long)k * (M.ny - 1) + j) * M.nx + i;
-    if (n == 1) return M.nfx + ((long long)k * M.ny + j) * (M.nx - 1) + i;
-    return M.nfx + M.nfy + ((long long)k * (M.ny - 1) + j) * (M.nx - 1) + i;
+    if (n == 0) return (k * (M.ny - 1) + j) * M.nx + i;
+    if (n == 1) return (int)M.nfx + (k * M.ny + j) * (M.nx - 1) + i;
+    return (int)(M.nfx + M.nfy) + (k * (M.ny - 1) + j) * (M.nx - 1) + i;
 }
 
 template <int SP>
-__device__ __forceinline__ dfc mf_x(const MF &M, const float4 *__restrict__ x, long long e, int k)
+__device__ __forceinline__ dfc mf_x(const MF &M, const float4 *__restrict__ x, int e, int k)
 {
     if (__ldg(M.bedge + e)) return dfc{df{0.f, 0.f}, df{0.f, 0.f}};
     return from4(__ldg(x + e * SP + k));
@@ -758,7 +759,7 @@ k_mf_faces(MF M, const float4 *__restrict__ x, const SysState *sys)
             j = (int)(q % (M.ny - 1));
             kk = (int)(q / (M.ny - 1));
         }
-        long long e0, e1, e2, e3;
+        int e0, e1, e2, e3;
         if (n == 0) {
             e0 = mf_edge(M, 1, i, j, kk);
             e1 = mf_edge(M, 2, i, j + 1, kk);
@@ -805,17 +806,18 @@ __device__ __forceinline__ dfc mf_row(const MF &M, long long e, int k, df om,
     const Pos p{(int)(c & 1023u), (int)((c >> 10) & 1023u), (int)((c >> 20) & 1023u)};
     const int t1 = d == 2 ? 0 : d + 1, t2 = d == 0 ? 2 : d - 1;
     const Pos u1 = unit(t1), u2 = unit(t2);
-    auto cell = [&](Pos q) { return ((long long)q.z * (M.ny - 1) + q.y) * (M.nx - 1) + q.x; };
+    auto cell = [&](Pos q) { return (q.z * (M.ny - 1) + q.y) * (M.nx - 1) + q.x; };
+    const int nc = (int)M.ncell;
     // weights of the 4 cells around the edge, offsets (a - 1, b - 1) along (t1, t2)
     df w1[2][2], w2[2][2], wm[2][2];
 #pragma unroll
     for (int a = 0; a < 2; a++)
 #pragma unroll
         for (int b = 0; b < 2; b++) {
-            const long long cc = cell(mv(mv(p, u1, a - 1), u2, b - 1));
-            w1[a][b] = d2f(__ldg(M.w + (long long)t1 * M.ncell + cc));
-            w2[a][b] = d2f(__ldg(M.w + (long long)t2 * M.ncell + cc));
-            wm[a][b] = d2f(__ldg(M.w + (long long)(3 + d) * M.ncell + cc));
+            const int cc = cell(mv(mv(p, u1, a - 1), u2, b - 1));
+            w1[a][b] = d2f(__ldg(M.w + t1 * nc + cc));
+            w2[a][b] = d2f(__ldg(M.w + t2 * nc + cc));
+            wm[a][b] = d2f(__ldg(M.w + (3 + d) * nc + cc));
         }
     acc kr, ki, mr, mi;
     // D^T F D: faces of normal t1 through the edge (t2 cells b - 1 = -1: +1,
@@ -840,31 +842,25 @@ __device__ __forceinline__ dfc mf_row(const MF &M, long long e, int k, df om,
             ki.mac(ca, fm.im); ki.mac(c0, f0.im); ki.mac(cb, fp.im);
         }
     }
-    // M: the 3 x 3 parallel edges around, each cell's 4 with multipliers
-    // 4 (this edge's position), 2 (one axis off), 1 (the diagonal)
-    dfc xv[3][3];
+    // M: the 3 x 3 parallel edges around (grid position (A, B), this edge at
+    // (1, 1)); edge (A, B) lies in the cells (a, b) with a in {A-1, A},
+    // b in {B-1, B}, each contributing its weight times 2 per axis on which
+    // A (B) is the edge's own position: coefficients 4 (w00+w01+w10+w11),
+    // 2 (pair sums) and 1 (corner cells)
+    const df s0_ = add(wm[0][0], wm[0][1]), s1_ = add(wm[1][0], wm[1][1]);
+    const df r0_ = add(wm[0][0], wm[1][0]), r1_ = add(wm[0][1], wm[1][1]);
+    const df cm[3][3] = {{wm[0][0], scale(s0_, 2.f), wm[0][1]},
+                         {scale(r0_, 2.f), scale(add(s0_, s1_), 4.f), scale(r1_, 2.f)},
+                         {wm[1][0], scale(s1_, 2.f), wm[1][1]}};
 #pragma unroll
     for (int a = 0; a < 3; a++)
 #pragma unroll
         for (int b = 0; b < 3; b++) {
             const Pos q = mv(mv(p, u1, a - 1), u2, b - 1);
-            xv[a][b] = mf_x<SP>(M, x, mf_edge(M, d, q.x, q.y, q.z), k);
+            const dfc xe = mf_x<SP>(M, x, mf_edge(M, d, q.x, q.y, q.z), k);
+            mr.mac(cm[a][b], xe.re);
+            mi.mac(cm[a][b], xe.im);
         }
-#pragma unroll
-    for (int a = 0; a < 2; a++)
-#pragma unroll
-        for (int b = 0; b < 2; b++)
-#pragma unroll
-            for (int a2 = 0; a2 < 2; a2++)
-#pragma unroll
-                for (int b2 = 0; b2 < 2; b2++) {
-                    // cell (a, b) holds offsets (a + a2 - 1, b + b2 - 1); this edge is at (1 - a, 1 - b)
-                    const float mult = (a2 == 1 - a ? 2.f : 1.f) * (b2 == 1 - b ? 2.f : 1.f);
-                    const df cw = scale(wm[a][b], mult);
-                    const dfc xe = xv[a + a2][b + b2];
-                    mr.mac(cw, xe.re);
-                    mi.mac(cw, xe.im);
-                }
     const df mxr = mr.get(), mxi = mi.get();
     kr.mac(neg(om), mxi);
     ki.mac(om, mxr);
@@ -1675,6 +1671,13 @@ int matfree_build(Survey &V, const mtgpu_assembly_s &a, int nsm)
             }
     const long long ncell = (long long)(nx - 1) * (ny - 1) * (nz - 1);
     if (ncell != P.kpar) return MTGPU_OK;
+    // 32-bit indexing in the kernels: edges, faces and weights times systems
+    const long long nfaces = (long long)nx * (ny - 1) * (nz - 1) +
+                             (long long)(nx - 1) * ny * (nz - 1) +
+                             (long long)(nx - 1) * (ny - 1) * nz;
+    if ((long long)P.nb * V.SP >= (1LL << 31) || 6 * ncell >= (1LL << 31) ||
+        nfaces * V.SP >= (1LL << 31))
+        return MTGPU_OK;
     for (int k = 0, c = 0; k < nz - 1; k++)
         for (int j = 0; j < ny - 1; j++)
             for (int i = 0; i < nx - 1; i++, c++) {
