@@ -59,7 +59,7 @@ void Survey::release()
 void MatFree::release()
 {
     dev_free(rb);
-    dev_free(code);
+    dev_free(pos);
     dev_free(w);
     dev_free(f);
     on = false;
@@ -691,8 +691,9 @@ k_spmv_r2(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restr
 struct MF {
     int nx, ny, nz;
     long long nfx, nfy, nfz, ncell;
+    int nex, ney;              // x- and y-edges: the first two segments of the row order
     const int *rb;
-    const unsigned *code;
+    const unsigned *pos;       // row (direction-major order) -> i | j << 10 | k << 20
     const float2 *w;
     const unsigned char *bedge;
     float4 *f;
@@ -787,60 +788,71 @@ k_mf_faces(MF M, const float4 *__restrict__ x, const SysState *sys)
 
 __device__ __forceinline__ df scale(df a, float s) { return df{a.h * s, a.l * s}; }   // s = +-1, 2, 4
 
-// one non-Dirichlet edge of direction d at lattice position p (p[d] the
-// cell index along d, the others line indices): (K + i omega M) s.
-// Positions are kept as three scalars moved along the unit steps of t1 and
-// t2 (no runtime-indexed arrays, which would live in local memory).
+// one non-Dirichlet edge of direction D at lattice position p (p[D] the
+// cell index along D, the others line indices): (K + i omega M) s.  D, and
+// with it the two transverse axes T1 = D+1, T2 = D+2 (mod 3), are compile-
+// time constants: the rows run direction by direction, so warps are uniform.
 struct Pos {
     int x, y, z;
 };
-__device__ __forceinline__ Pos mv(Pos p, Pos u, int o) { return Pos{p.x + o * u.x, p.y + o * u.y, p.z + o * u.z}; }
-__device__ __forceinline__ Pos unit(int a) { return Pos{a == 0, a == 1, a == 2}; }
-
-template <int SP>
-__device__ __forceinline__ dfc mf_row(const MF &M, long long e, int k, df om,
-                                      const float4 *__restrict__ x)
+template <int A>
+__device__ __forceinline__ Pos mv(Pos p, int o)
 {
-    const unsigned c = __ldg(M.code + e);
-    const int d = (int)(c >> 30);
-    const Pos p{(int)(c & 1023u), (int)((c >> 10) & 1023u), (int)((c >> 20) & 1023u)};
-    const int t1 = d == 2 ? 0 : d + 1, t2 = d == 0 ? 2 : d - 1;
-    const Pos u1 = unit(t1), u2 = unit(t2);
-    auto cell = [&](Pos q) { return (q.z * (M.ny - 1) + q.y) * (M.nx - 1) + q.x; };
+    return Pos{p.x + (A == 0 ? o : 0), p.y + (A == 1 ? o : 0), p.z + (A == 2 ? o : 0)};
+}
+template <int N>
+__device__ __forceinline__ int mf_face_n(const MF &M, Pos q)
+{
+    if (N == 0) return (q.z * (M.ny - 1) + q.y) * M.nx + q.x;
+    if (N == 1) return (int)M.nfx + (q.z * M.ny + q.y) * (M.nx - 1) + q.x;
+    return (int)(M.nfx + M.nfy) + (q.z * (M.ny - 1) + q.y) * (M.nx - 1) + q.x;
+}
+
+template <int SP, int D>
+__device__ __forceinline__ dfc mf_row(const MF &M, Pos p, int k, df om, const float4 *__restrict__ x)
+{
+    constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
     const int nc = (int)M.ncell;
-    // weights of the 4 cells around the edge, offsets (a - 1, b - 1) along (t1, t2)
+    auto cell = [&](Pos q) { return (q.z * (M.ny - 1) + q.y) * (M.nx - 1) + q.x; };
+    // weights of the 4 cells around the edge, offsets (a - 1, b - 1) along (T1, T2)
     df w1[2][2], w2[2][2], wm[2][2];
 #pragma unroll
     for (int a = 0; a < 2; a++)
 #pragma unroll
         for (int b = 0; b < 2; b++) {
-            const int cc = cell(mv(mv(p, u1, a - 1), u2, b - 1));
-            w1[a][b] = d2f(__ldg(M.w + t1 * nc + cc));
-            w2[a][b] = d2f(__ldg(M.w + t2 * nc + cc));
-            wm[a][b] = d2f(__ldg(M.w + (3 + d) * nc + cc));
+            const int cc = cell(mv<T2>(mv<T1>(p, a - 1), b - 1));
+            w1[a][b] = d2f(__ldg(M.w + T1 * nc + cc));
+            w2[a][b] = d2f(__ldg(M.w + T2 * nc + cc));
+            wm[a][b] = d2f(__ldg(M.w + (3 + D) * nc + cc));
         }
     acc kr, ki, mr, mi;
-    // D^T F D: faces of normal t1 through the edge (t2 cells b - 1 = -1: +1,
-    // 0: -1), then faces of normal t2 (t1 cells -1: -1, 0: +1); each face's
+    // D^T F D: faces of normal T1 through the edge (T2 cells b - 1 = -1: +1,
+    // 0: -1), then faces of normal T2 (T1 cells -1: -1, 0: +1); each face's
     // F row: wa (f_-1 + 2 f_0) + wb (2 f_0 + f_+1) over the cells before and
     // after it along the normal
 #pragma unroll
-    for (int nn = 0; nn < 2; nn++) {
-        const int n = nn == 0 ? t1 : t2;
-        const Pos un = nn == 0 ? u1 : u2, uo = nn == 0 ? u2 : u1;
+    for (int b = 0; b < 2; b++) {
+        const Pos q = mv<T2>(p, b - 1);
+        const float sg = b == 0 ? 1.f : -1.f;
+        const df wa = w1[0][b], wb = w1[1][b];
+        const dfc fm = from4(__ldg(M.f + mf_face_n<T1>(M, mv<T1>(q, -1)) * SP + k));
+        const dfc f0 = from4(__ldg(M.f + mf_face_n<T1>(M, q) * SP + k));
+        const dfc fp = from4(__ldg(M.f + mf_face_n<T1>(M, mv<T1>(q, 1)) * SP + k));
+        const df ca = scale(wa, sg), cb = scale(wb, sg), c0 = scale(add(wa, wb), 2.f * sg);
+        kr.mac(ca, fm.re); kr.mac(c0, f0.re); kr.mac(cb, fp.re);
+        ki.mac(ca, fm.im); ki.mac(c0, f0.im); ki.mac(cb, fp.im);
+    }
 #pragma unroll
-        for (int b = 0; b < 2; b++) {
-            const Pos q = mv(p, uo, b - 1);
-            const float sg = nn == 0 ? (b == 0 ? 1.f : -1.f) : (b == 0 ? -1.f : 1.f);
-            const df wa = nn == 0 ? w1[0][b] : w2[b][0], wb = nn == 0 ? w1[1][b] : w2[b][1];
-            const Pos qm = mv(q, un, -1), qp = mv(q, un, 1);
-            const dfc fm = from4(__ldg(M.f + mf_face(M, n, qm.x, qm.y, qm.z) * SP + k));
-            const dfc f0 = from4(__ldg(M.f + mf_face(M, n, q.x, q.y, q.z) * SP + k));
-            const dfc fp = from4(__ldg(M.f + mf_face(M, n, qp.x, qp.y, qp.z) * SP + k));
-            const df ca = scale(wa, sg), cb = scale(wb, sg), c0 = scale(add(wa, wb), 2.f * sg);
-            kr.mac(ca, fm.re); kr.mac(c0, f0.re); kr.mac(cb, fp.re);
-            ki.mac(ca, fm.im); ki.mac(c0, f0.im); ki.mac(cb, fp.im);
-        }
+    for (int a = 0; a < 2; a++) {
+        const Pos q = mv<T1>(p, a - 1);
+        const float sg = a == 0 ? -1.f : 1.f;
+        const df wa = w2[a][0], wb = w2[a][1];
+        const dfc fm = from4(__ldg(M.f + mf_face_n<T2>(M, mv<T2>(q, -1)) * SP + k));
+        const dfc f0 = from4(__ldg(M.f + mf_face_n<T2>(M, q) * SP + k));
+        const dfc fp = from4(__ldg(M.f + mf_face_n<T2>(M, mv<T2>(q, 1)) * SP + k));
+        const df ca = scale(wa, sg), cb = scale(wb, sg), c0 = scale(add(wa, wb), 2.f * sg);
+        kr.mac(ca, fm.re); kr.mac(c0, f0.re); kr.mac(cb, fp.re);
+        ki.mac(ca, fm.im); ki.mac(c0, f0.im); ki.mac(cb, fp.im);
     }
     // M: the 3 x 3 parallel edges around (grid position (A, B), this edge at
     // (1, 1)); edge (A, B) lies in the cells (a, b) with a in {A-1, A},
@@ -856,8 +868,8 @@ __device__ __forceinline__ dfc mf_row(const MF &M, long long e, int k, df om,
     for (int a = 0; a < 3; a++)
 #pragma unroll
         for (int b = 0; b < 3; b++) {
-            const Pos q = mv(mv(p, u1, a - 1), u2, b - 1);
-            const dfc xe = mf_x<SP>(M, x, mf_edge(M, d, q.x, q.y, q.z), k);
+            const Pos q = mv<T2>(mv<T1>(p, a - 1), b - 1);
+            const dfc xe = mf_x<SP>(M, x, mf_edge(M, D, q.x, q.y, q.z), k);
             mr.mac(cm[a][b], xe.re);
             mi.mac(cm[a][b], xe.im);
         }
@@ -883,9 +895,21 @@ k_mf_edges(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restr
     const int rpb = kB / SP;
     for (int row = blockIdx.x * rpb + threadIdx.x / SP; row < nb; row += gridDim.x * rpb) {
         if (!on) continue;
-        const long long i = (long long)row * SP + k;
+        const int d = row < M.nex ? 0 : (row < M.nex + M.ney ? 1 : 2);
+        const unsigned c = __ldg(M.pos + row);
+        const Pos p{(int)(c & 1023u), (int)((c >> 10) & 1023u), (int)((c >> 20) & 1023u)};
+        const int e = mf_edge(M, d, p.x, p.y, p.z);
+        const long long i = (long long)e * SP + k;
         const float4 sv4 = __ldg(s + i);
-        const dfc y = __ldg(M.bedge + row) ? from4(sv4) : mf_row<SP>(M, row, k, om, s);
+        dfc y;
+        if (__ldg(M.bedge + e))
+            y = from4(sv4);
+        else if (d == 0)
+            y = mf_row<SP, 0>(M, p, k, om, s);
+        else if (d == 1)
+            y = mf_row<SP, 1>(M, p, k, om, s);
+        else
+            y = mf_row<SP, 2>(M, p, k, om, s);
         tail.row(i, y, sv4, r, z, sm);
     }
     tail.finish<SP>(sys, partials, mode);
@@ -1395,7 +1419,8 @@ struct Impl {
     {
         const MatFree &F = V.mf;
         return MF{F.nx, F.ny, F.nz, F.nfx, F.nfy, F.nfz,
-                  (long long)(F.nx - 1) * (F.ny - 1) * (F.nz - 1), F.rb, F.code, F.w,
+                  (long long)(F.nx - 1) * (F.ny - 1) * (F.nz - 1),
+                  (F.nx - 1) * F.ny * F.nz, F.nx * (F.ny - 1) * F.nz, F.rb, F.pos, F.w,
                   V.P->d_bedge, F.f};
     }
     static void spmv(Survey &V, int mode)
@@ -1689,7 +1714,14 @@ int matfree_build(Survey &V, const mtgpu_assembly_s &a, int nsm)
             }
     // edges: node order, +x, +y, +z per node
     std::vector<int> rb((size_t)ny * nz);
-    std::vector<unsigned> code(P.nb);
+    // rows direction by direction: x-edges, y-edges, z-edges, each i fastest
+    std::vector<unsigned> pos;
+    pos.reserve(P.nb);
+    for (int d = 0; d < 3; d++)
+        for (int k = 0; k < nz - (d == 2); k++)
+            for (int j = 0; j < ny - (d == 1); j++)
+                for (int i = 0; i < nx - (d == 0); i++)
+                    pos.push_back((unsigned)i | ((unsigned)j << 10) | ((unsigned)k << 20));
     long long e = 0;
     for (int k = 0; k < nz; k++)
         for (int j = 0; j < ny; j++) {
@@ -1702,13 +1734,11 @@ int matfree_build(Survey &V, const mtgpu_assembly_s &a, int nsm)
                     if (!has[d]) continue;
                     if (e >= P.nb || a.edges[2 * e] != n || a.edges[2 * e + 1] != n + step[d])
                         return MTGPU_OK;
-                    code[e] = (unsigned)i | ((unsigned)j << 10) | ((unsigned)k << 20) |
-                              ((unsigned)d << 30);
                     e++;
                 }
             }
         }
-    if (e != P.nb) return MTGPU_OK;
+    if (e != P.nb || (long long)pos.size() != P.nb) return MTGPU_OK;
     // per-cell weights from the materials' mu and sigma
     std::vector<double> mu(P.n_materials), sig(P.n_materials);
     MTGPU_TRY(cudaMemcpyAsync(mu.data(), P.d_mu, sizeof(double) * P.n_materials,
@@ -1738,12 +1768,12 @@ int matfree_build(Survey &V, const mtgpu_assembly_s &a, int nsm)
     F.nfy = (long long)(nx - 1) * ny * (nz - 1);
     F.nfz = (long long)(nx - 1) * (ny - 1) * nz;
     int rc;
-    if ((rc = dev_alloc(&F.rb, rb.size())) || (rc = dev_alloc(&F.code, code.size())) ||
+    if ((rc = dev_alloc(&F.rb, rb.size())) || (rc = dev_alloc(&F.pos, pos.size())) ||
         (rc = dev_alloc(&F.w, w.size())) ||
         (rc = dev_alloc(&F.f, (size_t)(F.nfx + F.nfy + F.nfz) * V.SP)))
         return rc;
     MTGPU_TRY(cudaMemcpyAsync(F.rb, rb.data(), sizeof(int) * rb.size(), cudaMemcpyHostToDevice, V.st));
-    MTGPU_TRY(cudaMemcpyAsync(F.code, code.data(), sizeof(unsigned) * code.size(),
+    MTGPU_TRY(cudaMemcpyAsync(F.pos, pos.data(), sizeof(unsigned) * pos.size(),
                               cudaMemcpyHostToDevice, V.st));
     MTGPU_TRY(cudaMemcpyAsync(F.w, w.data(), sizeof(float2) * w.size(), cudaMemcpyHostToDevice, V.st));
     F.on = true;

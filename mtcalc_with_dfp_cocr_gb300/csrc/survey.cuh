@@ -35,7 +35,7 @@ struct MatFree {
     int nx = 0, ny = 0, nz = 0;      // lines per axis
     long long nfx = 0, nfy = 0, nfz = 0;
     int *rb = nullptr;               // [nz][ny] number of the first edge of node (0, j, k)
-    unsigned *code = nullptr;        // [nb] edge position i | j << 10 | k << 20 | direction << 30
+    unsigned *pos = nullptr;         // [nb] rows x-, y-, z-edges: i | j << 10 | k << 20
     float2 *w = nullptr;             // [6][cells] double-float wF/3 (x, y, z), wM/9 (x, y, z)
     float4 *f = nullptr;             // face circulations [faces][SP]
     double check = -1.0;             // set-up check: max |A_mf s - A s| / max |A s|
