@@ -13,12 +13,17 @@ continues until its true residual ||b - A x|| / ||b|| is below 1e-8.
 (Plain FP32 iterations do not converge on these systems: the air layer
 leaves the curl-curl null space regularised below FP32 resolution.)  `value` is seconds
 per solve (lower is better) from CUDA events on the solver's stream; the
-matrix is larger than L2, so no flush is needed between iterations.
+iteration's working set (twelve vectors of 58 MB plus the SpMV's matrix or
+face arrays) is several times L2, so no flush is needed between
+iterations.
 `plain_fp64` times the reference's FP64 algorithm on the GPU on the same
 systems.  `e2e` goes through the reference-facing C ABI
 (mtgpu_pcocr_2x2_folded_ex, double-float) with the SLAE in host memory:
 upload, set-up, solve and download of x every solve.  `roofline` is the
-batched FP32 SpMV against the measured HBM copy bandwidth.
+batched double-float SpMV, in the variant the set-up autotuning chose (on
+this tensor mesh the matrix-free one), against the measured HBM copy
+bandwidth.  The timed region is an NVTX range "timed" for ncu's
+--nvtx-include.
 
 Reference arm (--impl reference).  The reference's CPU algorithm (the
 oracle restatement of COCR_FP, all host threads) on a bounded sample of the
@@ -50,8 +55,10 @@ METRIC = "time/solve to rel-res 1e-8: batched mixed vs plain FP64 GPU; SpMV HBM 
 UNIT = "s/solve"
 WORKLOAD = "c2"
 # DRAM bytes of one launch of the batched SpMV on c2 (two lanes), from the
-# ncu capture summarised in profiles/spmv_batched_c2_s2.md
+# ncu captures summarised in profiles/spmv_batched_c2_s2.md (stored matrix)
+# and profiles/spmv_matfree_c2_s2.md (matrix-free: faces + edges kernels)
 SPMV_TRAFFIC_C2 = 957.0e6
+SPMV_MF_TRAFFIC_C2 = None
 
 
 def load_peaks():
@@ -247,8 +254,10 @@ def gpu_arm(args):
     for _ in range(args.warmup):
         step_batched()
     launches0 = _lib.kernel_launches()
+    torch.cuda.nvtx.range_push("timed")   # lets ncu capture the timed region alone
     with ClockSampler(local) as clk:
         ms = timed(step_batched, args.steps)
+    torch.cuda.nvtx.range_pop()
     launches = _lib.kernel_launches() - launches0
     ms_per_step = ms / args.steps
     value = whole_job_seconds_per_solve(ms, args.steps, S, world)
@@ -260,9 +269,11 @@ def gpu_arm(args):
     ms_plain = timed(step_plain, plain_steps)
     plain_value = (ms_plain / 1e3) / (plain_steps * S * world)
 
-    # roofline of the dominant kernel: the batched FP32 SpMV
+    # roofline of the dominant kernel: the batched double-float SpMV, in the
+    # variant the set-up autotuning chose
     peak, peak_kind = load_peaks()
     sv = survey.Survey(A, nus, stream)
+    variant = sv.tuning()[0]
     sv.spmv_timed(5)
     reps = 50
     spmv_ms = sv.spmv_timed(reps) / reps
@@ -271,7 +282,27 @@ def gpu_arm(args):
     nc, nr = inf["nnz_complex"], inf["nnz_real"]
     nslices = (nb + 31) // 32
     meta = nslices * (8 + 8 + 4 + 4)
-    spmv_bytes = nc * (4 + 8 + 8) + nr * (4 + 8) + meta + 2 * S * 16 * nb
+    SP = 1 << (S - 1).bit_length()
+    m_ = w.mesh
+    if variant == 32:
+        # matrix-free, z = A s alone: the faces kernel reads s and the
+        # Dirichlet flags and writes the face circulations; the edges kernel
+        # reads them, s, the flags, 6 double-float weights per cell and the
+        # row positions, and writes z
+        nx_, ny_, nz_ = m_.nx, m_.ny, m_.nz
+        nf = nx_ * (ny_ - 1) * (nz_ - 1) + (nx_ - 1) * ny_ * (nz_ - 1) + (nx_ - 1) * (ny_ - 1) * nz_
+        spmv_bytes = (2 * 16 * SP * nf + 3 * 16 * SP * nb + 2 * nb + 48 * m_.kpar + 4 * nb
+                      + 4 * ny_ * nz_)
+        spmv_kernel = "k_mf_faces + k_mf_edges (matrix-free double-float SpMV, S systems)"
+        traffic = SPMV_MF_TRAFFIC_C2 if WORKLOAD == "c2" else None
+        traffic_src = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_mf_faces<2> + "
+                       "k_mf_edges<2> on c2, profiles/spmv_matfree_c2_s2.md")
+    else:
+        spmv_bytes = nc * (4 + 8 + 8) + nr * (4 + 8) + meta + 2 * S * 16 * nb
+        spmv_kernel = f"k_spmv variant {variant} (batched double-float SELL-32 SpMV, S systems)"
+        traffic = SPMV_TRAFFIC_C2 if WORKLOAD == "c2" else None
+        traffic_src = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_spmv<2,4> on c2, "
+                       "profiles/spmv_batched_c2_s2.md")
     achieved = spmv_bytes / (spmv_ms * 1e-3) / 1e9
     # the FP64 SpMV of the plain path (bound by the FP64 pipe on GB300)
     ctx = A.cocr(nus[0], stream)
@@ -316,7 +347,7 @@ def gpu_arm(args):
         "config": {"workload": "c2: 96x96x64 cells, 1,812,736 edges, 0.1 Hz x 2 polarisations; "
                                "batched double-float COCR + folded preconditioner + MRS stop "
                                "rule, every system also to true rel-res < 1e-8",
-                   "systems_per_step": S, "nb": nb, "l2_flush": "none: matrix > L2 (0.6 GB FP32)",
+                   "systems_per_step": S, "nb": nb, "l2_flush": "none: the iteration's working set (12 double-float vectors of 58 MB, the SpMV's matrix or face arrays) exceeds L2 (129 MB)",
                    "iterations": {lab(f, a): it for (f, a), it in zip(systems, batched["iterations"])},
                    "true_rel_res": {lab(f, a): r for (f, a), r in zip(systems, batched["true_residual_rel"])},
                    "parallelism": f"replicas x{world}"},
@@ -324,13 +355,11 @@ def gpu_arm(args):
                        "iterations": {lab(f, a): v[0] for (f, a), v in info["plain"].items()},
                        "true_rel_res": {lab(f, a): v[1] for (f, a), v in info["plain"].items()},
                        "speedup_of_batched_double_float": plain_value / value},
-        "roofline": {"bound": "hbm", "kernel": "k_spmv<SP> (batched double-float SELL-32 SpMV, S systems)",
+        "roofline": {"bound": "hbm", "kernel": spmv_kernel, "spmv_variant": variant,
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": f"{peak_kind} hbm_gbs",
                      "bytes_per_launch": spmv_bytes, "ms_per_launch": spmv_ms,
-                     "traffic": SPMV_TRAFFIC_C2 if WORKLOAD == "c2" else None,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
-                                       "k_spmv<2,4> on c2, profiles/spmv_batched_c2_s2.md"},
+                     "traffic": traffic, "traffic_source": traffic_src},
         "roofline_fp64_spmv": {"bound": "fp64 pipe (GB300 FP64 = FP32/64)",
                                "achieved": achieved64, "peak": peak, "unit": "GB/s",
                                "frac": achieved64 / peak, "bytes_per_launch": spmv64_bytes,
