@@ -58,7 +58,7 @@ WORKLOAD = "c2"
 # ncu captures summarised in profiles/spmv_batched_c2_s2.md (stored matrix)
 # and profiles/spmv_matfree_c2_s2.md (matrix-free: faces + edges kernels)
 SPMV_TRAFFIC_C2 = 957.0e6
-SPMV_MF_TRAFFIC_C2 = None
+SPMV_MF_TRAFFIC_C2 = 517.9e6
 
 
 def load_peaks():

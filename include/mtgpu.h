@@ -276,6 +276,10 @@ int mtgpu_survey_spmv_timed(mtgpu_survey *s, int reps, float *ms);
  * and the times (ms per launch) it measured for the variants 0, 1, 2, 4, 8,
  * 18, 20, 32 (ms[8]; 0 where a variant was not available). */
 int mtgpu_survey_tuning(const mtgpu_survey *s, int *variant, float *ms);
+/* The environment variable MTGPU_SPMV_VARIANT, when it names a variant
+ * available for the survey, replaces the autotuning at mtgpu_survey_create
+ * (for profiler runs: a profiler serialises and cold-starts every launch, and
+ * would make the autotuning choose differently from a plain run). */
 
 /* Pins the SpMV variant (0, 1, 2, 4, 8, 18, 20 or 32) instead of the
  * autotuned choice.  The stored-matrix variants sum the same products in the

@@ -30,6 +30,8 @@
 
 #include <algorithm>
 #include <climits>
+#include <cstdlib>
+#include <cstring>
 
 namespace mtgpu {
 
@@ -1902,8 +1904,15 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
     note_launches(8);
     if ((rc = build_tiles(V, nsm))) return rc;
     if (a && (rc = matfree_build(V, *a, nsm))) return rc;
-    // autotune the SpMV variant: time each candidate, keep the fastest
-    {
+    // autotune the SpMV variant: time each candidate, keep the fastest.
+    // MTGPU_SPMV_VARIANT (environment) pins an available variant instead:
+    // runs under a profiler, which serialises and cold-starts every launch,
+    // would otherwise tune to other variants than plain runs do
+    const char *pin = getenv("MTGPU_SPMV_VARIANT");
+    if (pin && *pin && spmv_variant_available(V, atoi(pin))) {
+        V.ch = atoi(pin);
+        MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+    } else {
         const int cand[kSpmvVariants] = {0, 1, 2, 4, 8, kRowVariant + 2, kRowVariant + 4, kMatFree};
         float best = 1e30f;
         int best_ch = 4;
