@@ -272,23 +272,25 @@ int mtgpu_survey_spmv_timed(mtgpu_survey *s, int reps, float *ms);
  * 18, 20: two-system batches only, one thread per row for both systems with
  * 2 or 4 slots in flight; 32: matrix-free, tensor meshes only: the curl-curl
  * part as D^T F D (edge -> face circulations, face mass matrix) and the mass
- * part regenerated from six weights per cell instead of the stored matrix)
- * and the times (ms per launch) it measured for the variants 0, 1, 2, 4, 8,
- * 18, 20, 32 (ms[8]; 0 where a variant was not available). */
+ * part regenerated from six weights per cell instead of the stored matrix;
+ * 33: the same with two systems per thread, batches of 2 or more) and the
+ * times (ms per launch) it measured for the variants 0, 1, 2, 4, 8, 18, 20,
+ * 32, 33 (ms[9]; 0 where a variant was not available). */
 int mtgpu_survey_tuning(const mtgpu_survey *s, int *variant, float *ms);
 /* The environment variable MTGPU_SPMV_VARIANT, when it names a variant
  * available for the survey, replaces the autotuning at mtgpu_survey_create
  * (for profiler runs: a profiler serialises and cold-starts every launch, and
  * would make the autotuning choose differently from a plain run). */
 
-/* Pins the SpMV variant (0, 1, 2, 4, 8, 18, 20 or 32) instead of the
+/* Pins the SpMV variant (0, 1, 2, 4, 8, 18, 20, 32 or 33) instead of the
  * autotuned choice.  The stored-matrix variants sum the same products in the
  * same order; the matrix-free one computes the same operator in another
  * order (it is enabled only where a set-up product agrees with the stored
  * matrix's to 1e-9).  MTGPU_ERR_ARG if the variant is unknown or unavailable
  * for this survey (0 and 1 need their tiles to fit shared memory, 18 and 20
  * two systems, 32 a survey created from an assembly of a tensor mesh with
- * RegularMeshBuilder's numbering and all outer nodes Dirichlet). */
+ * RegularMeshBuilder's numbering and all outer nodes Dirichlet, 33 that and
+ * at least two systems). */
 int mtgpu_survey_set_spmv_variant(mtgpu_survey *s, int variant);
 
 void mtgpu_survey_destroy(mtgpu_survey *s);

@@ -881,6 +881,152 @@ __device__ __forceinline__ dfc mf_row(const MF &M, Pos p, int k, df om, const fl
     return dfc{kr.get(), ki.get()};
 }
 
+// The same row for two systems (k0, k0 + 1) at once: the index arithmetic,
+// the weights and their combinations are shared; the adjacent systems'
+// values are one contiguous 32-byte pair.
+template <int SP, int D>
+__device__ __forceinline__ void mf_row2(const MF &M, Pos p, int k0, const df (&om)[2],
+                                        const float4 *__restrict__ x, dfc (&y)[2])
+{
+    constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
+    const int nc = (int)M.ncell;
+    auto cell = [&](Pos q) { return (q.z * (M.ny - 1) + q.y) * (M.nx - 1) + q.x; };
+    df w1[2][2], w2[2][2], wm[2][2];
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 2; b++) {
+            const int cc = cell(mv<T2>(mv<T1>(p, a - 1), b - 1));
+            w1[a][b] = d2f(__ldg(M.w + T1 * nc + cc));
+            w2[a][b] = d2f(__ldg(M.w + T2 * nc + cc));
+            wm[a][b] = d2f(__ldg(M.w + (3 + D) * nc + cc));
+        }
+    acc kr[2], ki[2], mr[2], mi[2];
+#pragma unroll
+    for (int nn = 0; nn < 2; nn++)
+#pragma unroll
+        for (int b = 0; b < 2; b++) {
+            Pos q;
+            df wa, wb;
+            float sg;
+            int im, i0, ip;
+            if (nn == 0) {
+                q = mv<T2>(p, b - 1);
+                sg = b == 0 ? 1.f : -1.f;
+                wa = w1[0][b];
+                wb = w1[1][b];
+                im = mf_face_n<T1>(M, mv<T1>(q, -1));
+                i0 = mf_face_n<T1>(M, q);
+                ip = mf_face_n<T1>(M, mv<T1>(q, 1));
+            } else {
+                q = mv<T1>(p, b - 1);
+                sg = b == 0 ? -1.f : 1.f;
+                wa = w2[b][0];
+                wb = w2[b][1];
+                im = mf_face_n<T2>(M, mv<T2>(q, -1));
+                i0 = mf_face_n<T2>(M, q);
+                ip = mf_face_n<T2>(M, mv<T2>(q, 1));
+            }
+            const df ca = scale(wa, sg), cb = scale(wb, sg), c0 = scale(add(wa, wb), 2.f * sg);
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const dfc fm = from4(__ldg(M.f + im * SP + k0 + u));
+                const dfc f0 = from4(__ldg(M.f + i0 * SP + k0 + u));
+                const dfc fp = from4(__ldg(M.f + ip * SP + k0 + u));
+                kr[u].mac(ca, fm.re); kr[u].mac(c0, f0.re); kr[u].mac(cb, fp.re);
+                ki[u].mac(ca, fm.im); ki[u].mac(c0, f0.im); ki[u].mac(cb, fp.im);
+            }
+        }
+    const df s0_ = add(wm[0][0], wm[0][1]), s1_ = add(wm[1][0], wm[1][1]);
+    const df r0_ = add(wm[0][0], wm[1][0]), r1_ = add(wm[0][1], wm[1][1]);
+    const df cm[3][3] = {{wm[0][0], scale(s0_, 2.f), wm[0][1]},
+                         {scale(r0_, 2.f), scale(add(s0_, s1_), 4.f), scale(r1_, 2.f)},
+                         {wm[1][0], scale(s1_, 2.f), wm[1][1]}};
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            const Pos q = mv<T2>(mv<T1>(p, a - 1), b - 1);
+            const int e = mf_edge(M, D, q.x, q.y, q.z);
+            if (__ldg(M.bedge + e)) continue;
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const dfc xe = from4(__ldg(x + e * SP + k0 + u));
+                mr[u].mac(cm[a][b], xe.re);
+                mi[u].mac(cm[a][b], xe.im);
+            }
+        }
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+        const df mxr = mr[u].get(), mxi = mi[u].get();
+        kr[u].mac(neg(om[u]), mxi);
+        ki[u].mac(om[u], mxr);
+        y[u] = dfc{kr[u].get(), ki[u].get()};
+    }
+}
+
+// The matrix-free SpMV with two systems per thread (variant 33, SP >= 2):
+// SP / 2 threads per edge.  Partial sums are staged per system in shared
+// memory so that the grid reduction sees lane l carrying system l % SP.
+template <int SP>
+__global__ void __launch_bounds__(kB, 2)
+k_mf_edges2(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restrict__ s,
+            const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
+            SysState *sys, double *partials, int mode)
+{
+    constexpr int H = SP / 2;
+    const int k0 = 2 * (threadIdx.x % H);
+    bool on[2];
+    df om[2];
+    SpmvTail tail[2];
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+        on[u] = sys[k0 + u].status == kRun;
+        om[u] = d2f(omega[k0 + u]);
+        tail[u].mm = mode ? sys[k0 + u].mrs_mode : 0;
+        tail[u].wm = from_double(sys[k0 + u].mrs_w);
+    }
+    const int rpb = kB / H;
+    if (on[0] || on[1]) {
+        for (int row = blockIdx.x * rpb + threadIdx.x / H; row < nb; row += gridDim.x * rpb) {
+            const int d = row < M.nex ? 0 : (row < M.nex + M.ney ? 1 : 2);
+            const unsigned c = __ldg(M.pos + row);
+            const Pos p{(int)(c & 1023u), (int)((c >> 10) & 1023u), (int)((c >> 20) & 1023u)};
+            const int e = mf_edge(M, d, p.x, p.y, p.z);
+            const long long i = (long long)e * SP + k0;
+            const float4 sv[2] = {__ldg(s + i), __ldg(s + i + 1)};
+            dfc y[2];
+            if (__ldg(M.bedge + e)) {
+                y[0] = from4(sv[0]);
+                y[1] = from4(sv[1]);
+            } else if (d == 0) {
+                mf_row2<SP, 0>(M, p, k0, om, s, y);
+            } else if (d == 1) {
+                mf_row2<SP, 1>(M, p, k0, om, s, y);
+            } else {
+                mf_row2<SP, 2>(M, p, k0, om, s, y);
+            }
+#pragma unroll
+            for (int u = 0; u < 2; u++)
+                if (on[u]) tail[u].row(i + u, y[u], sv[u], r, z, sm);
+        }
+    }
+    __shared__ double stage[3][SP];
+    for (int t = threadIdx.x; t < 3 * SP; t += kB) (&stage[0][0])[t] = 0.0;
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+        atomicAdd(&stage[0][k0 + u], tail[u].zsr.to_double());
+        atomicAdd(&stage[1][k0 + u], tail[u].zsi.to_double());
+        atomicAdd(&stage[2][k0 + u], tail[u].nn.to_double());
+    }
+    __syncthreads();
+    double v[3] = {0.0, 0.0, 0.0};
+    if (threadIdx.x < SP)
+        for (int n = 0; n < 3; n++) v[n] = stage[n][threadIdx.x];
+    SpmvTail::finish_v<SP>(v, sys, partials, mode);
+}
+
 // z = A s by the matrix-free operator, with the SpMV tail of k_spmv
 template <int SP>
 __global__ void __launch_bounds__(kB, 2)
@@ -1428,9 +1574,16 @@ struct Impl {
     static void spmv(Survey &V, int mode)
     {
         const Mat A = mat(V);
-        if (V.ch == kMatFree) {
+        if (V.ch == kMatFree || V.ch == kMatFree + 1) {
             const MF M = mfd(V);
             k_mf_faces<SP><<<V.g_mff, kB, 0, V.st>>>(M, V.s, V.sys);
+            if constexpr (SP >= 2) {
+                if (V.ch == kMatFree + 1) {
+                    k_mf_edges2<SP><<<V.g_mfe, kB, 0, V.st>>>(V.nb, M, V.omega, V.s, V.r, V.z,
+                                                              V.sm, V.sys, V.partials, mode);
+                    return;
+                }
+            }
             k_mf_edges<SP><<<V.g_mfe, kB, 0, V.st>>>(V.nb, M, V.omega, V.s, V.r, V.z, V.sm, V.sys,
                                                     V.partials, mode);
             return;
@@ -1527,6 +1680,11 @@ struct Impl {
             V.g_mff = g((const void *)k_mf_faces<SP>, (int)std::min<long long>(
                                                           (nf + kB / SP - 1) / (kB / SP), INT_MAX));
             V.g_mfe = g((const void *)k_mf_edges<SP>, V.grid_rows);
+            if constexpr (SP >= 2) {
+                if (V.ch == kMatFree + 1)
+                    V.g_mfe = g((const void *)k_mf_edges2<SP>,
+                                (V.nb + 2 * kB / SP - 1) / (2 * kB / SP));
+            }
         }
         if constexpr (SP == 2) {
             if (V.ch == kRowVariant + 2 || V.ch == kRowVariant + 4) {
@@ -1913,7 +2071,8 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
         V.ch = atoi(pin);
         MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
     } else {
-        const int cand[kSpmvVariants] = {0, 1, 2, 4, 8, kRowVariant + 2, kRowVariant + 4, kMatFree};
+        const int cand[kSpmvVariants] = {0, 1, 2, 4, 8, kRowVariant + 2, kRowVariant + 4, kMatFree,
+                                         kMatFree + 1};
         float best = 1e30f;
         int best_ch = 4;
         for (int c = 0; c < kSpmvVariants; c++) {
@@ -2066,7 +2225,7 @@ int survey_solve(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, do
         MTGPU_TRY(e);
         V.graph_iters = iters_per_launch;
     }
-    const unsigned long long kpi = (V.G.m > 0 ? 4 : 3) + (V.ch == kMatFree ? 1 : 0);
+    const unsigned long long kpi = (V.G.m > 0 ? 4 : 3) + (V.ch >= kMatFree ? 1 : 0);
     long long guard = 0;
     const long long guard_max =
         (long long)maxiter + (long long)(kMaxContinue + 1) * 4 * iters_per_launch + 64;

@@ -24,8 +24,8 @@ struct SysState {
 };
 
 constexpr int kRowVariant = 16;    // + slots in flight: one thread per row, both systems
-constexpr int kMatFree = 32;       // matrix-free SpMV on tensor meshes
-constexpr int kSpmvVariants = 8;   // 0, 1, 2, 4, 8, 18, 20, 32
+constexpr int kMatFree = 32;       // matrix-free SpMV on tensor meshes (+1: two systems per thread)
+constexpr int kSpmvVariants = 9;   // 0, 1, 2, 4, 8, 18, 20, 32, 33
 
 // Matrix-free SpMV of a tensor (RegularMeshBuilder) mesh: K = D^T F D with D
 // the edge -> face circulations and F the face mass matrix, M the edge mass
@@ -56,7 +56,7 @@ struct Survey {
     int tile_T = 1, ntiles = 0, tile_smem = 0, tile_smem_x = 0, g_spmv_t = 0, g_spmv_tx = 0;
     int *uoff = nullptr, *ucol = nullptr;
     unsigned short *lc = nullptr, *lr = nullptr;
-    float tune_ms[kSpmvVariants] = {};   // SpMV times of the variants 0, 1, 2, 4, 8, 18, 20, 32
+    float tune_ms[kSpmvVariants] = {};   // SpMV times of the variants 0, 1, 2, 4, 8, 18, 20, 32, 33
     MatFree mf;
     int g_mff = 0, g_mfe = 0;                    // matrix-free launch grids (faces, edges)
     Folded G;                                    // pattern of G and G^T
@@ -87,6 +87,7 @@ inline bool spmv_variant_available(const Survey &V, int v)
     if (v == 2 || v == 4 || v == 8) return true;
     if (v == kRowVariant + 2 || v == kRowVariant + 4) return V.SP == 2;
     if (v == kMatFree) return V.mf.on;
+    if (v == kMatFree + 1) return V.mf.on && V.SP >= 2;
     return false;
 }
 

@@ -20,7 +20,7 @@ import numpy as np
 from . import _lib
 
 
-SPMV_VARIANTS = (0, 1, 2, 4, 8, 18, 20, 32)   # include/mtgpu.h, mtgpu_survey_tuning
+SPMV_VARIANTS = (0, 1, 2, 4, 8, 18, 20, 32, 33)   # include/mtgpu.h, mtgpu_survey_tuning
 
 
 class Survey:
@@ -58,7 +58,8 @@ class Survey:
         """(chosen SpMV variant, {variant: ms per launch}) of the set-up
         autotuning; variants 0 and 1 stage x in shared memory per tile,
         18 and 20 (two systems) run one thread per row for both systems, 32
-        is the matrix-free SpMV of tensor meshes."""
+        is the matrix-free SpMV of tensor meshes, 33 the same with two
+        systems per thread."""
         v = C.c_int()
         ms = (C.c_float * len(SPMV_VARIANTS))()
         _lib.check(_lib.lib().mtgpu_survey_tuning(self._h, C.byref(v), ms),
@@ -67,7 +68,7 @@ class Survey:
 
     def set_spmv_variant(self, variant):
         """Pin the SpMV variant (0 x and matrix staged, 1 x staged, 2, 4, 8
-        slots in flight, 18, 20 row per thread for two systems, 32
+        slots in flight, 18, 20 row per thread for two systems, 32, 33
         matrix-free) instead of the autotuned one."""
         _lib.check(_lib.lib().mtgpu_survey_set_spmv_variant(self._h, int(variant)),
                    "mtgpu_survey_set_spmv_variant")
