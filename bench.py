@@ -54,11 +54,10 @@ sys.path.insert(0, ROOT)
 METRIC = "time/solve to rel-res 1e-8: batched mixed vs plain FP64 GPU; SpMV HBM GB/s"
 UNIT = "s/solve"
 WORKLOAD = "c2"
-# DRAM bytes of one launch of the batched SpMV on c2 (two lanes), from the
-# ncu captures summarised in profiles/spmv_batched_c2_s2.md (stored matrix)
-# and profiles/spmv_matfree_c2_s2.md (matrix-free: faces + edges kernels)
-SPMV_TRAFFIC_C2 = 957.0e6
-SPMV_MF_TRAFFIC_C2 = 517.9e6
+# DRAM bytes of one launch of the matrix-free SpMV pair on c2 (two lanes,
+# with the MRS tail as the iteration launches it), from the ncu capture
+# summarised in profiles/spmv_matfree_c2_s2.md
+SPMV_MF_TRAFFIC_C2 = None
 
 
 def load_peaks():
@@ -284,25 +283,29 @@ def gpu_arm(args):
     meta = nslices * (8 + 8 + 4 + 4)
     SP = 1 << (S - 1).bit_length()
     m_ = w.mesh
-    if variant == 32:
-        # matrix-free, z = A s alone: the faces kernel reads s and the
-        # Dirichlet flags and writes the face circulations; the edges kernel
-        # reads them, s, the flags, 6 double-float weights per cell and the
-        # row positions, and writes z
+    # as the iteration launches it: z = A s plus the MRS tail (r read, s_m
+    # read and written)
+    tail = 3 * 16 * SP * nb
+    if variant in (32, 33):
+        # matrix-free: the faces kernel reads s and the Dirichlet flags and
+        # writes the face circulations; the edges kernel reads them, s, the
+        # flags, 6 double-float weights per cell and the row positions, and
+        # writes z
         nx_, ny_, nz_ = m_.nx, m_.ny, m_.nz
         nf = nx_ * (ny_ - 1) * (nz_ - 1) + (nx_ - 1) * ny_ * (nz_ - 1) + (nx_ - 1) * (ny_ - 1) * nz_
         spmv_bytes = (2 * 16 * SP * nf + 3 * 16 * SP * nb + 2 * nb + 48 * m_.kpar + 4 * nb
-                      + 4 * ny_ * nz_)
-        spmv_kernel = "k_mf_faces + k_mf_edges (matrix-free double-float SpMV, S systems)"
+                      + 4 * ny_ * nz_ + tail)
+        edges = "k_mf_edges2" if variant == 33 else "k_mf_edges"
+        spmv_kernel = f"k_mf_faces + {edges} (matrix-free double-float SpMV + MRS tail, S systems)"
         traffic = SPMV_MF_TRAFFIC_C2 if WORKLOAD == "c2" else None
-        traffic_src = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_mf_faces<2> + "
-                       "k_mf_edges<2> on c2, profiles/spmv_matfree_c2_s2.md")
+        traffic_src = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of k_mf_faces<2> + "
+                       f"{edges}<2> on c2, profiles/spmv_matfree_c2_s2.md")
     else:
-        spmv_bytes = nc * (4 + 8 + 8) + nr * (4 + 8) + meta + 2 * S * 16 * nb
-        spmv_kernel = f"k_spmv variant {variant} (batched double-float SELL-32 SpMV, S systems)"
-        traffic = SPMV_TRAFFIC_C2 if WORKLOAD == "c2" else None
-        traffic_src = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_spmv<2,4> on c2, "
-                       "profiles/spmv_batched_c2_s2.md")
+        spmv_bytes = nc * (4 + 8 + 8) + nr * (4 + 8) + meta + 2 * S * 16 * nb + tail
+        spmv_kernel = (f"k_spmv variant {variant} (batched double-float SELL-32 SpMV + MRS "
+                       f"tail, S systems)")
+        traffic = None
+        traffic_src = None
     achieved = spmv_bytes / (spmv_ms * 1e-3) / 1e9
     # the FP64 SpMV of the plain path (bound by the FP64 pipe on GB300)
     ctx = A.cocr(nus[0], stream)

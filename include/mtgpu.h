@@ -262,8 +262,10 @@ int mtgpu_survey_create(mtgpu_assembly *a, int S, const double *nu, void *stream
 int mtgpu_survey_solve(mtgpu_survey *s, const double *d_b, double *d_x, double eps, int maxiter,
                        int verify, mtgpu_survey_stats *stats);
 
-/* Time `reps` launches of the batched double-float SpMV (all systems) with
- * CUDA events on the survey's stream; *ms receives the total. */
+/* Time `reps` launches of the batched double-float SpMV (all systems) as the
+ * iteration launches it (z = A s with the MRS tail: r read, s_m read and
+ * written), with CUDA events on the survey's stream; *ms receives the total.
+ * It overwrites the survey's work vectors; a solve re-initialises them. */
 int mtgpu_survey_spmv_timed(mtgpu_survey *s, int reps, float *ms);
 
 /* The SpMV variant the set-up autotuning chose (0: x segments and matrix
@@ -274,8 +276,10 @@ int mtgpu_survey_spmv_timed(mtgpu_survey *s, int reps, float *ms);
  * part as D^T F D (edge -> face circulations, face mass matrix) and the mass
  * part regenerated from six weights per cell instead of the stored matrix;
  * 33: the same with two systems per thread, batches of 2 or more) and the
- * times (ms per launch) it measured for the variants 0, 1, 2, 4, 8, 18, 20,
- * 32, 33 (ms[9]; 0 where a variant was not available). */
+ * times it measured for the variants 0, 1, 2, 4, 8, 18, 20, 32, 33 (ms[9]: ms
+ * per whole iteration with that variant, so that each SpMV sees the cache as
+ * the other kernels of an iteration leave it; 0 where a variant was not
+ * available). */
 int mtgpu_survey_tuning(const mtgpu_survey *s, int *variant, float *ms);
 /* The environment variable MTGPU_SPMV_VARIANT, when it names a variant
  * available for the survey, replaces the autotuning at mtgpu_survey_create

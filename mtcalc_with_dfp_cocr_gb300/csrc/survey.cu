@@ -2080,8 +2080,8 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
             V.ch = cand[c];
             MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
             float ms = 0.f;
-            if ((rc = survey_spmv_timed(V, 1, &ms))) return rc;   // warm-up
-            if ((rc = survey_spmv_timed(V, 3, &ms))) return rc;
+            if ((rc = survey_iter_timed(V, 1, &ms))) return rc;   // warm-up
+            if ((rc = survey_iter_timed(V, 3, &ms))) return rc;
             V.tune_ms[c] = ms / 3.f;
             if (ms < best) {
                 best = ms;
@@ -2107,23 +2107,78 @@ int survey_set_variant(Survey &V, int variant)
     return MTGPU_OK;
 }
 
+// Times the SpMV as the iteration launches it: mode 1 with the MRS tail
+// (r read, s_m read and written), every system running.  The state set here
+// (no stop threshold, no iteration limit) keeps all systems running across
+// the launches; a solve re-initialises the state and the vectors it touches.
 int survey_spmv_timed(Survey &V, int reps, float *ms)
 {
     std::vector<SysState> init(32);
     for (int k = 0; k < 32; k++) {
         SysState s{};
         s.status = k < V.S ? kRun : MTGPU_OK;
-        s.maxiter = 1;
+        s.maxiter = INT_MAX;
+        s.eps_k = -1.0;
+        s.r_old = 1.0;
+        s.mrs_mode = 2;
+        s.mrs_w = 0.5;
         init[k] = s;
     }
     MTGPU_TRY(cudaMemcpyAsync(V.sys, init.data(), sizeof(SysState) * 32, cudaMemcpyHostToDevice, V.st));
-    MTGPU_TRY(cudaMemsetAsync(V.s, 0, sizeof(float4) * (size_t)V.nb * V.SP, V.st));
+    const size_t nv = sizeof(float4) * (size_t)V.nb * V.SP;
+    MTGPU_TRY(cudaMemsetAsync(V.s, 0, nv, V.st));
+    MTGPU_TRY(cudaMemsetAsync(V.r, 0, nv, V.st));
+    MTGPU_TRY(cudaMemsetAsync(V.sm, 0, nv, V.st));
     cudaEvent_t e0, e1;
     MTGPU_TRY(cudaEventCreate(&e0));
     MTGPU_TRY(cudaEventCreate(&e1));
     MTGPU_TRY(cudaEventRecord(e0, V.st));
-    for (int q = 0; q < reps; q++) MTGPU_SP_DISPATCH(V.SP, spmv_only(V));
+    for (int q = 0; q < reps; q++) MTGPU_SP_DISPATCH(V.SP, spmv(V, 1));
     note_launches((unsigned long long)reps);
+    MTGPU_TRY(cudaEventRecord(e1, V.st));
+    MTGPU_TRY(cudaEventSynchronize(e1));
+    MTGPU_TRY(cudaEventElapsedTime(ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    MTGPU_TRY(cudaGetLastError());
+    return MTGPU_OK;
+}
+
+// Times `reps` whole iterations (node, edge and update kernels, SpMV) on
+// pattern-filled vectors with every system running: the autotuning ranks
+// the SpMV variants by these, since the kernels before the SpMV leave the
+// cache as it finds it inside a solve.  The values go to NaN within a few
+// iterations, which changes neither the work nor its speed; no state
+// reaches a stop (no threshold, no iteration limit, and the breakdown test
+// of (a, w) does not fire on NaN).  A solve re-initialises everything.
+int survey_iter_timed(Survey &V, int reps, float *ms)
+{
+    std::vector<SysState> init(32);
+    for (int k = 0; k < 32; k++) {
+        SysState s{};
+        s.status = k < V.S ? kRun : MTGPU_OK;
+        s.maxiter = INT_MAX;
+        s.eps_k = -1.0;
+        s.r_old = 1.0;
+        s.mrs_mode = 2;
+        s.mrs_w = 0.5;
+        s.zs = make_double2(1.0, 0.0);
+        s.alpha = make_double2(1e-3, 0.0);
+        s.beta = make_double2(0.5, 0.0);
+        init[k] = s;
+    }
+    MTGPU_TRY(cudaMemcpyAsync(V.sys, init.data(), sizeof(SysState) * 32, cudaMemcpyHostToDevice, V.st));
+    const long long nv = (long long)V.nb * V.SP;
+    for (float4 *v : {V.x, V.r, V.s, V.p, V.a, V.z, V.w, V.sm})
+        k_pattern<<<1024, kB, 0, V.st>>>(nv, v);
+    if (V.G.m > 0) k_pattern<<<1024, kB, 0, V.st>>>((long long)V.G.m * V.SP, V.h);
+    note_launches(V.G.m > 0 ? 9 : 8);
+    cudaEvent_t e0, e1;
+    MTGPU_TRY(cudaEventCreate(&e0));
+    MTGPU_TRY(cudaEventCreate(&e1));
+    MTGPU_TRY(cudaEventRecord(e0, V.st));
+    for (int q = 0; q < reps; q++) MTGPU_SP_DISPATCH(V.SP, iteration(V));
+    note_launches((unsigned long long)reps * ((V.G.m > 0 ? 4 : 3) + (V.ch >= kMatFree ? 1 : 0)));
     MTGPU_TRY(cudaEventRecord(e1, V.st));
     MTGPU_TRY(cudaEventSynchronize(e1));
     MTGPU_TRY(cudaEventElapsedTime(ms, e0, e1));
