@@ -57,7 +57,7 @@ WORKLOAD = "c2"
 # DRAM bytes of one launch of the matrix-free SpMV pair on c2 (two lanes,
 # with the MRS tail as the iteration launches it), from the ncu capture
 # summarised in profiles/spmv_matfree_c2_s2.md
-SPMV_MF_TRAFFIC_C2 = None
+SPMV_MF_TRAFFIC_C2 = 907.7e6
 
 
 def load_peaks():
