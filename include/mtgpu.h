@@ -64,6 +64,12 @@ typedef struct {
     double setup_seconds;      /* upload, format conversion, preconditioner   */
     double solve_seconds;      /* COCR iterations                             */
     int status;
+    int spmv_variant;          /* double-float path: the SpMV variant used
+                                  (see mtgpu_survey_tuning); -1 otherwise    */
+    double matfree_check;      /* double-float path: the matrix-free set-up
+                                  check max|A_mf s - A s| / max|A s| (the
+                                  variant is offered below 1e-9); -1 when the
+                                  mesh is not a tensor mesh or xyz is NULL   */
 } mtgpu_solve_stats;
 
 typedef struct {
@@ -80,7 +86,14 @@ typedef struct {
 } mtgpu_solve_opts;
 
 /* Same as mtgpu_pcocr_2x2_folded with options and statistics and without
- * writing `kit`.  opts and stats may be NULL. */
+ * writing `kit`.  opts and stats may be NULL.  sigma3d: the preconditioner
+ * uses only its non-zero pattern (the reference passes 0/1 flags,
+ * HarmVect3d.cpp:247-316).  With double_float, when sigma3d holds the
+ * materials' conductivities, xyz the node coordinates and the mesh is a
+ * tensor mesh in RegularMeshBuilder's numbering, the solve may use the
+ * matrix-free SpMV (mu taken as MU_0, omega read from the SLAE's diagonal):
+ * it is offered only if a set-up product agrees with the SLAE's to 1e-9
+ * (stats->matfree_check), otherwise the stored matrix is used. */
 int mtgpu_pcocr_2x2_folded_ex(int n, const int *ig, const int *jg, const int *idi,
                               const int *ijg, const double *di, const double *gg,
                               const double *pr, double *x, double eps, int maxiter,

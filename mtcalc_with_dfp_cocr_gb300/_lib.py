@@ -32,7 +32,8 @@ MTGPU_ERR_TIMEOUT = -105
 class SolveStats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("residual_rel", C.c_double),
                 ("true_residual_rel", C.c_double), ("setup_seconds", C.c_double),
-                ("solve_seconds", C.c_double), ("status", C.c_int)]
+                ("solve_seconds", C.c_double), ("status", C.c_int), ("spmv_variant", C.c_int),
+                ("matfree_check", C.c_double)]
 
 
 class SolveOpts(C.Structure):

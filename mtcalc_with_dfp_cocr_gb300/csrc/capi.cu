@@ -127,13 +127,15 @@ int mtgpu::make_stream(mtgpu_cocr_s *c, void *stream)
 }
 
 namespace {
+constexpr double kMu0 = 1.25663706143591729e-6;   // BuildMatrix/stdafx.h:31 (MU_0)
+
 // One system through the double-float survey solver: K = Re A, M = Im A,
 // omega = 1, so A = K + i M exactly.
 int solve_double_float_host(int nb, const int *ig, const int *jg, const int *idi, const int *ijg,
                      const double *di, const double *gg, const double *pr, double *x, double eps,
-                     int maxiter, int kpar, int n_nodes_c, const int *nvkat, const int *nver14,
-                     const double *sigma3d, const int *edges2, const int *ig_t, const int *jg_t,
-                     const double *gg_t, const int *is_node_bound, int verify,
+                     int maxiter, int kpar, int n_nodes_c, const double *xyz, const int *nvkat,
+                     const int *nver14, const double *sigma3d, const int *edges2, const int *ig_t,
+                     const int *jg_t, const double *gg_t, const int *is_node_bound, int verify,
                      mtgpu_solve_stats *stats)
 {
     const double t0 = now_seconds();
@@ -159,7 +161,26 @@ int solve_double_float_host(int nb, const int *ig, const int *jg, const int *idi
     if (!rc) rc = param_from_sell(A, P, st);
     if (!rc) {
         A.release();
-        rc = survey_setup(P, mesh, 1, &one, V, st);
+        // the mesh for the matrix-free SpMV (tensor meshes): mu is taken as
+        // MU_0 (the call carries no mu3d) and omega from the SLAE's diagonal;
+        // the survey set-up enables the variant only if its product agrees
+        // with this SLAE's to 1e-9
+        MatFreeMesh mm;
+        if (xyz) {
+            int nmat = 0;
+            for (int c = 0; c < kpar; c++) nmat = std::max(nmat, nvkat[c] + 1);
+            mm.xyz = xyz;
+            mm.nver = nver14;
+            mm.nver_stride = 14;
+            mm.nvkat = nvkat;
+            mm.edges = edges2;
+            mm.bound = is_node_bound;
+            mm.mu.assign(nmat, kMu0);
+            mm.sigma.assign(sigma3d, sigma3d + nmat);
+            mm.idi = idi;
+            mm.di = di;
+        }
+        rc = survey_setup(P, mesh, 1, &one, V, st, nullptr, xyz ? &mm : nullptr);
     }
     if (!rc && !(rc = upload(&db, (const double2 *)pr, nb, st)) &&
         !(rc = upload(&dx, (const double2 *)x, nb, st))) {
@@ -180,6 +201,8 @@ int solve_double_float_host(int nb, const int *ig, const int *jg, const int *idi
             stats->setup_seconds = t1 - t0;
             stats->solve_seconds = now_seconds() - t1;
             stats->status = ss.status[0];
+            stats->spmv_variant = V.ch;
+            stats->matfree_check = V.mf.check;
         }
     }
     cudaStreamSynchronize(st);
@@ -348,7 +371,6 @@ int mtgpu_pcocr_2x2_folded_ex(int n, const int *ig, const int *jg, const int *id
                               const double *gg_t, const int *is_node_bound,
                               const mtgpu_solve_opts *opts, mtgpu_solve_stats *stats)
 {
-    (void)xyz;
     MTGPU_CHECK_ARG(n > 0 && n % 2 == 0, "n must be a positive even number");
     MTGPU_CHECK_ARG(pr && x, "null vector");
     const int nb = n / 2;
@@ -358,8 +380,8 @@ int mtgpu_pcocr_2x2_folded_ex(int n, const int *ig, const int *jg, const int *id
     if (opts && opts->double_float) {
         mtgpu_solve_stats sd{};
         const int r = solve_double_float_host(nb, ig, jg, idi, ijg, di, gg, pr, x, eps, maxiter,
-                                              kpar, n_nodes_c, nvkat, nver14, sigma3d, edges2,
-                                              ig_t, jg_t, gg_t, is_node_bound,
+                                              kpar, n_nodes_c, xyz, nvkat, nver14, sigma3d,
+                                              edges2, ig_t, jg_t, gg_t, is_node_bound,
                                               opts->stop_on_true_residual, &sd);
         // a system the double-float iteration cannot finish continues in FP64:
         // from its double-float solution when that is within 100 eps of the
@@ -381,6 +403,8 @@ int mtgpu_pcocr_2x2_folded_ex(int n, const int *ig, const int *jg, const int *id
     if (rc) return rc;
     double *d_b = nullptr, *d_x = nullptr;
     mtgpu_solve_stats st{};
+    st.spmv_variant = -1;
+    st.matfree_check = -1.0;
     if ((rc = dev_alloc(&d_b, n)) || (rc = dev_alloc(&d_x, n))) goto out;
     {
         cudaError_t e = cudaMemcpyAsync(d_b, pr, sizeof(double) * n, cudaMemcpyHostToDevice, c->S.st);
@@ -428,6 +452,8 @@ int mtgpu_pcocr_2x2_folded(int n, int *ig, int *jg, int *idi, int *ijg, double *
     (void)y_omp;
     const double t0 = now_s();
     mtgpu_solve_stats st{};
+    st.spmv_variant = -1;
+    st.matfree_check = -1.0;
     st.residual_rel = 1.0;
     const int rc = mtgpu_pcocr_2x2_folded_ex(
         n, ig, jg, idi, ijg, di, gg, pr, x, eps, maxiter, kpar, n_edges_c, n_nodes_c,

@@ -483,6 +483,8 @@ int cocr_solve(CocrSolver &S, const double2 *b, double2 *x, double eps, int maxi
         stats->residual_rel = S.hctl->residual_rel;
         stats->true_residual_rel = true_rr;
         stats->status = S.hctl->status;
+        stats->spmv_variant = -1;
+        stats->matfree_check = -1.0;
     }
     return S.hctl->status;
 }

@@ -62,6 +62,7 @@ void MatFree::release()
 {
     dev_free(rb);
     dev_free(pos);
+    dev_free(bedge);
     dev_free(w);
     dev_free(f);
     on = false;
@@ -1569,7 +1570,7 @@ struct Impl {
         return MF{F.nx, F.ny, F.nz, F.nfx, F.nfy, F.nfz,
                   (long long)(F.nx - 1) * (F.ny - 1) * (F.nz - 1),
                   (F.nx - 1) * F.ny * F.nz, F.nx * (F.ny - 1) * F.nz, F.rb, F.pos, F.w,
-                  V.P->d_bedge, F.f};
+                  F.bedge, F.f};
     }
     static void spmv(Survey &V, int mode)
     {
@@ -1823,14 +1824,15 @@ namespace {
 // Dirichlet node); anything else leaves the variant off.  A set-up check
 // compares one matrix-free product with the stored-matrix product and
 // leaves the variant off unless they agree to 1e-9.
-int matfree_build(Survey &V, const mtgpu_assembly_s &a, int nsm)
+int matfree_build(Survey &V, const MatFreeMesh &a, int kuz, int kpar, int nsm)
 {
     MatFree &F = V.mf;
     F.release();
     const ParamMatrix &P = *V.P;
-    const int kuz = P.kuzlov, ns = a.nver_stride;
-    const std::vector<double> &xyz = a.xyz;
-    if ((long long)xyz.size() != 3LL * kuz || kuz < 27 || ns < 8) return MTGPU_OK;
+    const int ns = a.nver_stride;
+    const double *xyz = a.xyz;
+    if (!xyz || !a.nver || !a.nvkat || !a.edges || !a.bound || kuz < 27 || ns < 8)
+        return MTGPU_OK;
     int nx = 1;
     while (nx < kuz && xyz[3 * nx + 1] == xyz[1] && xyz[3 * nx + 2] == xyz[2]) nx++;
     int nxy = nx;
@@ -1855,7 +1857,7 @@ int matfree_build(Survey &V, const mtgpu_assembly_s &a, int nsm)
                 if (surf && !a.bound[n]) return MTGPU_OK;
             }
     const long long ncell = (long long)(nx - 1) * (ny - 1) * (nz - 1);
-    if (ncell != P.kpar) return MTGPU_OK;
+    if (ncell != kpar) return MTGPU_OK;
     // 32-bit indexing in the kernels: edges, faces and weights times systems
     const long long nfaces = (long long)nx * (ny - 1) * (nz - 1) +
                              (long long)(nx - 1) * ny * (nz - 1) +
@@ -1899,28 +1901,48 @@ int matfree_build(Survey &V, const mtgpu_assembly_s &a, int nsm)
             }
         }
     if (e != P.nb || (long long)pos.size() != P.nb) return MTGPU_OK;
+    // Dirichlet edges: both nodes flagged
+    std::vector<unsigned char> bedge(P.nb);
+    for (long long q = 0; q < P.nb; q++)
+        bedge[q] = a.bound[a.edges[2 * q]] && a.bound[a.edges[2 * q + 1]];
     // per-cell weights from the materials' mu and sigma
-    std::vector<double> mu(P.n_materials), sig(P.n_materials);
-    MTGPU_TRY(cudaMemcpyAsync(mu.data(), P.d_mu, sizeof(double) * P.n_materials,
-                              cudaMemcpyDeviceToHost, V.st));
-    MTGPU_TRY(cudaMemcpyAsync(sig.data(), P.d_sig, sizeof(double) * P.n_materials,
-                              cudaMemcpyDeviceToHost, V.st));
-    MTGPU_TRY(cudaStreamSynchronize(V.st));
-    std::vector<float2> w((size_t)6 * ncell);
+    const int nmat = (int)std::min(a.mu.size(), a.sigma.size());
+    std::vector<double> wf((size_t)3 * ncell), wmv((size_t)3 * ncell);
     for (int k = 0, c = 0; k < nz - 1; k++)
         for (int j = 0; j < ny - 1; j++)
             for (int i = 0; i < nx - 1; i++, c++) {
                 const int mat = a.nvkat[c];
-                if (mat < 0 || mat >= P.n_materials || !(mu[mat] > 0.0)) return MTGPU_OK;
+                if (mat < 0 || mat >= nmat || !(a.mu[mat] > 0.0)) return MTGPU_OK;
                 const double h[3] = {X[i + 1] - X[i], Y[j + 1] - Y[j], Z[k + 1] - Z[k]};
                 for (int d = 0; d < 3; d++) {
                     const int t1 = (d + 1) % 3, t2 = (d + 2) % 3;
-                    const dfl::df f = dfl::from_double(2.0 * h[d] / (h[t1] * h[t2]) / mu[mat] / 3.0);
-                    const dfl::df m = dfl::from_double(sig[mat] * h[t1] * h[t2] / h[d] / 9.0);
-                    w[(size_t)d * ncell + c] = make_float2(f.h, f.l);
-                    w[(size_t)(3 + d) * ncell + c] = make_float2(m.h, m.l);
+                    wf[(size_t)d * ncell + c] = 2.0 * h[d] / (h[t1] * h[t2]) / a.mu[mat] / 3.0;
+                    wmv[(size_t)d * ncell + c] = a.sigma[mat] * h[t1] * h[t2] / h[d] / 9.0;
                 }
             }
+    // a host SLAE's M carries omega_true: the ratio of its diagonal to the
+    // mass coefficient of the edge itself (4 times the 4 cells' wM) on an
+    // interior x-edge; the set-up check below confirms it on every row
+    if (a.idi && a.di) {
+        const int i = (nx - 1) / 2, j = ny / 2, k = nz / 2;
+        const int e = rb[(size_t)k * ny + j] + i * 3;   // +x edge of an interior node
+        double wsum = 0.0;
+        for (int b1 = -1; b1 <= 0; b1++)
+            for (int b2 = -1; b2 <= 0; b2++) {
+                const size_t c = ((size_t)(k + b2) * (ny - 1) + (j + b1)) * (nx - 1) + i;
+                wsum += wmv[c];
+            }
+        if (a.idi[e + 1] - a.idi[e] != 2 || !(wsum > 0.0)) return MTGPU_OK;
+        const double om = a.di[a.idi[e] + 1] / (4.0 * wsum);
+        if (!(om > 0.0)) return MTGPU_OK;
+        for (double &v : wmv) v *= om;
+    }
+    std::vector<float2> w((size_t)6 * ncell);
+    for (size_t t = 0; t < (size_t)3 * ncell; t++) {
+        const dfl::df f = dfl::from_double(wf[t]), m = dfl::from_double(wmv[t]);
+        w[t] = make_float2(f.h, f.l);
+        w[(size_t)3 * ncell + t] = make_float2(m.h, m.l);
+    }
     F.nx = nx;
     F.ny = ny;
     F.nz = nz;
@@ -1929,6 +1951,7 @@ int matfree_build(Survey &V, const mtgpu_assembly_s &a, int nsm)
     F.nfz = (long long)(nx - 1) * (ny - 1) * nz;
     int rc;
     if ((rc = dev_alloc(&F.rb, rb.size())) || (rc = dev_alloc(&F.pos, pos.size())) ||
+        (rc = dev_alloc(&F.bedge, bedge.size())) ||
         (rc = dev_alloc(&F.w, w.size())) ||
         (rc = dev_alloc(&F.f, (size_t)(F.nfx + F.nfy + F.nfz) * V.SP)))
         return rc;
@@ -1936,6 +1959,7 @@ int matfree_build(Survey &V, const mtgpu_assembly_s &a, int nsm)
     MTGPU_TRY(cudaMemcpyAsync(F.pos, pos.data(), sizeof(unsigned) * pos.size(),
                               cudaMemcpyHostToDevice, V.st));
     MTGPU_TRY(cudaMemcpyAsync(F.w, w.data(), sizeof(float2) * w.size(), cudaMemcpyHostToDevice, V.st));
+    MTGPU_TRY(cudaMemcpyAsync(F.bedge, bedge.data(), bedge.size(), cudaMemcpyHostToDevice, V.st));
     F.on = true;
     // set-up check against the stored-matrix SpMV on a test vector
     const int ch = V.ch;
@@ -1985,7 +2009,7 @@ int matfree_build(Survey &V, const mtgpu_assembly_s &a, int nsm)
 }  // namespace
 
 int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const double *omega,
-                 Survey &V, cudaStream_t st, const mtgpu_assembly_s *a)
+                 Survey &V, cudaStream_t st, const mtgpu_assembly_s *a, const MatFreeMesh *mfm)
 {
     V.release();
     MTGPU_CHECK_ARG(S >= 1 && S <= 32, "a survey batch holds 1 to 32 systems");
@@ -2061,7 +2085,27 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
     MTGPU_TRY(cudaStreamSynchronize(st));
     note_launches(8);
     if ((rc = build_tiles(V, nsm))) return rc;
-    if (a && (rc = matfree_build(V, *a, nsm))) return rc;
+    if (a) {
+        MatFreeMesh mm;
+        mm.xyz = a->xyz.data();
+        mm.nver = a->nver.data();
+        mm.nver_stride = a->nver_stride;
+        mm.nvkat = a->nvkat.data();
+        mm.edges = a->edges.data();
+        mm.bound = a->bound.data();
+        mm.mu.resize(P.n_materials);
+        mm.sigma.resize(P.n_materials);
+        MTGPU_TRY(cudaMemcpyAsync(mm.mu.data(), P.d_mu, sizeof(double) * P.n_materials,
+                                  cudaMemcpyDeviceToHost, st));
+        MTGPU_TRY(cudaMemcpyAsync(mm.sigma.data(), P.d_sig, sizeof(double) * P.n_materials,
+                                  cudaMemcpyDeviceToHost, st));
+        MTGPU_TRY(cudaStreamSynchronize(st));
+        if ((long long)a->xyz.size() == 3LL * P.kuzlov &&
+            (rc = matfree_build(V, mm, P.kuzlov, P.kpar, nsm)))
+            return rc;
+    } else if (mfm && (rc = matfree_build(V, *mfm, mesh.n_nodes_c, mesh.kpar, nsm))) {
+        return rc;
+    }
     // autotune the SpMV variant: time each candidate, keep the fastest.
     // MTGPU_SPMV_VARIANT (environment) pins an available variant instead:
     // runs under a profiler, which serialises and cold-starts every launch,

@@ -37,6 +37,7 @@ struct MatFree {
     int *rb = nullptr;               // [nz][ny] number of the first edge of node (0, j, k)
     unsigned *pos = nullptr;         // [nb] rows x-, y-, z-edges: i | j << 10 | k << 20
     float2 *w = nullptr;             // [6][cells] double-float wF/3 (x, y, z), wM/9 (x, y, z)
+    unsigned char *bedge = nullptr;  // [nb] Dirichlet edges
     float4 *f = nullptr;             // face circulations [faces][SP]
     double check = -1.0;             // set-up check: max |A_mf s - A s| / max |A s|
     void release();
@@ -91,10 +92,27 @@ inline bool spmv_variant_available(const Survey &V, int v)
     return false;
 }
 
-// a: the assembly (host mesh copies) when the survey is built from one: on a
-// tensor mesh it enables the matrix-free SpMV variant
+// Host mesh description for the matrix-free SpMV (all arrays host, 0-based)
+struct MatFreeMesh {
+    const double *xyz = nullptr;       // [kuzlov][3]
+    const int *nver = nullptr;         // [kpar][nver_stride]
+    int nver_stride = 14;
+    const int *nvkat = nullptr;        // [kpar]
+    const int *edges = nullptr;        // [nb][2]
+    const int *bound = nullptr;        // [kuzlov] Dirichlet node flags
+    std::vector<double> mu, sigma;     // per material: mu3d * MU_0, sigma3d
+    // the survey's M holds omega_true sigma C (a host SLAE at one frequency,
+    // solved with omega = 1): omega_true is read from the SLAE's diagonal
+    const int *idi = nullptr;          // block diagonal of that SLAE (lower storage)
+    const double *di = nullptr;
+};
+
+// a: the assembly (host mesh copies) when the survey is built from one, or
+// mfm: the mesh of a host SLAE; on a tensor mesh either enables the
+// matrix-free SpMV variant
 int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const double *omega,
-                 Survey &V, cudaStream_t st, const mtgpu_assembly_s *a = nullptr);
+                 Survey &V, cudaStream_t st, const mtgpu_assembly_s *a = nullptr,
+                 const MatFreeMesh *mfm = nullptr);
 // b, x: system-major FP64 [S][nb] complex; x is the initial guess in and the
 // solution out.  verify: continue until the true residual is below eps too.
 int survey_solve(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, double eps,

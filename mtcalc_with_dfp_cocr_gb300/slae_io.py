@@ -158,7 +158,7 @@ def mesh_to_solve_mesh(m) -> SolveMesh:
     nver = np.zeros((m.kpar, 14), np.int32)
     nver[:, :8] = m.cell_nodes()
     return SolveMesh(m.kpar, m.nb, m.kuzlov, m.xyz(), m.nvkat, nver,
-                     (m.mat_sigma != 0).astype(np.float64), m.edges(),
+                     np.asarray(m.mat_sigma, np.float64), m.edges(),
                      np.zeros(m.kuzlov + 1, np.int32), np.zeros(1, np.int32),
                      np.zeros(1, np.float64), m.is_node_bound())
 
