@@ -297,9 +297,10 @@ def gpu_arm(args):
                       + 4 * ny_ * nz_ + tail)
         edges = "k_mf_edges2" if variant == 33 else "k_mf_edges"
         spmv_kernel = f"k_mf_faces + {edges} (matrix-free double-float SpMV + MRS tail, S systems)"
-        traffic = SPMV_MF_TRAFFIC_C2 if WORKLOAD == "c2" else None
-        traffic_src = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of k_mf_faces<2> + "
-                       f"{edges}<2> on c2, profiles/spmv_matfree_c2_s2.md")
+        # the capture is of variant 32 (the autotuning's pick on c2)
+        traffic = SPMV_MF_TRAFFIC_C2 if WORKLOAD == "c2" and variant == 32 else None
+        traffic_src = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_mf_faces<2> + "
+                       "k_mf_edges<2> on c2, profiles/spmv_matfree_c2_s2.md") if traffic else None
     else:
         spmv_bytes = nc * (4 + 8 + 8) + nr * (4 + 8) + meta + 2 * S * 16 * nb + tail
         spmv_kernel = (f"k_spmv variant {variant} (batched double-float SELL-32 SpMV + MRS "
