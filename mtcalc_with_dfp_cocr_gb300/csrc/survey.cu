@@ -2001,8 +2001,9 @@ int matfree_build(Survey &V, const MatFreeMesh &a, int kuz, int kpar, int nsm)
     double dm, bm;
     memcpy(&dm, &mx[0], sizeof(double));
     memcpy(&bm, &mx[1], sizeof(double));
-    F.check = bm > 0.0 ? dm / bm : 1.0;
-    if (!(F.check < 1e-9)) F.on = false;
+    const double check = bm > 0.0 ? dm / bm : 1.0;
+    if (!(check < 1e-9)) F.release();   // not this matrix's operator: variant off, memory back
+    F.check = check;
     return MTGPU_OK;
 }
 
