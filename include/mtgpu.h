@@ -119,12 +119,21 @@ int mtgpu_mult_mv_block_2x2(int nb, const int *ig, const int *jg, const int *idi
  * a 16 MiB static device scratch array that every GPU loading the library
  * holds until exit and that all calls share: calls whose kernels overlap on
  * the GPU (e.g. on two streams at once) race on it.  The first call on a
- * device looks the array's address up for that device.  The call only
- * enqueues work on `stream` (a cudaStream_t, NULL = default stream):
- * synchronise before reading d_y. */
+ * device looks the array's address up for that device and keeps it; calls
+ * after cudaDeviceReset (which may reload the module elsewhere) are not
+ * supported.  The call only enqueues work on `stream` (a cudaStream_t,
+ * NULL = default stream): synchronise before reading d_y or *d_status.
+ * The kernels check the index arrays they cannot see from the host: if ig,
+ * idi or ijg does not start at 0 (1-based arrays), nothing else is read, y is
+ * left unspecified and *d_status gets MTGPU_NOALLOC_NOT_ZERO_BASED; an entry
+ * whose column is not below its row, or whose block is neither 1 nor 2
+ * doubles, is skipped and sets MTGPU_NOALLOC_BAD_ENTRY.  d_status is one
+ * device int of the caller (0 = every entry used), or NULL. */
+#define MTGPU_NOALLOC_NOT_ZERO_BASED 1
+#define MTGPU_NOALLOC_BAD_ENTRY 2
 int mtgpu_mult_mv_block_2x2_noalloc(int nb, const int *d_ig, const int *d_jg, const int *d_idi,
                                     const int *d_ijg, const double *d_di, const double *d_gg,
-                                    const double *d_x, double *d_y, void *stream);
+                                    const double *d_x, double *d_y, int *d_status, void *stream);
 
 /* Folded preconditioner on host buffers: BuildGMatrix + BuildDiagComplex +
  * ApplyPreconditionerComplex (Code/COCR_FP/FoldedPreconditioner.cpp:68-259,
@@ -280,6 +289,14 @@ int mtgpu_survey_solve(mtgpu_survey *s, const double *d_b, double *d_x, double e
  * written), with CUDA events on the survey's stream; *ms receives the total.
  * It overwrites the survey's work vectors; a solve re-initialises them. */
 int mtgpu_survey_spmv_timed(mtgpu_survey *s, int reps, float *ms);
+
+/* y_k = A_k x_k = (K + i omega_k M) x_k for every system of the survey, with
+ * the SpMV variant in use (double-float arithmetic; x and y FP64 device
+ * [S][2 nb]).  No counterpart in the reference (Mult_MV_block_2x2,
+ * Code/COCR_FP/block_2x2_solver.cpp:73-173, applies one system's stored
+ * matrix).  It overwrites the survey's work vectors; a solve
+ * re-initialises them. */
+int mtgpu_survey_spmv(mtgpu_survey *s, const double *d_x, double *d_y);
 
 /* The SpMV variant the set-up autotuning chose (0: x segments and matrix
  * slots staged in shared memory per tile of slices; 1: x segments staged

@@ -27,6 +27,8 @@ MTGPU_ERR_CUDA = -102
 MTGPU_ERR_IO = -103
 MTGPU_ERR_UNSUPPORTED = -104
 MTGPU_ERR_TIMEOUT = -105
+MTGPU_NOALLOC_NOT_ZERO_BASED = 1
+MTGPU_NOALLOC_BAD_ENTRY = 2
 
 
 class SolveStats(C.Structure):
@@ -74,7 +76,7 @@ SIGNATURES = {
         C.POINTER(SolveOpts), C.POINTER(SolveStats)]),
     "mtgpu_mult_mv_block_2x2": (C.c_int, [C.c_int, _i, _i, _i, _i, _d, _d, _d, _d]),
     "mtgpu_mult_mv_block_2x2_noalloc": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
-                                                  _vp, _vp]),
+                                                  _vp, _vp, _vp]),
     "mtgpu_folded_apply": (C.c_int, [
         C.c_int, _i, _i, _i, _i, _d, _d, C.c_int, C.c_int, _i, _i, _d, _i, _i, _i, _d, _i,
         _d, _d, C.POINTER(C.c_int), _vp, _vp]),
@@ -100,6 +102,7 @@ SIGNATURES = {
     "mtgpu_survey_create": (C.c_int, [_vp, C.c_int, _d, _vp, C.POINTER(_vp)]),
     "mtgpu_survey_solve": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int, C.c_int,
                                      C.POINTER(SurveyStats)]),
+    "mtgpu_survey_spmv": (C.c_int, [_vp, _vp, _vp]),
     "mtgpu_survey_spmv_timed": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_float)]),
     "mtgpu_survey_tuning": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_float)]),
     "mtgpu_survey_set_spmv_variant": (C.c_int, [_vp, C.c_int]),

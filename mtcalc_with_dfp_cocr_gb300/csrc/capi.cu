@@ -461,11 +461,14 @@ int mtgpu_pcocr_2x2_folded(int n, int *ig, int *jg, int *idi, int *ijg, double *
         gg_t, is_node_bound, nullptr, &st);
     if (rc < -100) return rc;
     const double secs = now_s() - t0;
-    // the reference's `kit` line, base_solver.cpp:181-200
+    // the reference's `kit` line, base_solver.cpp:181-200.  As there, a kit
+    // file that cannot be opened is reported and the solver's code returned:
+    // x holds the solution either way.
     FILE *fp = fopen("kit", "w");
     if (!fp) {
+        printf("cannot open file kit\n");
         set_last_message("cannot open file kit");
-        return MTGPU_ERR_IO;
+        return rc;
     }
     fprintf(fp, "r=%e\teps=%e\tkit=%d\t", st.residual_rel, eps, st.iterations);
     fprintf(fp, "time=%lf sec\n", secs);

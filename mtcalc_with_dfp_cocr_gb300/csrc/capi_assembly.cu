@@ -284,6 +284,13 @@ int mtgpu_survey_spmv_timed(mtgpu_survey *s, int reps, float *ms)
     return survey_spmv_timed(s->V, reps, ms);
 }
 
+int mtgpu_survey_spmv(mtgpu_survey *s, const double *d_x, double *d_y)
+{
+    MTGPU_CHECK_ARG(s && d_x && d_y, "null argument");
+    MTGPU_TRY(cudaStreamSynchronize(cudaStreamLegacy));
+    return survey_spmv(s->V, (const double2 *)d_x, (double2 *)d_y);
+}
+
 void mtgpu_survey_destroy(mtgpu_survey *s)
 {
     if (!s) return;

@@ -14,6 +14,12 @@
 // it.  It receives the upper-triangle contributions A_ij x_i of the lower
 // storage; each call clears the part it uses first.  Calls whose kernels
 // overlap on the GPU (for example on two streams at once) race on it.
+//
+// The index arrays live on the device, so the host cannot check them.  The
+// kernels do: arrays that do not start at 0 (the reference's 1-based files
+// passed without subtracting 1) are not read beyond their first element, and
+// an entry whose column is not below its row or whose block is neither 1 nor
+// 2 doubles is skipped.  Either case sets a bit of the call's status word.
 #include "mtgpu_internal.cuh"
 
 #include <mutex>
@@ -24,6 +30,8 @@ namespace {
 constexpr int kNoAllocMaxEdges = 1 << 20;   // 1,048,576 edges (16 MiB of scratch)
 
 __device__ __align__(256) double2 g_upper[kNoAllocMaxEdges];
+// status of the latest call: MTGPU_NOALLOC_NOT_ZERO_BASED | MTGPU_NOALLOC_BAD_ENTRY
+__device__ int g_status;
 
 // device address of g_upper for every device, looked up once per device
 std::mutex g_mu;
@@ -49,6 +57,7 @@ __global__ void k_na_clear(int nb, double2 *upper)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nb) upper[i] = make_double2(0.0, 0.0);
+    if (i == 0) g_status = 0;
 }
 
 __device__ __forceinline__ double2 block_times(const double *a, int size, double2 x)
@@ -58,7 +67,8 @@ __device__ __forceinline__ double2 block_times(const double *a, int size, double
 }
 
 // row i: y_i = D_i x_i + sum_lower A_ij x_j (stored directly), and the
-// mirrored A_ij x_i added into upper[j]
+// mirrored A_ij x_i added into upper[j].  Nothing past the first element of
+// an index array is read unless all three start at 0.
 __global__ void k_na_rows(int nb, const int *__restrict__ ig, const int *__restrict__ jg,
                           const int *__restrict__ idi, const int *__restrict__ ijg,
                           const double *__restrict__ di, const double *__restrict__ gg,
@@ -66,12 +76,25 @@ __global__ void k_na_rows(int nb, const int *__restrict__ ig, const int *__restr
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nb) return;
+    if (__ldg(ig) != 0 || __ldg(idi) != 0 || __ldg(ijg) != 0) {
+        if (i == 0) atomicOr(&g_status, MTGPU_NOALLOC_NOT_ZERO_BASED);
+        return;
+    }
     const double2 xi = x[i];
-    double2 acc = block_times(&di[idi[i]], idi[i + 1] - idi[i], xi);
-    for (int q = ig[i]; q < ig[i + 1]; q++) {
+    const int d0 = idi[i], dsz = idi[i + 1] - d0;
+    double2 acc = make_double2(0.0, 0.0);
+    bool bad = false;
+    if (dsz == 1 || dsz == 2) acc = block_times(&di[d0], dsz, xi);
+    else bad = true;
+    const int q0 = ig[i], q1 = ig[i + 1];
+    for (int q = q0; q < q1; q++) {
         const int j = jg[q];
-        const double *a = &gg[ijg[q]];
-        const int size = ijg[q + 1] - ijg[q];
+        const int a0 = ijg[q], size = ijg[q + 1] - a0;
+        if (j < 0 || j >= i || (size != 1 && size != 2)) {
+            bad = true;
+            continue;
+        }
+        const double *a = &gg[a0];
         const double2 t = block_times(a, size, x[j]);
         acc.x += t.x;
         acc.y += t.y;
@@ -79,13 +102,17 @@ __global__ void k_na_rows(int nb, const int *__restrict__ ig, const int *__restr
         atomicAdd(&upper[j].x, u.x);
         atomicAdd(&upper[j].y, u.y);
     }
+    if (bad) atomicOr(&g_status, MTGPU_NOALLOC_BAD_ENTRY);
     y[i] = acc;
 }
 
-__global__ void k_na_add(int nb, const double2 *upper, double2 *y)
+// y += upper; the status word goes to the caller's d_status
+__global__ void k_na_add(int nb, const double2 *upper, double2 *y, int *status)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nb) return;
+    const int st = *(volatile int *)&g_status;
+    if (i == 0 && status) *status = st;
+    if (i >= nb || (st & MTGPU_NOALLOC_NOT_ZERO_BASED)) return;
     const double2 u = upper[i];
     double2 v = y[i];
     v.x += u.x;
@@ -101,7 +128,8 @@ using namespace mtgpu;
 extern "C" int mtgpu_mult_mv_block_2x2_noalloc(int nb, const int *d_ig, const int *d_jg,
                                                const int *d_idi, const int *d_ijg,
                                                const double *d_di, const double *d_gg,
-                                               const double *d_x, double *d_y, void *stream)
+                                               const double *d_x, double *d_y, int *d_status,
+                                               void *stream)
 {
     MTGPU_CHECK_ARG(nb > 0, "nb must be positive");
     MTGPU_CHECK_ARG(nb <= kNoAllocMaxEdges,
@@ -111,6 +139,7 @@ extern "C" int mtgpu_mult_mv_block_2x2_noalloc(int nb, const int *d_ig, const in
                     "null device pointer");
     MTGPU_CHECK_ARG(((uintptr_t)d_x % 16) == 0 && ((uintptr_t)d_y % 16) == 0,
                     "x and y must be 16-byte aligned");
+    MTGPU_CHECK_ARG(((uintptr_t)d_status % sizeof(int)) == 0, "d_status must be int-aligned");
     double2 *upper = nullptr;
     int rc = scratch_address(&upper);
     if (rc) return rc;
@@ -119,7 +148,7 @@ extern "C" int mtgpu_mult_mv_block_2x2_noalloc(int nb, const int *d_ig, const in
     k_na_clear<<<blocks, kThreads, 0, st>>>(nb, upper);
     k_na_rows<<<blocks, kThreads, 0, st>>>(nb, d_ig, d_jg, d_idi, d_ijg, d_di, d_gg,
                                            (const double2 *)d_x, (double2 *)d_y, upper);
-    k_na_add<<<blocks, kThreads, 0, st>>>(nb, upper, (double2 *)d_y);
+    k_na_add<<<blocks, kThreads, 0, st>>>(nb, upper, (double2 *)d_y, d_status);
     note_launches(3);
     MTGPU_TRY(cudaGetLastError());
     return MTGPU_OK;

@@ -2233,6 +2233,31 @@ int survey_iter_timed(Survey &V, int reps, float *ms)
     return MTGPU_OK;
 }
 
+// y_k = A_k x_k for every system with the current SpMV variant: FP64
+// system-major x, y [S][nb] complex in and out, through the double-float
+// vectors of the iteration.  It overwrites the survey's work vectors; a
+// solve re-initialises them.
+int survey_spmv(Survey &V, const double2 *x_sys_major, double2 *y_sys_major)
+{
+    std::vector<SysState> init(32);
+    for (int k = 0; k < 32; k++) {
+        SysState s{};
+        s.status = k < V.S ? kRun : MTGPU_OK;
+        s.maxiter = 1;
+        init[k] = s;
+    }
+    MTGPU_TRY(cudaMemcpyAsync(V.sys, init.data(), sizeof(SysState) * 32, cudaMemcpyHostToDevice, V.st));
+    const long long tot = (long long)V.nb * V.SP;
+    const unsigned ge = (unsigned)((tot + kB - 1) / kB);
+    k_in<<<ge, kB, 0, V.st>>>(V.nb, V.S, V.SP, x_sys_major, V.s);
+    MTGPU_SP_DISPATCH(V.SP, spmv_only(V));
+    k_out<<<ge, kB, 0, V.st>>>(V.nb, V.S, V.SP, V.z, y_sys_major);
+    note_launches(2);
+    MTGPU_TRY(cudaGetLastError());
+    MTGPU_TRY(cudaStreamSynchronize(V.st));
+    return MTGPU_OK;
+}
+
 namespace {
 
 int upload_sys(Survey &V)
@@ -2327,8 +2352,13 @@ int survey_solve(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, do
     }
     const unsigned long long kpi = (V.G.m > 0 ? 4 : 3) + (V.ch >= kMatFree ? 1 : 0);
     long long guard = 0;
-    const long long guard_max =
+    long long guard_max =
         (long long)maxiter + (long long)(kMaxContinue + 1) * 4 * iters_per_launch + 64;
+    // MTGPU_SURVEY_GUARD_ITERS (environment) lowers the guard: the device
+    // stops every system at maxiter, so only this makes the guard's error
+    // path run in a test
+    if (const char *g = getenv("MTGPU_SURVEY_GUARD_ITERS"))
+        if (atoll(g) > 0) guard_max = std::min(guard_max, atoll(g));
     for (;;) {
         bool running = false;
         for (int k = 0; k < V.S; k++) running |= V.hsys[k].status == kRun;

@@ -118,6 +118,7 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
 int survey_solve(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, double eps,
                  int maxiter, int verify, int iters_per_launch, mtgpu_survey_stats *stats);
 int survey_spmv_timed(Survey &V, int reps, float *ms);
+int survey_spmv(Survey &V, const double2 *x_sys_major, double2 *y_sys_major);
 int survey_iter_timed(Survey &V, int reps, float *ms);
 int survey_set_variant(Survey &V, int variant);
 

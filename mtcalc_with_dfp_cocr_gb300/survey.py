@@ -48,11 +48,17 @@ class Survey:
             pass
 
     def spmv_timed(self, reps):
-        """Device milliseconds of `reps` batched FP32 SpMV launches."""
+        """Device milliseconds of `reps` batched double-float SpMV launches."""
         ms = C.c_float()
         _lib.check(_lib.lib().mtgpu_survey_spmv_timed(self._h, int(reps), C.byref(ms)),
                    "mtgpu_survey_spmv_timed")
         return ms.value
+
+    def spmv(self, x, y):
+        """y[k] = A_k x[k] for every system with the SpMV variant in use;
+        x, y: torch CUDA float64 tensors shaped (S, 2 nb)."""
+        _lib.check(_lib.lib().mtgpu_survey_spmv(self._h, C.c_void_p(x.data_ptr()),
+                                                C.c_void_p(y.data_ptr())), "mtgpu_survey_spmv")
 
     def tuning(self):
         """(chosen SpMV variant, {variant: ms per launch}) of the set-up

@@ -19,10 +19,11 @@
 #                plus ref_smoothing_main.cpp and ref_shim/pardiso_shim.cpp:
 #                the default (smoothing) receiver output
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   (default $MTCALC_REFERENCE_ROOT, else a `reference` directory beside the repository)
 set -euo pipefail
-REF="${1:-/root/reference}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
+REF="${1:-${MTCALC_REFERENCE_ROOT:-$HERE/../../reference}}"
 OUT="$HERE/_ref"
 SHIM="$HERE/ref_shim"
 mkdir -p "$OUT"

@@ -23,7 +23,7 @@ what a solve needs, compactly:
                       (2500 m / 500 m steps)
 
 Usage (needs the reference; not run by the tests):
-    python tests/golden/make_dtm_fixture.py [--ref /root/reference]
+    python tests/golden/make_dtm_fixture.py [--ref REFERENCE_ROOT]
 """
 from __future__ import annotations
 
@@ -71,7 +71,8 @@ def run_builder(ex, s, steps):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get(
+        "MTCALC_REFERENCE_ROOT", os.path.join(os.path.dirname(ROOT), "reference")))
     a = ap.parse_args()
     subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), a.ref])
     ex = os.path.join(a.ref, "CalculationExample")

@@ -11,7 +11,7 @@ meshes written by this package's generator, and stores what they produce:
                         counts, solution norms and seeded sample entries
 
 Usage (needs the reference sources; not run by the tests):
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py [--ref REFERENCE_ROOT]
 """
 from __future__ import annotations
 
@@ -95,7 +95,8 @@ def c1_summary():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get(
+        "MTCALC_REFERENCE_ROOT", os.path.join(os.path.dirname(ROOT), "reference")))
     a = ap.parse_args()
     subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), a.ref])
     full_fixture("tiny", 1.0, 1)

@@ -16,7 +16,7 @@ The receivers are the workload's 3x3 surface grid plus points inside cells,
 on faces, in the air and in the padding, to exercise the location rule.
 
 Usage (needs the reference sources; not run by the tests):
-    python tests/golden/make_golden_receivers.py [--ref /root/reference]
+    python tests/golden/make_golden_receivers.py [--ref REFERENCE_ROOT]
 """
 from __future__ import annotations
 
@@ -79,7 +79,8 @@ def run_receivers(m, rec, v3):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get(
+        "MTCALC_REFERENCE_ROOT", os.path.join(os.path.dirname(ROOT), "reference")))
     a = ap.parse_args()
     subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), a.ref])
     w = workloads.make("small")

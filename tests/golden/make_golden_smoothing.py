@@ -21,7 +21,7 @@ of every subdomain as the reference logs them (Subdomain.cpp:447-448), the
 curl A subdomain first, then the A subdomains by material.
 
 Usage (needs the reference sources; not run by the tests):
-    python tests/golden/make_golden_smoothing.py [--ref /root/reference]
+    python tests/golden/make_golden_smoothing.py [--ref REFERENCE_ROOT]
 """
 from __future__ import annotations
 
@@ -83,7 +83,8 @@ def run_smoothing(m, rec, v3):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get(
+        "MTCALC_REFERENCE_ROOT", os.path.join(os.path.dirname(ROOT), "reference")))
     a = ap.parse_args()
     subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), a.ref])
     out = {}

@@ -141,3 +141,65 @@ def test_spmv_variants_agree(gpu, name, S):
             a = x[k].cpu().numpy().view(np.complex128)[earth]
             r = ref[0][k].cpu().numpy().view(np.complex128)[earth]
             assert np.linalg.norm(a - r) <= tol * np.linalg.norm(r), (v, k)
+
+
+def test_survey_iteration_guard_times_out(gpu, monkeypatch):
+    """The host loop around the graph launches gives up with MTGPU_ERR_TIMEOUT
+    once it has run more iterations than its guard allows (the device stops
+    every system at maxiter, so the test lowers the guard through
+    MTGPU_SURVEY_GUARD_ITERS); the survey object stays usable."""
+    torch = gpu
+    from mtcalc_with_dfp_cocr_gb300 import _lib
+    w = workloads.make("small")
+    tabs = _tables(w, [0.1])
+    A = assembly.Assembly(w.mesh)
+    b = torch.empty(1, 2 * w.mesh.nb, dtype=torch.float64, device="cuda")
+    A.rhs([0.1], [1], tabs[0][0], np.stack([tabs[0][1]]), np.stack([tabs[0][2]]), b)
+    sv = survey.Survey(A, [0.1])
+    x = torch.zeros_like(b)
+    monkeypatch.setenv("MTGPU_SURVEY_GUARD_ITERS", "8")
+    with pytest.raises(_lib.MtgpuError) as e:
+        sv.solve(b, x, eps=1e-8, maxiter=20000, verify=True)
+    assert "guard" in str(e.value)
+    monkeypatch.delenv("MTGPU_SURVEY_GUARD_ITERS")
+    x.zero_()
+    code, st = sv.solve(b, x, eps=1e-8, maxiter=20000, verify=True)
+    assert code == 0 and st["true_residual_rel"][0] < 1e-8
+    sv.close()
+    A.close()
+
+
+@pytest.mark.parametrize("variant", [32, 33])
+def test_matfree_operator_on_gradients(gpu, variant):
+    """The matrix-free SpMV on discrete gradients x = grad(phi): the curl-curl
+    part vanishes (curl grad = 0), so y = i omega M x checks the mass part
+    alone, which the set-up check (a random vector, dominated by the
+    curl-curl part) cannot resolve below ~1e-9.  Compared per system with
+    the oracle's port of Mult_MV_block_2x2 on the assembled SLAE."""
+    torch = gpu
+    w = workloads.make("c1")
+    nus = [1.0, 10.0, 0.01, 100.0]
+    tabs = _tables(w, nus)
+    A = assembly.Assembly(w.mesh)
+    sv = survey.Survey(A, nus)
+    sv.set_spmv_variant(variant)
+    e = w.mesh.edges()
+    bound = np.zeros(len(w.mesh.xyz()), bool)
+    bound[w.mesh.boundary_nodes()] = True
+    rng = np.random.default_rng(5)
+    X = np.zeros((len(nus), 2 * w.mesh.nb))
+    for k in range(len(nus)):
+        phi = rng.standard_normal(len(bound)) + 1j * rng.standard_normal(len(bound))
+        phi[bound] = 0.0
+        g = phi[e[:, 1]] - phi[e[:, 0]]
+        X[k, 0::2], X[k, 1::2] = g.real, g.imag
+    x = torch.tensor(X, device="cuda")
+    y = torch.empty_like(x)
+    sv.spmv(x, y)
+    Y = y.cpu().numpy()
+    for k, nu in enumerate(nus):
+        s = O.assemble(w.mesh, nu, 1, *tabs[k])
+        y_ref = O.spmv(s, X[k])
+        assert np.max(np.abs(Y[k] - y_ref)) <= 1e-9 * np.max(np.abs(y_ref)), (variant, nu)
+    sv.close()
+    A.close()
