@@ -26,10 +26,10 @@ bandwidth.  The timed region is an NVTX range "timed" for ncu's
 --nvtx-include.
 
 Reference arm (--impl reference).  The reference's CPU algorithm (the
-oracle restatement of COCR_FP, all host threads) on a bounded sample of the
-same workload: preconditioner set-up plus a fixed number of iterations,
-extrapolated to the reference's own iteration count for the system (pinned
-by running the reference programs, tests/golden/c2_summary.json).
+oracle restatement of COCR_FP with the reference's thread cap, nproc - 1)
+on the headline system: every timed step is one whole solve (set-up and
+iterations to the reference's stop rule), in a process of its own
+(oracle/cpu_solve.py).  `cpu_baseline` of the GPU arm is one such solve.
 
 Multi-GPU: systems are independent (replicas over the survey's systems);
 every rank solves its own copy of the workload and `value` is the
@@ -262,6 +262,11 @@ def gpu_arm(args):
     value = whole_job_seconds_per_solve(ms, args.steps, S, world)
     batched = info["batched"]
 
+    # per-result error of the headline solutions against the FP64 answers
+    # of the reference's own COCR_FP (tests/golden/c2_survey.npz, made by
+    # tests/golden/make_oracle_surveys.py) at the workload's receivers
+    oracle_err = oracle_parity(w, systems, tables, A, x)
+
     # comparison: the plain FP64 COCR (the reference's algorithm) on the GPU
     step_plain()
     plain_steps = max(1, min(args.steps, 2))
@@ -371,73 +376,142 @@ def gpu_arm(args):
         "e2e": {"value": e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d // e2e_steps,
                 "d2h_bytes_per_step": d2h // e2e_steps,
                 "path": "mtgpu_pcocr_2x2_folded_ex(double_float=1, stop_on_true_residual=1), host SLAE buffers"},
+        "oracle_parity": oracle_err,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_sample(host[0], mesh_h, systems[0],
-                                         fallback_iterations=info["plain"][systems[0]][0])
+        import tempfile
+        s0 = host[0]
+        with tempfile.TemporaryDirectory() as td:
+            f = os.path.join(td, "slae.npz")
+            np.savez(f, ig=s0.ig, jg=s0.jg, idi=s0.idi, ijg=s0.ijg, di=s0.di, gg=s0.gg, pr=s0.pr,
+                     eps=s0.eps, maxiter=s0.maxiter)
+            pinned = ref_iterations()
+            out["cpu_baseline"] = cpu_baseline(systems[0], f,
+                                               pinned[systems[0]] if pinned else None)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
+def oracle_parity(w, systems, tables, A, x):
+    """Errors of the batched solutions' MT responses against the reference's
+    FP64 COCR_FP answers, per receiver result: Z of every component relative
+    to the tensor's off-diagonal scale, |Z| and rho_a of Zxy, Zyx relative,
+    their phases in degrees."""
+    from mtcalc_with_dfp_cocr_gb300 import receivers
+    p = os.path.join(ROOT, "tests", "golden", f"{WORKLOAD}_survey.npz")
+    if not os.path.exists(p):
+        return None
+    g = np.load(p)
+    nus = [f for f, _ in systems]
+    alfas = [a for _, a in systems]
+    z1d = tables[nus[0]][0]
+    us = np.stack([tables[f][1] for f in nus])
+    uc = np.stack([tables[f][2] for f in nus])
+    R = receivers.Receivers(A, w.receivers)
+    freqs = sorted(set(nus))
+    if not np.allclose(freqs, g["freqs"], rtol=1e-14):
+        return None
+    sx = [systems.index((f, 1)) for f in freqs]
+    sy = [systems.index((f, 0)) for f in freqs]
+    E, H, _ = R.fields(x, nus, alfas, z1d, us, uc)
+    mt = R.mt_response(freqs, sx, sy, E, H).cpu().numpy()[..., g["keep"]]
+    R.close()
+    ref = g["mt"]
+    z = mt[..., 0:8:2] + 1j * mt[..., 1:8:2]
+    zr = ref[..., 0:8:2] + 1j * ref[..., 1:8:2]
+    off = [1, 2]
+    scale = np.abs(zr[..., off]).max(axis=-1, keepdims=True)
+    ph = np.abs(mt[..., 12:16][..., off] - ref[..., 12:16][..., off]) % 360.0
+    return {"reference": str(g["source"]), "receivers": int(len(w.receivers)),
+            "Z_rel_to_offdiag_max": float((np.abs(z - zr) / scale).max()),
+            "Zabs_offdiag_rel_max": float((np.abs(mt[..., 8:12][..., off] - ref[..., 8:12][..., off])
+                                           / ref[..., 8:12][..., off]).max()),
+            "rho_a_offdiag_rel_max": float((np.abs(mt[..., 16:20][..., off] - ref[..., 16:20][..., off])
+                                            / ref[..., 16:20][..., off]).max()),
+            "phase_offdiag_deg_max": float(np.minimum(ph, 360.0 - ph).max()),
+            "iterations_reference": [int(v) for v in g["iterations"]],
+            "true_rel_reference": [float(v) for v in g["true_rel"]]}
+
+
 # --------------------------------------------------------------- CPU baseline
-def cpu_sample(slae, mesh, key, target_seconds=15.0, fallback_iterations=None):
-    """The oracle restatement of COCR_FP with all host threads: set-up plus
-    a bounded number of iterations, extrapolated to the reference's
-    iteration count for this system."""
-    from oracle import pyoracle as O
-    cores = os.cpu_count() or 1
-    _, _, s1 = O.pcocr(slae, mesh, nthreads=cores, iter_limit=3)
-    _, _, s0 = O.pcocr(slae, mesh, nthreads=cores, iter_limit=23)
-    per_guess = max((s0.seconds - s1.seconds) / 20.0, 1e-4)
-    n2 = int(min(3000, max(50, (target_seconds - s1.seconds) / per_guess)))
-    _, _, s2 = O.pcocr(slae, mesh, nthreads=cores, iter_limit=n2)
-    per_iter = (s2.seconds - s1.seconds) / (n2 - 3)
-    setup = max(0.0, s1.seconds - 3 * per_iter)
-    # one thread (the reference's default nthreads.txt): a shorter sample
-    _, _, t1 = O.pcocr(slae, mesh, nthreads=1, iter_limit=3)
-    _, _, t2 = O.pcocr(slae, mesh, nthreads=1, iter_limit=13)
-    per_iter_1 = (t2.seconds - t1.seconds) / 10
-    setup_1 = max(0.0, t1.seconds - 3 * per_iter_1)
-    pinned = ref_iterations()
-    n_ref = pinned[key] if pinned else fallback_iterations
-    return {"value": setup + per_iter * n_ref, "unit": UNIT, "cores": cores, "kind": "port",
-            "cpu_model": cpu_model(),
-            "value_1_thread": setup_1 + per_iter_1 * n_ref,
-            "sample": f"oracle COCR_FP restatement, {cores} threads: set-up + {n2} iterations "
-                      f"on the {key[0]} Hz / {'XY'[1 - key[1]]} system "
-                      f"({s2.seconds:.1f} s), extrapolated to " +
-                      (f"the reference's {n_ref} iterations" if pinned else
-                       f"{n_ref} iterations (the GPU solve's count; reference count not pinned)"),
-            "seconds_per_iteration": per_iter, "setup_seconds": setup}
+def cpu_threads():
+    """The reference's OpenMP cap, omp_get_max_threads() - 1
+    (Code/COCR_FP/ControlOMP.cpp:46), on this host."""
+    return max(1, (os.cpu_count() or 2) - 1)
+
+
+def run_cpu_solves(key, threads, slae_file=None, warmup=0, steps=1, sample_iterations=0):
+    """Whole solves of the oracle's COCR_FP restatement in a process of its
+    own (oracle/cpu_solve.py): nothing else shares its cores or OpenMP
+    runtime, in either arm."""
+    cmd = [sys.executable, "-m", "oracle.cpu_solve", WORKLOAD, str(float(key[0])), str(int(key[1])),
+           str(threads), "--warmup", str(warmup), "--steps", str(steps),
+           "--sample-iterations", str(sample_iterations)]
+    if slae_file:
+        cmd += ["--slae", slae_file]
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"CPU solve failed: {r.stdout[-2000:]}\n{r.stderr[-2000:]}")
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def one_thread_estimate(key, slae_file, iterations):
+    """The reference's default (nthreads.txt = 1): a whole one-thread solve
+    takes minutes, so set-up + 5 and set-up + 45 iterations are timed and
+    the solve is extrapolated to `iterations`."""
+    a = run_cpu_solves(key, 1, slae_file, sample_iterations=5)["seconds"][0]
+    b = run_cpu_solves(key, 1, slae_file, sample_iterations=45)["seconds"][0]
+    per = (b - a) / 40.0
+    return max(0.0, a - 5 * per) + per * iterations
+
+
+def cpu_baseline(key, slae_file, ref_iters):
+    """One whole solve of the headline system with the reference's thread
+    cap, timed on the wall clock (set-up included, as the reference's kit
+    time), plus the one-thread estimate."""
+    threads = cpu_threads()
+    r = run_cpu_solves(key, threads, slae_file, warmup=1, steps=1)
+    t, it = r["seconds"][0], r["iterations"][0]
+    return {"value": t, "unit": UNIT, "cores": threads, "kind": "port",
+            "cpu_model": cpu_model(), "iterations": it,
+            "iterations_reference": ref_iters, "true_rel": r["true_rel"],
+            "value_1_thread_estimate": one_thread_estimate(key, slae_file, it),
+            "sample": f"one whole solve of the {key[0]} Hz / {'XY'[1 - key[1]]} system (set-up + "
+                      f"{it} iterations to the reference's stop rule) by the oracle's COCR_FP "
+                      f"restatement with {threads} threads (the reference's cap, nproc - 1), "
+                      f"in a process of its own; value_1_thread_estimate: set-up + 45 iterations "
+                      f"on one thread, extrapolated to {it}"}
 
 
 def reference_arm(args):
     world, rank, local = dist_init()
     if rank != 0:
         return
-    from mtcalc_with_dfp_cocr_gb300 import slae_io, workloads
-    from oracle import pyoracle as O
+    from mtcalc_with_dfp_cocr_gb300 import workloads
     w = workloads.make(WORKLOAD)
-    tables = make_inputs(w)
-    nu, alfa = w.systems[0]
-    t = tables[nu]
-    slae = O.assemble(w.mesh, nu, alfa, t[0], t[1], t[2], eps=1e-8, maxiter=20000)
-    mesh = slae_io.mesh_to_solve_mesh(w.mesh)
-    vals, base = [], None
-    for i in range(args.warmup + args.steps):
-        b = cpu_sample(slae, mesh, (nu, alfa), target_seconds=6.0)
-        if i >= args.warmup:
-            vals.append(b["value"])
-            base = b
-    v = statistics.median(vals)
-    base["value"] = v
+    key = w.systems[0]
+    threads = cpu_threads()
+    t0 = time.perf_counter()
+    r = run_cpu_solves(key, threads, warmup=args.warmup, steps=args.steps)
+    wall = time.perf_counter() - t0
+    secs = r["seconds"]
+    v = statistics.median(secs)
+    base = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "cpu_model": cpu_model(),
+            "iterations": r["iterations"][0], "true_rel": r["true_rel"],
+            "seconds_per_step": secs, "process_wall_s": wall,
+            "sample": f"{args.steps} whole solves of the {key[0]} Hz / {'XY'[1 - key[1]]} "
+                      f"system (set-up + {r['iterations'][0]} iterations each, to the "
+                      f"reference's stop rule) by the oracle's COCR_FP restatement with "
+                      f"{threads} threads (the reference's cap, nproc - 1); {args.warmup} "
+                      f"warm-up solves of 20 iterations; median reported"}
     out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f64 (complex128)",
+           "warmup": args.warmup, "ms_per_step": statistics.mean(secs) * 1e3,
+           "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64 (complex128)",
            "data": "synthetic (seeded layered earth + 20 random blocks)",
            "config": {"workload": "c2: 96x96x64 cells, 1,812,736 edges, 0.1 Hz, COCR_FP "
                                   "algorithm on the host cores"},
@@ -564,6 +638,7 @@ def survey_run(args):
             "Z_offdiag_rel_max": float(zerr.max()), "Z_diag_rel_to_offdiag_max": float(derr.max()),
             "rho_a_rel_max": float(rho_err.max()), "phase_deg_max": float(ph_err.max()),
             "per_frequency": per_freq},
+        "oracle_parity": oracle_err,
         "gpu_launches": int(launches), "clocks": clk.summary(),
     }
     print(json.dumps(out), flush=True)

@@ -260,23 +260,43 @@ void mtgpu_assembly_destroy(mtgpu_assembly *a);
  * ---------------------------------------------------------------------- */
 typedef struct mtgpu_survey_s mtgpu_survey;
 
+#define MTGPU_SURVEY_MAX_SYSTEMS 256
+
 typedef struct {
-    int status[32];               /* MTGPU_OK / MTGPU_MAXITER / ... per system   */
-    int iterations[32];           /* double-float iterations per system         */
-    int verifications[32];        /* true-residual evaluations per system       */
-    int fp64_iterations[32];      /* iterations of the FP64 re-solve (0: none)  */
-    double true_residual_rel[32]; /* final ||b - A x|| / ||b|| per system        */
-    double residual_rel[32];      /* last smoothed (stop-test) residual per system */
-    double seconds;               /* host wall time of the solve                 */
+    int status[MTGPU_SURVEY_MAX_SYSTEMS];          /* MTGPU_OK / MTGPU_MAXITER / ... per system */
+    int iterations[MTGPU_SURVEY_MAX_SYSTEMS];      /* double-float iterations per system       */
+    int verifications[MTGPU_SURVEY_MAX_SYSTEMS];   /* true-residual evaluations per system     */
+    int fp64_iterations[MTGPU_SURVEY_MAX_SYSTEMS]; /* iterations of the FP64 re-solve (0: none) */
+    double true_residual_rel[MTGPU_SURVEY_MAX_SYSTEMS]; /* final ||b - A x|| / ||b||           */
+    double residual_rel[MTGPU_SURVEY_MAX_SYSTEMS]; /* last smoothed (stop-test) residual       */
+    double seconds;                                /* host wall time of the solve              */
 } mtgpu_survey_stats;
 
-/* S systems with frequencies nu[S] [Hz] on assembly a; stream: a
- * cudaStream_t or NULL. */
+/* S systems (1 <= S <= MTGPU_SURVEY_MAX_SYSTEMS) with frequencies nu[S] [Hz]
+ * on assembly a; stream: a cudaStream_t (its work is waited for before a
+ * solve) or NULL.  The systems are solved in batches of up to 32 (one lane
+ * per system), each batch on a stream of its own, the batches' CUDA graphs
+ * launched in turn so that they run side by side. */
 int mtgpu_survey_create(mtgpu_assembly *a, int S, const double *nu, void *stream,
                         mtgpu_survey **out);
 
-/* d_b: device [S][2 nb] right-hand sides (e.g. from mtgpu_assembly_rhs);
- * d_x: device [S][2 nb] initial guesses in, solutions out.  Each system stops
+/* A survey over nmesh meshes (uneven sizes): S[m] systems on assembly a[m],
+ * nu[] the frequencies of all systems, mesh by mesh.  The systems' vectors
+ * are packed one after the other: system k's 2 nb(k) doubles start at
+ * offset_k = sum over j < k of 2 nb(j) in d_b, d_x (mtgpu_survey_info gives
+ * the offsets).  Each mesh's systems form their own batches; all batches
+ * run side by side as in mtgpu_survey_create.  No counterpart in the
+ * reference, which runs every mesh's systems one by one. */
+int mtgpu_survey_create_multi(int nmesh, mtgpu_assembly *const *a, const int *S, const double *nu,
+                              void *stream, mtgpu_survey **out);
+
+/* Number of systems, of batches, and the S + 1 packing offsets (doubles; any
+ * pointer may be NULL). */
+int mtgpu_survey_info(const mtgpu_survey *s, int *S, int *batches, long long *offsets);
+
+/* d_b: device right-hand sides of all systems, packed by mtgpu_survey_info's
+ * offsets ([S][2 nb] on one mesh; e.g. from mtgpu_assembly_rhs);
+ * d_x: the same layout, initial guesses in, solutions out.  Each system stops
  * when its MRS-smoothed relative residual is below eps (the reference rule,
  * Code/COCR_FP/rci.cpp:66-75); with verify = 1 it then also continues until
  * ||b - A x|| / ||b|| < eps.  maxiter: per-system iteration limit (double-float
@@ -284,7 +304,8 @@ int mtgpu_survey_create(mtgpu_assembly *a, int S, const double *nu, void *stream
 int mtgpu_survey_solve(mtgpu_survey *s, const double *d_b, double *d_x, double eps, int maxiter,
                        int verify, mtgpu_survey_stats *stats);
 
-/* Time `reps` launches of the batched double-float SpMV (all systems) as the
+/* Time `reps` launches of the batched double-float SpMV (the first batch's
+ * systems) as the
  * iteration launches it (z = A s with the MRS tail: r read, s_m read and
  * written), with CUDA events on the survey's stream; *ms receives the total.
  * It overwrites the survey's work vectors; a solve re-initialises them. */
@@ -298,15 +319,18 @@ int mtgpu_survey_spmv_timed(mtgpu_survey *s, int reps, float *ms);
  * re-initialises them. */
 int mtgpu_survey_spmv(mtgpu_survey *s, const double *d_x, double *d_y);
 
-/* The SpMV variant the set-up autotuning chose (0: x segments and matrix
+/* The SpMV variant the set-up autotuning chose for the first batch (0: x segments and matrix
  * slots staged in shared memory per tile of slices; 1: x segments staged
  * only; 2, 4, 8: slots in flight per thread, gathers from global memory;
  * 18, 20: two-system batches only, one thread per row for both systems with
  * 2 or 4 slots in flight; 32: matrix-free, tensor meshes only: the curl-curl
  * part as D^T F D (edge -> face circulations, face mass matrix) and the mass
  * part regenerated from six weights per cell instead of the stored matrix;
- * 33: the same with two systems per thread, batches of 2 or more) and the
- * times it measured for the variants 0, 1, 2, 4, 8, 18, 20, 32, 33 (ms[9]: ms
+ * 33: the same with two systems per thread, batches of 2 or more; 34: the
+ * same operator in one kernel per launch, a block marching through the node
+ * planes of its tile with the edge values and face circulations in shared
+ * memory, bit-for-bit equal to 32) and the times it measured for the
+ * variants 0, 1, 2, 4, 8, 18, 20, 32, 33, 34 (ms[10]: ms
  * per whole iteration with that variant, so that each SpMV sees the cache as
  * the other kernels of an iteration leave it; 0 where a variant was not
  * available). */
@@ -316,7 +340,7 @@ int mtgpu_survey_tuning(const mtgpu_survey *s, int *variant, float *ms);
  * (for profiler runs: a profiler serialises and cold-starts every launch, and
  * would make the autotuning choose differently from a plain run). */
 
-/* Pins the SpMV variant (0, 1, 2, 4, 8, 18, 20, 32 or 33) instead of the
+/* Pins the SpMV variant (0, 1, 2, 4, 8, 18, 20, 32, 33 or 34) instead of the
  * autotuned choice.  The stored-matrix variants sum the same products in the
  * same order; the matrix-free one computes the same operator in another
  * order (it is enabled only where a set-up product agrees with the stored
@@ -324,7 +348,7 @@ int mtgpu_survey_tuning(const mtgpu_survey *s, int *variant, float *ms);
  * for this survey (0 and 1 need their tiles to fit shared memory, 18 and 20
  * two systems, 32 a survey created from an assembly of a tensor mesh with
  * RegularMeshBuilder's numbering and all outer nodes Dirichlet, 33 that and
- * at least two systems). */
+ * at least two systems, 34 that and no Dirichlet node inside the mesh). */
 int mtgpu_survey_set_spmv_variant(mtgpu_survey *s, int variant);
 
 void mtgpu_survey_destroy(mtgpu_survey *s);

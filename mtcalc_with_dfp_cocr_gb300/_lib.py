@@ -52,10 +52,16 @@ class FemMesh(C.Structure):
                 ("dpr0", C.c_void_p), ("n_bound", C.c_int), ("bound_nodes", C.c_void_p)]
 
 
+SURVEY_MAX_SYSTEMS = 256   # MTGPU_SURVEY_MAX_SYSTEMS
+
+
 class SurveyStats(C.Structure):
-    _fields_ = [("status", C.c_int * 32), ("iterations", C.c_int * 32),
-                ("verifications", C.c_int * 32), ("fp64_iterations", C.c_int * 32),
-                ("true_residual_rel", C.c_double * 32), ("residual_rel", C.c_double * 32),
+    _fields_ = [("status", C.c_int * SURVEY_MAX_SYSTEMS),
+                ("iterations", C.c_int * SURVEY_MAX_SYSTEMS),
+                ("verifications", C.c_int * SURVEY_MAX_SYSTEMS),
+                ("fp64_iterations", C.c_int * SURVEY_MAX_SYSTEMS),
+                ("true_residual_rel", C.c_double * SURVEY_MAX_SYSTEMS),
+                ("residual_rel", C.c_double * SURVEY_MAX_SYSTEMS),
                 ("seconds", C.c_double)]
 
 
@@ -102,6 +108,9 @@ SIGNATURES = {
     "mtgpu_survey_create": (C.c_int, [_vp, C.c_int, _d, _vp, C.POINTER(_vp)]),
     "mtgpu_survey_solve": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int, C.c_int,
                                      C.POINTER(SurveyStats)]),
+    "mtgpu_survey_create_multi": (C.c_int, [C.c_int, C.POINTER(_vp), _i, _d, _vp, C.POINTER(_vp)]),
+    "mtgpu_survey_info": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                    C.POINTER(C.c_longlong)]),
     "mtgpu_survey_spmv": (C.c_int, [_vp, _vp, _vp]),
     "mtgpu_survey_spmv_timed": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_float)]),
     "mtgpu_survey_tuning": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_float)]),

@@ -9,10 +9,15 @@ separate programs per frequency and polarisation (RegularMeshBuilder,
 Harm1D, BuildMatrix, COCR_FP, OutputNu, then ImpedanceZToEdsAll and
 calcimpedance over all of them): the mesh (meshbuilder.py), the 1-D normal
 fields (normal1d.py), the device assembly, every frequency x polarisation
-through the batched solver (16 frequencies per batch), the receiver fields
+in one batched survey solve, the receiver fields
 (by default through the reference's default output, subdomain smoothing;
 --output direct evaluates the edge basis at the receivers) and the MT
 responses.
+
+With --results DIR (default CASE_DIR/Results) it also writes the files of
+the reference's last step: calcimpedance's 4-byte result files (|Z|, phases,
+rho_a, effective rho_a, the Wiese-Parkinson tipper and the complex values)
+and ImpedanceZToEdsAll's edsall0_0_imp / ft0_0 (edsall.py).
 
 The table has the layout of the reference's published results
 (CalculationResults/625_500_reg_R_Z.txt): per receiver and period,
@@ -30,11 +35,8 @@ import time
 
 import numpy as np
 
-from . import meshbuilder, normal1d
+from . import edsall, meshbuilder, normal1d
 from .receivers import MT_RHO, MT_ZABS
-
-BATCH = 16   # frequencies per batch (x 2 polarisations = 32 systems)
-
 
 def run(case, eps=None, maxiter=None, device="cuda", log=None, output="smooth"):
     """Solve every frequency x polarisation of `case`; returns
@@ -59,31 +61,32 @@ def run(case, eps=None, maxiter=None, device="cuda", log=None, output="smooth"):
     out = np.empty((len(freqs), len(case.receivers), 34))
     stats = {"nb": mesh.nb, "cells": mesh.kpar, "lines": [mesh.nx, mesh.ny, mesh.nz],
              "receivers_outside_mesh": miss, "eps": eps, "output": output, "systems": []}
-    for f0 in range(0, len(freqs), BATCH):
-        fb = freqs[f0:f0 + BATCH]
-        nus = np.repeat(fb, 2)
-        alfas = np.tile(np.array([1, 0], np.int32), len(fb))
-        tabs = [normal1d.solve_1d(f, tops, sig) for f in fb]
-        us = np.repeat(np.stack([t[1] for t in tabs]), 2, axis=0)
-        uc = np.repeat(np.stack([t[2] for t in tabs]), 2, axis=0)
-        b = torch.empty(len(nus), 2 * mesh.nb, dtype=torch.float64, device=device)
-        A.rhs(nus, alfas, tabs[0][0], us, uc, b)
-        x = torch.zeros_like(b)
-        sv = Survey(A, nus)
-        code, st = sv.solve(b, x, eps=eps, maxiter=maxiter, verify=True)
-        sv.close()
-        for k in range(len(nus)):
-            stats["systems"].append({
-                "nu": float(nus[k]), "polarisation": "XY"[1 - int(alfas[k])],
-                "status": st["status"][k], "iterations": st["iterations"][k],
-                "fp64_iterations": st["fp64_iterations"][k],
-                "true_residual_rel": st["true_residual_rel"][k]})
-        if log:
-            log(f"frequencies {f0 + 1}-{f0 + len(fb)} of {len(freqs)}: code {code}, "
-                f"iterations {max(st['iterations'])}")
-        E, H, _ = R.fields(x, nus, alfas, tabs[0][0], us, uc)
-        out[f0:f0 + len(fb)] = R.mt_response(
-            fb, np.arange(0, 2 * len(fb), 2), np.arange(1, 2 * len(fb), 2), E, H).cpu().numpy()
+    # every frequency x polarisation in one survey (CalcStarter's order: for
+    # every frequency X then Y, Code/CalcStarter/main.cpp:311-325)
+    nus = np.repeat(freqs, 2)
+    alfas = np.tile(np.array([1, 0], np.int32), len(freqs))
+    tabs = [normal1d.solve_1d(f, tops, sig) for f in freqs]
+    us = np.repeat(np.stack([t[1] for t in tabs]), 2, axis=0)
+    uc = np.repeat(np.stack([t[2] for t in tabs]), 2, axis=0)
+    b = torch.empty(len(nus), 2 * mesh.nb, dtype=torch.float64, device=device)
+    A.rhs(nus, alfas, tabs[0][0], us, uc, b)
+    x = torch.zeros_like(b)
+    sv = Survey(A, nus)
+    code, st = sv.solve(b, x, eps=eps, maxiter=maxiter, verify=True)
+    stats["batches"] = sv.batches
+    sv.close()
+    for k in range(len(nus)):
+        stats["systems"].append({
+            "nu": float(nus[k]), "polarisation": "XY"[1 - int(alfas[k])],
+            "status": st["status"][k], "iterations": st["iterations"][k],
+            "fp64_iterations": st["fp64_iterations"][k],
+            "true_residual_rel": st["true_residual_rel"][k]})
+    if log:
+        log(f"{len(nus)} systems in {stats['batches']} batches: code {code}, "
+            f"iterations {max(st['iterations'])}")
+    E, H, _ = R.fields(x, nus, alfas, tabs[0][0], us, uc)
+    out[:] = R.mt_response(freqs, np.arange(0, 2 * len(freqs), 2),
+                           np.arange(1, 2 * len(freqs), 2), E, H).cpu().numpy()
     if output == "smooth":
         stats["smoothing"] = R.smoothing_info()
     stats["seconds"] = time.perf_counter() - t0
@@ -115,6 +118,9 @@ def main(argv=None):
     ap.add_argument("--eps", type=float, default=None,
                     help="relative residual of the solves (default: settings.cfg's)")
     ap.add_argument("--maxiter", type=int, default=None)
+    ap.add_argument("--results", default=None,
+                    help="directory of calcimpedance's result files and edsall0_0_imp "
+                         "(default CASE/Results; '-' writes none)")
     ap.add_argument("--output", choices=["smooth", "direct"], default="smooth",
                     help="receiver output: the reference's default subdomain smoothing, or the "
                          "direct evaluation of the edge basis at the receiver")
@@ -124,6 +130,9 @@ def main(argv=None):
                       output=a.output)
     out = a.out or os.path.join(a.case, "results_R_Z.txt")
     write_table(out, case, resp)
+    if a.results != "-":
+        edsall.write_results(a.results or os.path.join(a.case, "Results"), case.freqs,
+                             case.receivers, resp)
     with open(os.path.splitext(out)[0] + "_stats.json", "w") as f:
         json.dump(stats, f, indent=1)
     print(f"{out}: {len(case.receivers)} receivers x {len(case.freqs)} periods, "

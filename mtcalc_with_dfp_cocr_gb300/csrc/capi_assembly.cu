@@ -171,48 +171,103 @@ int mtgpu_cocr_create_from_assembly(mtgpu_assembly *a, double nu, void *stream, 
 // ------------------------------------------------------------ survey
 #include "survey.cuh"
 
+#include <memory>
+
+// A survey: its systems, mesh by mesh, cut into batches (groups) of at most
+// 32 systems of one mesh, each with its own stream and CUDA graph.  The
+// systems' vectors are packed one after the other (system k at sys_off[k]
+// doubles) in the caller's d_b / d_x.
 struct mtgpu_survey_s {
-    mtgpu::Survey V;
-    std::vector<double> nu;
-    mtgpu_assembly *a = nullptr;
-    cudaStream_t st = nullptr;
-    bool own_stream = false;
+    std::vector<std::unique_ptr<mtgpu::Survey>> groups;
+    std::vector<int> g_first;                 // first system of every group
+    std::vector<cudaStream_t> g_st;           // stream of every group (owned)
+    std::vector<double> nu;                   // frequency of every system
+    std::vector<mtgpu_assembly *> sys_asm;    // assembly of every system
+    std::vector<long long> sys_off;           // [S + 1] offsets in doubles
+    cudaStream_t user = nullptr;              // the caller's stream (NULL: legacy default)
 };
 
 extern "C" {
 
+void mtgpu_survey_destroy(mtgpu_survey *s)
+{
+    if (!s) return;
+    for (size_t g = 0; g < s->groups.size(); g++) {
+        if (s->g_st[g]) cudaStreamSynchronize(s->g_st[g]);
+        s->groups[g]->release();
+        if (s->g_st[g]) cudaStreamDestroy(s->g_st[g]);
+    }
+    delete s;
+}
+
+int mtgpu_survey_create_multi(int nmesh, mtgpu_assembly *const *a, const int *S, const double *nu,
+                              void *stream, mtgpu_survey **out)
+{
+    MTGPU_CHECK_ARG(a && S && nu && out && nmesh >= 1, "null argument");
+    *out = nullptr;
+    int total = 0;
+    for (int m = 0; m < nmesh; m++) {
+        MTGPU_CHECK_ARG(a[m] != nullptr, "null assembly");
+        MTGPU_CHECK_ARG(S[m] >= 1, "every mesh needs at least one system");
+        total += S[m];
+    }
+    MTGPU_CHECK_ARG(total <= MTGPU_SURVEY_MAX_SYSTEMS, "a survey holds at most "
+                    "MTGPU_SURVEY_MAX_SYSTEMS (256) systems");
+    for (int k = 0; k < total; k++) MTGPU_CHECK_ARG(nu[k] > 0.0, "frequencies must be positive");
+    auto *s = new mtgpu_survey_s();
+    s->user = (cudaStream_t)stream;
+    s->nu.assign(nu, nu + total);
+    s->sys_off.assign(1, 0);
+    int k0 = 0;
+    for (int m = 0; m < nmesh; m++) {
+        mtgpu_assembly *am = a[m];
+        mtgpu_mesh_desc mesh{am->P.kpar, am->P.nb, am->P.kuzlov, am->nvkat.data(), am->nver.data(),
+                             am->sigflag.data(), am->edges.data(), am->ig_t.data(), am->ig_t.data(),
+                             nullptr, am->bound.data(), am->nver_stride};
+        for (int k = 0; k < S[m]; k++) {
+            s->sys_asm.push_back(am);
+            s->sys_off.push_back(s->sys_off.back() + 2LL * am->P.nb);
+        }
+        // batches of 32 systems, the last one smaller
+        for (int f = 0; f < S[m]; f += 32) {
+            const int n = std::min(32, S[m] - f);
+            cudaStream_t st = nullptr;
+            cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+            if (e != cudaSuccess) {
+                mtgpu_survey_destroy(s);
+                set_last_error(e, "cudaStreamCreateWithFlags", __FILE__, __LINE__);
+                return MTGPU_ERR_CUDA;
+            }
+            s->groups.push_back(std::make_unique<mtgpu::Survey>());
+            s->g_st.push_back(st);
+            s->g_first.push_back(k0 + f);
+            std::vector<double> om(n);
+            for (int k = 0; k < n; k++) om[k] = kTwoPi * nu[k0 + f + k];
+            int rc = survey_setup(am->P, mesh, n, om.data(), *s->groups.back(), st, am);
+            if (rc) {
+                mtgpu_survey_destroy(s);
+                return rc;
+            }
+        }
+        k0 += S[m];
+    }
+    *out = s;
+    return MTGPU_OK;
+}
+
 int mtgpu_survey_create(mtgpu_assembly *a, int S, const double *nu, void *stream,
                         mtgpu_survey **out)
 {
-    MTGPU_CHECK_ARG(a && nu && out, "null argument");
-    *out = nullptr;
-    MTGPU_CHECK_ARG(S >= 1 && S <= 32, "a survey batch holds 1 to 32 systems");
-    for (int k = 0; k < S; k++) MTGPU_CHECK_ARG(nu[k] > 0.0, "frequencies must be positive");
-    auto *s = new mtgpu_survey_s();
-    s->a = a;
-    s->nu.assign(nu, nu + S);
-    if (stream) {
-        s->st = (cudaStream_t)stream;
-    } else {
-        cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
-        if (e != cudaSuccess) {
-            delete s;
-            set_last_error(e, "cudaStreamCreateWithFlags", __FILE__, __LINE__);
-            return MTGPU_ERR_CUDA;
-        }
-        s->own_stream = true;
-    }
-    std::vector<double> om(S);
-    for (int k = 0; k < S; k++) om[k] = kTwoPi * nu[k];
-    mtgpu_mesh_desc mesh{a->P.kpar, a->P.nb, a->P.kuzlov, a->nvkat.data(), a->nver.data(),
-                         a->sigflag.data(), a->edges.data(), a->ig_t.data(), a->ig_t.data(),
-                         nullptr, a->bound.data(), a->nver_stride};
-    int rc = survey_setup(a->P, mesh, S, om.data(), s->V, s->st, a);
-    if (rc) {
-        mtgpu_survey_destroy(s);
-        return rc;
-    }
-    *out = s;
+    return mtgpu_survey_create_multi(1, &a, &S, nu, stream, out);
+}
+
+int mtgpu_survey_info(const mtgpu_survey *s, int *S, int *groups, long long *offsets)
+{
+    MTGPU_CHECK_ARG(s != nullptr, "null survey");
+    if (S) *S = (int)s->nu.size();
+    if (groups) *groups = (int)s->groups.size();
+    if (offsets)
+        for (size_t k = 0; k < s->sys_off.size(); k++) offsets[k] = s->sys_off[k];
     return MTGPU_OK;
 }
 
@@ -222,32 +277,59 @@ int mtgpu_survey_solve(mtgpu_survey *s, const double *d_b, double *d_x, double e
     MTGPU_CHECK_ARG(s && d_b && d_x, "null argument");
     MTGPU_CHECK_ARG(eps > 0.0, "eps must be positive");
     MTGPU_TRY(cudaStreamSynchronize(cudaStreamLegacy));
+    if (s->user) MTGPU_TRY(cudaStreamSynchronize(s->user));
     const double t0 = now_seconds();
     mtgpu_survey_stats local{};
     mtgpu_survey_stats *st = stats ? stats : &local;
-    int rc = survey_solve(s->V, (const double2 *)d_b, (double2 *)d_x, eps, maxiter, verify, 16,
-                          st);
-    if (rc <= MTGPU_ERR_ARG) return rc;
+    // every batch started, then launched and collected in turn, so that
+    // their graphs run side by side on the GPU
+    const size_t ng = s->groups.size();
+    std::vector<SurveyRun> R(ng);
+    int rc = MTGPU_OK;
+    for (size_t g = 0; g < ng && !rc; g++) {
+        const long long off = s->sys_off[s->g_first[g]];
+        rc = survey_begin(*s->groups[g], (const double2 *)(d_b + off), (double2 *)(d_x + off), eps,
+                          maxiter, verify, 16, R[g]);
+    }
+    for (bool busy = true; !rc && busy;) {
+        busy = false;
+        for (size_t g = 0; g < ng && !rc; g++) rc = survey_launch(*s->groups[g], R[g]);
+        for (size_t g = 0; g < ng && !rc; g++) {
+            rc = survey_collect(*s->groups[g], R[g]);
+            busy |= !R[g].done;
+        }
+    }
+    for (size_t g = 0; g < ng && !rc; g++) {
+        const int r2 = survey_finish(*s->groups[g], R[g], st, s->g_first[g]);
+        if (r2 <= MTGPU_ERR_ARG) rc = r2;
+    }
+    for (auto &r : R) r.release();
+    if (rc <= MTGPU_ERR_ARG) {
+        for (size_t g = 0; g < ng; g++) cudaStreamSynchronize(s->g_st[g]);
+        return rc;
+    }
     // systems the double-float iteration could not finish: FP64 COCR with the
     // iterations left.  A double-float solution within 100 eps of the target
     // is the FP64 iteration's start; a stalled one (far above: very low
     // frequencies, large errors in the air's gradient components, from which
     // the FP64 iteration does not recover) is discarded for x = 0.
-    const long long nb = s->V.nb;
     int worst = MTGPU_OK;
-    for (int k = 0; k < s->V.S; k++) {
+    const int S = (int)s->nu.size();
+    cudaStream_t st0 = s->g_st[0];
+    for (int k = 0; k < S; k++) {
         const int left = maxiter - st->iterations[k];
+        const long long off = s->sys_off[k], n = s->sys_off[k + 1] - off;
         if (st->status[k] == MTGPU_MAXITER && left > 0) {
             mtgpu_cocr *c = nullptr;
-            int r2 = mtgpu_cocr_create_from_assembly(s->a, s->nu[k], s->st, &c);
+            int r2 = mtgpu_cocr_create_from_assembly(s->sys_asm[k], s->nu[k], st0, &c);
             if (r2) return r2;
             mtgpu_solve_opts opts{verify, 0, 0};
             mtgpu_solve_stats s64{};
             const double tr = st->true_residual_rel[k];
             if (!(tr >= 0.0 && tr < 100.0 * eps))
-                MTGPU_TRY(cudaMemsetAsync(d_x + 2 * nb * k, 0, sizeof(double) * 2 * nb, s->st));
-            MTGPU_TRY(cudaStreamSynchronize(s->st));
-            r2 = mtgpu_cocr_solve(c, d_b + 2 * nb * k, d_x + 2 * nb * k, eps, left, &opts, &s64);
+                MTGPU_TRY(cudaMemsetAsync(d_x + off, 0, sizeof(double) * n, st0));
+            MTGPU_TRY(cudaStreamSynchronize(st0));
+            r2 = mtgpu_cocr_solve(c, d_b + off, d_x + off, eps, left, &opts, &s64);
             mtgpu_cocr_destroy(c);
             if (r2 <= MTGPU_ERR_ARG) return r2;
             st->status[k] = r2;
@@ -264,40 +346,43 @@ int mtgpu_survey_solve(mtgpu_survey *s, const double *d_b, double *d_x, double e
 int mtgpu_survey_tuning(const mtgpu_survey *s, int *variant, float *ms)
 {
     MTGPU_CHECK_ARG(s != nullptr, "null survey");
-    if (variant) *variant = s->V.ch;
+    const mtgpu::Survey &V = *s->groups[0];
+    if (variant) *variant = V.ch;
     if (ms)
-        for (int i = 0; i < kSpmvVariants; i++) ms[i] = s->V.tune_ms[i];
+        for (int i = 0; i < kSpmvVariants; i++) ms[i] = V.tune_ms[i];
     return MTGPU_OK;
 }
 
 int mtgpu_survey_set_spmv_variant(mtgpu_survey *s, int variant)
 {
     MTGPU_CHECK_ARG(s != nullptr, "null survey");
-    MTGPU_CHECK_ARG(spmv_variant_available(s->V, variant),
-                    "unknown SpMV variant, or not available for this survey");
-    return survey_set_variant(s->V, variant);
+    for (auto &g : s->groups)
+        MTGPU_CHECK_ARG(spmv_variant_available(*g, variant),
+                        "unknown SpMV variant, or not available for this survey");
+    for (auto &g : s->groups) {
+        const int rc = survey_set_variant(*g, variant);
+        if (rc) return rc;
+    }
+    return MTGPU_OK;
 }
 
 int mtgpu_survey_spmv_timed(mtgpu_survey *s, int reps, float *ms)
 {
     MTGPU_CHECK_ARG(s && ms && reps > 0, "bad argument");
-    return survey_spmv_timed(s->V, reps, ms);
+    return survey_spmv_timed(*s->groups[0], reps, ms);
 }
 
 int mtgpu_survey_spmv(mtgpu_survey *s, const double *d_x, double *d_y)
 {
     MTGPU_CHECK_ARG(s && d_x && d_y, "null argument");
     MTGPU_TRY(cudaStreamSynchronize(cudaStreamLegacy));
-    return survey_spmv(s->V, (const double2 *)d_x, (double2 *)d_y);
-}
-
-void mtgpu_survey_destroy(mtgpu_survey *s)
-{
-    if (!s) return;
-    if (s->st) cudaStreamSynchronize(s->st);
-    s->V.release();
-    if (s->own_stream && s->st) cudaStreamDestroy(s->st);
-    delete s;
+    if (s->user) MTGPU_TRY(cudaStreamSynchronize(s->user));
+    for (size_t g = 0; g < s->groups.size(); g++) {
+        const long long off = s->sys_off[s->g_first[g]];
+        const int rc = survey_spmv(*s->groups[g], (const double2 *)(d_x + off), (double2 *)(d_y + off));
+        if (rc) return rc;
+    }
+    return MTGPU_OK;
 }
 
 }  // extern "C"

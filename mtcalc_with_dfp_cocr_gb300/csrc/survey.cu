@@ -66,6 +66,7 @@ void MatFree::release()
     dev_free(w);
     dev_free(f);
     on = false;
+    lattice = false;
 }
 
 namespace {
@@ -1064,6 +1065,8 @@ k_mf_edges(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restr
     tail.finish<SP>(sys, partials, mode);
 }
 
+#include "mf_tile.cuh"
+
 // largest |a - b| and |b| over n float4 double-float pairs (as ordered bits
 // of non-negative doubles)
 __global__ void k_maxdiff(long long n, const float4 *__restrict__ a, const float4 *__restrict__ b,
@@ -1575,6 +1578,12 @@ struct Impl {
     static void spmv(Survey &V, int mode)
     {
         const Mat A = mat(V);
+        if (V.ch == kMatFree + 2) {
+            const MfTileGrid G{V.mft[0], V.mft[1], V.mft[2], V.mft[3], V.mft[4], V.mft[5], V.mft[6]};
+            k_mf_tile<SP><<<V.g_mft, MfTile<SP>::NT, MfTile<SP>::SMEM, V.st>>>(
+                mfd(V), G, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode);
+            return;
+        }
         if (V.ch == kMatFree || V.ch == kMatFree + 1) {
             const MF M = mfd(V);
             k_mf_faces<SP><<<V.g_mff, kB, 0, V.st>>>(M, V.s, V.sys);
@@ -1686,6 +1695,43 @@ struct Impl {
                     V.g_mfe = g((const void *)k_mf_edges2<SP>,
                                 (V.nb + 2 * kB / SP - 1) / (2 * kB / SP));
             }
+            // tiled variant: tiles x systems groups, the z range cut into
+            // chunks so that about one wave of resident blocks is launched
+            using T = MfTile<SP>;
+            int res = 0;
+            if (cudaFuncSetAttribute((const void *)k_mf_tile<SP>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, T::SMEM) != cudaSuccess ||
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&res, (const void *)k_mf_tile<SP>, T::NT,
+                                                              T::SMEM) != cudaSuccess ||
+                res < 1) {
+                cudaGetLastError();
+                res = 1;
+            }
+            // tile shape: the x columns split evenly in tiles of at most TX,
+            // then as many rows as the threads and the halo frame allow
+            const int ntx = ceil_div(V.mf.nx, T::TX);
+            const int tw = ceil_div(V.mf.nx, ntx);
+            int th = std::min(T::TX * T::TY / tw, T::NS / (tw + 2) - 2);
+            th = std::max(1, std::min(th, V.mf.ny));
+            const int tx = ntx, ty = ceil_div(V.mf.ny, th), grp = SP / T::SB;
+            V.mft[5] = tw;
+            V.mft[6] = th;
+            const int bxy = tx * ty * grp;
+            // z chunks: the fewest waves x (planes per chunk + 2 of prologue)
+            int zc = 1;
+            long long best = -1;
+            for (int c = 1; c <= std::max(1, V.mf.nz / 4); c++) {
+                const long long waves = ceil_div(bxy * c, res * nsm);
+                const long long cost = waves * (ceil_div(V.mf.nz, c) + 2);
+                if (best < 0 || cost < best) {
+                    best = cost;
+                    zc = c;
+                }
+            }
+            const int kz = ceil_div(V.mf.nz, zc);
+            zc = ceil_div(V.mf.nz, kz);
+            V.mft[0] = tx; V.mft[1] = ty; V.mft[2] = zc; V.mft[3] = grp; V.mft[4] = kz;
+            V.g_mft = bxy * zc;
         }
         if constexpr (SP == 2) {
             if (V.ch == kRowVariant + 2 || V.ch == kRowVariant + 4) {
@@ -1905,6 +1951,20 @@ int matfree_build(Survey &V, const MatFreeMesh &a, int kuz, int kpar, int nsm)
     std::vector<unsigned char> bedge(P.nb);
     for (long long q = 0; q < P.nb; q++)
         bedge[q] = a.bound[a.edges[2 * q]] && a.bound[a.edges[2 * q + 1]];
+    // the tiled variant derives the Dirichlet edges from the lattice: an edge
+    // is Dirichlet iff one of its two transverse node lines is on the surface
+    bool lattice = true;
+    for (int k = 0, q = 0; k < nz && lattice; k++)
+        for (int j = 0; j < ny && lattice; j++)
+            for (int i = 0; i < nx; i++) {
+                const bool bi = i == 0 || i == nx - 1, bj = j == 0 || j == ny - 1,
+                           bk = k == 0 || k == nz - 1;
+                const bool want[3] = {bj || bk, bi || bk, bi || bj};
+                const bool has[3] = {i < nx - 1, j < ny - 1, k < nz - 1};
+                for (int d = 0; d < 3; d++)
+                    if (has[d] && (bool)bedge[q++] != want[d]) lattice = false;
+                if (!lattice) break;
+            }
     // per-cell weights from the materials' mu and sigma
     const int nmat = (int)std::min(a.mu.size(), a.sigma.size());
     std::vector<double> wf((size_t)3 * ncell), wmv((size_t)3 * ncell);
@@ -1946,6 +2006,7 @@ int matfree_build(Survey &V, const MatFreeMesh &a, int kuz, int kpar, int nsm)
     F.nx = nx;
     F.ny = ny;
     F.nz = nz;
+    F.lattice = lattice;
     F.nfx = (long long)nx * (ny - 1) * (nz - 1);
     F.nfy = (long long)(nx - 1) * ny * (nz - 1);
     F.nfz = (long long)(nx - 1) * (ny - 1) * nz;
@@ -2002,8 +2063,40 @@ int matfree_build(Survey &V, const MatFreeMesh &a, int kuz, int kpar, int nsm)
     memcpy(&dm, &mx[0], sizeof(double));
     memcpy(&bm, &mx[1], sizeof(double));
     const double check = bm > 0.0 ? dm / bm : 1.0;
-    if (!(check < 1e-9)) F.release();   // not this matrix's operator: variant off, memory back
+    if (!(check < 1e-9)) {
+        F.release();   // not this matrix's operator: variant off, memory back
+        F.check = check;
+        return MTGPU_OK;
+    }
     F.check = check;
+    MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+    if (F.lattice && !spmv_variant_available(V, kMatFree + 2)) F.lattice = false;
+    if (F.lattice) {
+        // the tiled variant sums in the same order: its product must equal
+        // the two-kernel one to the last bit
+        MTGPU_TRY(cudaMemcpyAsync(V.w, V.z, sizeof(float4) * n, cudaMemcpyDeviceToDevice, V.st));
+        MTGPU_TRY(cudaMemcpyAsync(V.sys, init.data(), sizeof(SysState) * 32, cudaMemcpyHostToDevice, V.st));
+        V.ch = kMatFree + 2;
+        MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+        MTGPU_SP_DISPATCH(V.SP, spmv_only(V));
+        V.ch = ch;
+        MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+        if ((rc = dev_alloc(&d_mx, 2))) return rc;
+        MTGPU_TRY(cudaMemsetAsync(d_mx, 0, sizeof(unsigned long long) * 2, V.st));
+        k_maxdiff<<<4 * nsm, kB, 0, V.st>>>(n, V.z, V.w, d_mx);
+        note_launches(2);
+        err = cudaGetLastError();
+        if (err == cudaSuccess)
+            err = cudaMemcpyAsync(mx, d_mx, sizeof(mx), cudaMemcpyDeviceToHost, V.st);
+        if (err == cudaSuccess) err = cudaStreamSynchronize(V.st);
+        dev_free(d_mx);
+        if (err != cudaSuccess) {
+            set_last_error(err, "tiled matrix-free SpMV set-up check", __FILE__, __LINE__);
+            return MTGPU_ERR_CUDA;
+        }
+        memcpy(&dm, &mx[0], sizeof(double));
+        F.lattice = dm == 0.0;
+    }
     return MTGPU_OK;
 }
 
@@ -2044,6 +2137,7 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
         (rc = dev_alloc(&V.xacc, nv)) || (rc = dev_alloc(&V.all_on, 32)) ||
         (rc = dev_alloc(&V.partials, (size_t)3 * std::max(gmax, nsm * 32) * V.SP)))
         return rc;
+    V.pblocks = std::max(gmax, nsm * 32);
     MTGPU_TRY(cudaMallocHost((void **)&V.hsys, sizeof(SysState) * 32));
     {
         const std::vector<int> ones(32, 1);
@@ -2117,7 +2211,7 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
         MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
     } else {
         const int cand[kSpmvVariants] = {0, 1, 2, 4, 8, kRowVariant + 2, kRowVariant + 4, kMatFree,
-                                         kMatFree + 1};
+                                         kMatFree + 1, kMatFree + 2};
         float best = 1e30f;
         int best_ch = 4;
         for (int c = 0; c < kSpmvVariants; c++) {
@@ -2223,7 +2317,7 @@ int survey_iter_timed(Survey &V, int reps, float *ms)
     MTGPU_TRY(cudaEventCreate(&e1));
     MTGPU_TRY(cudaEventRecord(e0, V.st));
     for (int q = 0; q < reps; q++) MTGPU_SP_DISPATCH(V.SP, iteration(V));
-    note_launches((unsigned long long)reps * ((V.G.m > 0 ? 4 : 3) + (V.ch >= kMatFree ? 1 : 0)));
+    note_launches((unsigned long long)reps * ((V.G.m > 0 ? 4 : 3) + (V.ch == kMatFree || V.ch == kMatFree + 1 ? 1 : 0)));
     MTGPU_TRY(cudaEventRecord(e1, V.st));
     MTGPU_TRY(cudaEventSynchronize(e1));
     MTGPU_TRY(cudaEventElapsedTime(ms, e0, e1));
@@ -2286,18 +2380,39 @@ int upload_flags(int *d, const std::vector<int> &h, cudaStream_t st)
 // accuracy: very low frequencies on fine meshes, where omega sigma_air is
 // ~1e-13 of the curl-curl scale) or that does not reach eps ends with
 // MTGPU_MAXITER; the caller re-solves those in FP64.
-int survey_solve(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, double eps,
-                 int maxiter, int verify, int iters_per_launch, mtgpu_survey_stats *stats)
+//
+// A solve is a sequence of steps so that several batches (groups of up to 32
+// systems, or the systems of different meshes) can run interleaved on their
+// own streams: survey_begin (initial residual, start, graph), then
+// survey_launch (one graph launch if a system is running, asynchronous) and
+// survey_collect (wait, then the host's decisions) until done, then
+// survey_finish.
+namespace {
+constexpr int kMaxContinue = 4;      // continuations after the first stop
+// stalled: the smoothed residual has not halved for max(kStallWindow,
+// iterations before its last halving) iterations (COCR plateaus that end
+// are shorter than the way down to them)
+constexpr int kStallWindow = 1000;
+}  // namespace
+
+void SurveyRun::release()
+{
+    dev_free(d_flag);
+}
+
+int survey_begin(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, double eps,
+                 int maxiter, int verify, int iters_per_launch, SurveyRun &R)
 {
     const long long tot = (long long)V.nb * V.SP;
     const unsigned ge = (unsigned)((tot + kB - 1) / kB);
+    R = SurveyRun{};
+    R.x_out = x_sys_major;
+    R.eps = eps;
+    R.maxiter = maxiter;
+    R.verify = verify;
     V.eps = eps;
     if (iters_per_launch <= 0) iters_per_launch = 16;
-    constexpr int kMaxContinue = 4;      // continuations after the first stop
-    // stalled: the smoothed residual has not halved for max(kStallWindow,
-    // iterations before its last halving) iterations (COCR plateaus that
-    // end are shorter than the way down to them)
-    constexpr int kStallWindow = 1000;
+    R.ipl = iters_per_launch;
     for (int k = 0; k < 32; k++) {
         SysState s{};
         s.status = k < V.S ? kRun : MTGPU_OK;
@@ -2313,131 +2428,154 @@ int survey_solve(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, do
     k_in64<<<ge, kB, 0, V.st>>>(V.nb, V.S, V.SP, x_sys_major, V.xacc);
     note_launches(2);
     MTGPU_TRY(cudaMemsetAsync(V.x, 0, sizeof(float4) * (size_t)tot, V.st));
-    int *d_flag = nullptr;
-    if ((rc = dev_alloc(&d_flag, 32))) return rc;
-    std::vector<int> flag(32, 0), cont(32, 0), final_(32, 0), stalled(32, 0), best_it(32, 0);
-    std::vector<double> last_true(32, 1e300), best(32, 1e300);
-    auto finish = [&](int code) {
-        dev_free(d_flag);
-        return code;
-    };
+    if ((rc = dev_alloc(&R.d_flag, 32))) return rc;
     // inner right-hand side r0 = b - A x0 (FP64), threshold relative to ||b||
-    for (int k = 0; k < 32; k++) flag[k] = k < V.S;
-    if ((rc = upload_flags(d_flag, flag, V.st))) return finish(rc);
-    MTGPU_SP_DISPATCH(V.SP, res64(V, d_flag, 1));
-    if ((rc = sync_sys(V))) return finish(rc);
+    for (int k = 0; k < 32; k++) R.flag[k] = k < V.S;
+    if ((rc = upload_flags(R.d_flag, R.flag, V.st))) return rc;
+    MTGPU_SP_DISPATCH(V.SP, res64(V, R.d_flag, 1));
+    if ((rc = sync_sys(V))) return rc;
     for (int k = 0; k < V.S; k++) {
         SysState &q = V.hsys[k];
         q.checks = 0;
         q.true_rel = -1.0;
         q.eps_k = (q.rnorm > 0.0 && q.bnorm > 0.0) ? eps * q.bnorm / q.rnorm : eps;
     }
-    if ((rc = upload_sys(V))) return finish(rc);
+    if ((rc = upload_sys(V))) return rc;
     MTGPU_SP_DISPATCH(V.SP, start(V));
     MTGPU_TRY(cudaGetLastError());
-    if ((rc = sync_sys(V))) return finish(rc);
-    if (!V.graph || V.graph_iters != iters_per_launch) {
+    if ((rc = sync_sys(V))) return rc;
+    if (!V.graph || V.graph_iters != R.ipl) {
         if (V.graph) cudaGraphExecDestroy(V.graph);
         V.graph = nullptr;
         cudaGraph_t g;
         MTGPU_TRY(cudaStreamBeginCapture(V.st, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < iters_per_launch; k++) MTGPU_SP_DISPATCH(V.SP, iteration(V));
+        for (int k = 0; k < R.ipl; k++) MTGPU_SP_DISPATCH(V.SP, iteration(V));
         // group update: the double-float increment of x goes into the FP64 x
         MTGPU_SP_DISPATCH(V.SP, fold(V, V.all_on));
         MTGPU_TRY(cudaStreamEndCapture(V.st, &g));
         cudaError_t e = cudaGraphInstantiate(&V.graph, g, 0);
         cudaGraphDestroy(g);
         MTGPU_TRY(e);
-        V.graph_iters = iters_per_launch;
+        V.graph_iters = R.ipl;
     }
-    const unsigned long long kpi = (V.G.m > 0 ? 4 : 3) + (V.ch >= kMatFree ? 1 : 0);
-    long long guard = 0;
-    long long guard_max =
-        (long long)maxiter + (long long)(kMaxContinue + 1) * 4 * iters_per_launch + 64;
+    R.guard_max = (long long)maxiter + (long long)(kMaxContinue + 1) * 4 * R.ipl + 64;
     // MTGPU_SURVEY_GUARD_ITERS (environment) lowers the guard: the device
     // stops every system at maxiter, so only this makes the guard's error
     // path run in a test
     if (const char *g = getenv("MTGPU_SURVEY_GUARD_ITERS"))
-        if (atoll(g) > 0) guard_max = std::min(guard_max, atoll(g));
-    for (;;) {
-        bool running = false;
-        for (int k = 0; k < V.S; k++) running |= V.hsys[k].status == kRun;
-        if (running) {
-            cudaError_t e = cudaGraphLaunch(V.graph, V.st);
-            if (e != cudaSuccess) {
-                set_last_error(e, "cudaGraphLaunch", __FILE__, __LINE__);
-                return finish(MTGPU_ERR_CUDA);
-            }
-            note_launches(kpi * (unsigned long long)iters_per_launch + 1);
-            guard += iters_per_launch;
-            if ((rc = sync_sys(V))) return finish(rc);
-            if (guard > guard_max) {
-                set_last_message("survey solve did not finish within its iteration guard");
-                return finish(MTGPU_ERR_TIMEOUT);
-            }
-            bool changed = false;
-            for (int k = 0; k < V.S; k++) {
-                SysState &q = V.hsys[k];
-                if (q.status != kRun) continue;
-                if (q.residual_rel < 0.5 * best[k]) {
-                    best[k] = q.residual_rel;
-                    best_it[k] = q.iter;
-                } else if (q.iter - best_it[k] > std::max(kStallWindow, best_it[k])) {
-                    q.status = MTGPU_MAXITER;   // stalled
-                    stalled[k] = 1;
-                    changed = true;
-                }
-            }
-            if (changed && (rc = upload_sys(V))) return finish(rc);
-            continue;
-        }
-        // every system has stopped: FP64 true residual of those that stopped
-        // on their threshold (first time, or again after further iterations)
-        bool any = false;
-        for (int k = 0; k < 32; k++) {
-            flag[k] = k < V.S && !final_[k] && V.hsys[k].status == MTGPU_OK;
-            any |= flag[k] != 0;
-        }
-        if (!any) break;
-        if ((rc = upload_flags(d_flag, flag, V.st))) return finish(rc);
-        MTGPU_SP_DISPATCH(V.SP, res64(V, d_flag, 0));
-        if ((rc = sync_sys(V))) return finish(rc);
-        bool resume = false;
-        for (int k = 0; k < V.S; k++) {
-            if (!flag[k]) continue;
-            SysState &q = V.hsys[k];
-            if (!verify || q.true_rel < eps) {
-                final_[k] = 1;
-            } else if (q.iter < q.maxiter && cont[k] < kMaxContinue &&
-                       q.true_rel < 0.9 * last_true[k]) {
-                // the Krylov iteration still lowers the true residual: go on,
-                // asking the recurrence for the missing factor (and a margin)
-                cont[k]++;
-                q.eps_k *= fmin(0.9, fmax(0.05, 0.8 * eps / q.true_rel));
-                q.status = kRun;
-                q.iter += 1;
-                resume = true;
-            } else {
-                q.status = MTGPU_MAXITER;   // not converged: left to the caller
-                final_[k] = 1;
-            }
-            last_true[k] = q.true_rel;
-        }
-        if (!resume) break;
-        if ((rc = upload_sys(V))) return finish(rc);
+        if (atoll(g) > 0) R.guard_max = std::min(R.guard_max, atoll(g));
+    return MTGPU_OK;
+}
+
+// one graph launch (asynchronous) if a system is running
+int survey_launch(Survey &V, SurveyRun &R)
+{
+    R.launched = false;
+    if (R.done) return MTGPU_OK;
+    bool running = false;
+    for (int k = 0; k < V.S; k++) running |= V.hsys[k].status == kRun;
+    if (!running) return MTGPU_OK;
+    cudaError_t e = cudaGraphLaunch(V.graph, V.st);
+    if (e != cudaSuccess) {
+        set_last_error(e, "cudaGraphLaunch", __FILE__, __LINE__);
+        return MTGPU_ERR_CUDA;
     }
+    const unsigned long long kpi = (V.G.m > 0 ? 4 : 3) + (V.ch == kMatFree || V.ch == kMatFree + 1 ? 1 : 0);
+    note_launches(kpi * (unsigned long long)R.ipl + 1);
+    R.guard += R.ipl;
+    // the state arrives with the launch's end (read in survey_collect)
+    MTGPU_TRY(cudaMemcpyAsync(V.hsys, V.sys, sizeof(SysState) * 32, cudaMemcpyDeviceToHost, V.st));
+    R.launched = true;
+    return MTGPU_OK;
+}
+
+// the host's decisions after a launch, or, once every system has stopped,
+// the FP64 true residuals and the continuation decisions
+int survey_collect(Survey &V, SurveyRun &R)
+{
+    if (R.done) return MTGPU_OK;
+    int rc;
+    if (R.launched) {
+        MTGPU_TRY(cudaStreamSynchronize(V.st));
+        if (R.guard > R.guard_max) {
+            set_last_message("survey solve did not finish within its iteration guard");
+            return MTGPU_ERR_TIMEOUT;
+        }
+        bool changed = false;
+        for (int k = 0; k < V.S; k++) {
+            SysState &q = V.hsys[k];
+            if (q.status != kRun) continue;
+            if (q.residual_rel < 0.5 * R.best[k]) {
+                R.best[k] = q.residual_rel;
+                R.best_it[k] = q.iter;
+            } else if (q.iter - R.best_it[k] > std::max(kStallWindow, R.best_it[k])) {
+                q.status = MTGPU_MAXITER;   // stalled
+                R.stalled[k] = 1;
+                changed = true;
+            }
+        }
+        if (changed && (rc = upload_sys(V))) return rc;
+        return MTGPU_OK;
+    }
+    // every system has stopped: FP64 true residual of those that stopped
+    // on their threshold (first time, or again after further iterations)
+    bool any = false;
+    for (int k = 0; k < 32; k++) {
+        R.flag[k] = k < V.S && !R.final_[k] && V.hsys[k].status == MTGPU_OK;
+        any |= R.flag[k] != 0;
+    }
+    if (!any) {
+        R.done = true;
+        return MTGPU_OK;
+    }
+    if ((rc = upload_flags(R.d_flag, R.flag, V.st))) return rc;
+    MTGPU_SP_DISPATCH(V.SP, res64(V, R.d_flag, 0));
+    if ((rc = sync_sys(V))) return rc;
+    bool resume = false;
+    for (int k = 0; k < V.S; k++) {
+        if (!R.flag[k]) continue;
+        SysState &q = V.hsys[k];
+        if (!R.verify || q.true_rel < R.eps) {
+            R.final_[k] = 1;
+        } else if (q.iter < q.maxiter && R.cont[k] < kMaxContinue &&
+                   q.true_rel < 0.9 * R.last_true[k]) {
+            // the Krylov iteration still lowers the true residual: go on,
+            // asking the recurrence for the missing factor (and a margin)
+            R.cont[k]++;
+            q.eps_k *= fmin(0.9, fmax(0.05, 0.8 * R.eps / q.true_rel));
+            q.status = kRun;
+            q.iter += 1;
+            resume = true;
+        } else {
+            q.status = MTGPU_MAXITER;   // not converged: left to the caller
+            R.final_[k] = 1;
+        }
+        R.last_true[k] = q.true_rel;
+    }
+    if (!resume) {
+        R.done = true;
+        return MTGPU_OK;
+    }
+    return upload_sys(V);
+}
+
+int survey_finish(Survey &V, SurveyRun &R, mtgpu_survey_stats *stats, int stat_offset)
+{
+    const long long tot = (long long)V.nb * V.SP;
+    const unsigned ge = (unsigned)((tot + kB - 1) / kB);
+    int rc;
     // true residual of the systems that ended without a check
     bool any = false;
     for (int k = 0; k < 32; k++) {
-        flag[k] = k < V.S && V.hsys[k].checks == 0 && V.hsys[k].status != MTGPU_X0_NULL;
-        any |= flag[k] != 0;
+        R.flag[k] = k < V.S && V.hsys[k].checks == 0 && V.hsys[k].status != MTGPU_X0_NULL;
+        any |= R.flag[k] != 0;
     }
     if (any) {
-        if ((rc = upload_flags(d_flag, flag, V.st))) return finish(rc);
-        MTGPU_SP_DISPATCH(V.SP, res64(V, d_flag, 0));
-        if ((rc = sync_sys(V))) return finish(rc);
+        if ((rc = upload_flags(R.d_flag, R.flag, V.st))) return rc;
+        MTGPU_SP_DISPATCH(V.SP, res64(V, R.d_flag, 0));
+        if ((rc = sync_sys(V))) return rc;
     }
-    k_out64<<<ge, kB, 0, V.st>>>(V.nb, V.S, V.SP, V.xacc, V.x, x_sys_major);
+    k_out64<<<ge, kB, 0, V.st>>>(V.nb, V.S, V.SP, V.xacc, V.x, R.x_out);
     note_launches(1);
     MTGPU_TRY(cudaGetLastError());
     MTGPU_TRY(cudaStreamSynchronize(V.st));
@@ -2445,16 +2583,30 @@ int survey_solve(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, do
     for (int k = 0; k < V.S; k++) {
         const SysState &q = V.hsys[k];
         if (stats) {
-            stats->status[k] = q.status;
-            stats->iterations[k] = q.iter;
-            stats->verifications[k] = q.checks;
-            stats->fp64_iterations[k] = 0;
-            stats->true_residual_rel[k] = q.true_rel;
-            stats->residual_rel[k] = q.residual_rel;
+            const int o = stat_offset + k;
+            stats->status[o] = q.status;
+            stats->iterations[o] = q.iter;
+            stats->verifications[o] = q.checks;
+            stats->fp64_iterations[o] = 0;
+            stats->true_residual_rel[o] = q.true_rel;
+            stats->residual_rel[o] = q.residual_rel;
         }
         if (q.status != MTGPU_OK && worst == MTGPU_OK) worst = q.status;
     }
-    return finish(worst);
+    return worst;
+}
+
+int survey_solve(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, double eps,
+                 int maxiter, int verify, int iters_per_launch, mtgpu_survey_stats *stats)
+{
+    SurveyRun R;
+    int rc = survey_begin(V, b_sys_major, x_sys_major, eps, maxiter, verify, iters_per_launch, R);
+    while (!rc && !R.done) {
+        if (!(rc = survey_launch(V, R))) rc = survey_collect(V, R);
+    }
+    if (!rc) rc = survey_finish(V, R, stats, 0);
+    R.release();
+    return rc;
 }
 
 }  // namespace mtgpu

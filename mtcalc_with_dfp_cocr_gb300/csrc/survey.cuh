@@ -25,7 +25,7 @@ struct SysState {
 
 constexpr int kRowVariant = 16;    // + slots in flight: one thread per row, both systems
 constexpr int kMatFree = 32;       // matrix-free SpMV on tensor meshes (+1: two systems per thread)
-constexpr int kSpmvVariants = 9;   // 0, 1, 2, 4, 8, 18, 20, 32, 33
+constexpr int kSpmvVariants = 10;  // 0, 1, 2, 4, 8, 18, 20, 32, 33, 34
 
 // Matrix-free SpMV of a tensor (RegularMeshBuilder) mesh: K = D^T F D with D
 // the edge -> face circulations and F the face mass matrix, M the edge mass
@@ -40,6 +40,7 @@ struct MatFree {
     unsigned char *bedge = nullptr;  // [nb] Dirichlet edges
     float4 *f = nullptr;             // face circulations [faces][SP]
     double check = -1.0;             // set-up check: max |A_mf s - A s| / max |A s|
+    bool lattice = false;            // Dirichlet edges follow the lattice rule (variant 34)
     void release();
 };
 
@@ -57,9 +58,11 @@ struct Survey {
     int tile_T = 1, ntiles = 0, tile_smem = 0, tile_smem_x = 0, g_spmv_t = 0, g_spmv_tx = 0;
     int *uoff = nullptr, *ucol = nullptr;
     unsigned short *lc = nullptr, *lr = nullptr;
-    float tune_ms[kSpmvVariants] = {};   // SpMV times of the variants 0, 1, 2, 4, 8, 18, 20, 32, 33
+    float tune_ms[kSpmvVariants] = {};   // SpMV times of the variants 0, 1, 2, 4, 8, 18, 20, 32, 33, 34
     MatFree mf;
     int g_mff = 0, g_mfe = 0;                    // matrix-free launch grids (faces, edges)
+    int g_mft = 0;                               // tiled matrix-free launch grid (variant 34)
+    int mft[7] = {};                             // its tiles x, y, z chunks, groups, planes per chunk, tile columns x, y
     Folded G;                                    // pattern of G and G^T
     float2 *kc = nullptr, *mc = nullptr, *kr = nullptr;   // double-float K and M per slot
     float *gv32 = nullptr, *tv32 = nullptr;      // values of G and G^T (+-1/2, exact in FP32)
@@ -74,6 +77,7 @@ struct Survey {
     double2 *b64 = nullptr, *xacc = nullptr;      // FP64 b and accumulated x: [row][SP]
     int *all_on = nullptr;                        // 32 flags, all set
     double *partials = nullptr;
+    int pblocks = 0;                              // blocks the partial-sum buffer holds
     cudaGraphExec_t graph = nullptr;
     int graph_iters = 0;
     double eps = 1e-8;
@@ -89,6 +93,7 @@ inline bool spmv_variant_available(const Survey &V, int v)
     if (v == kRowVariant + 2 || v == kRowVariant + 4) return V.SP == 2;
     if (v == kMatFree) return V.mf.on;
     if (v == kMatFree + 1) return V.mf.on && V.SP >= 2;
+    if (v == kMatFree + 2) return V.mf.on && V.mf.lattice && V.g_mft > 0 && V.g_mft <= V.pblocks;
     return false;
 }
 
@@ -117,6 +122,27 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
 // solution out.  verify: continue until the true residual is below eps too.
 int survey_solve(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, double eps,
                  int maxiter, int verify, int iters_per_launch, mtgpu_survey_stats *stats);
+// host state of one batch's solve (survey_begin .. survey_finish)
+struct SurveyRun {
+    double2 *x_out = nullptr;
+    double eps = 1e-8;
+    int maxiter = 0, verify = 0, ipl = 16;
+    int *d_flag = nullptr;
+    std::vector<int> flag = std::vector<int>(32, 0), cont = std::vector<int>(32, 0),
+                     final_ = std::vector<int>(32, 0), stalled = std::vector<int>(32, 0),
+                     best_it = std::vector<int>(32, 0);
+    std::vector<double> last_true = std::vector<double>(32, 1e300),
+                        best = std::vector<double>(32, 1e300);
+    long long guard = 0, guard_max = 0;
+    bool launched = false, done = false;
+    void release();
+};
+int survey_begin(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, double eps,
+                 int maxiter, int verify, int iters_per_launch, SurveyRun &R);
+int survey_launch(Survey &V, SurveyRun &R);
+int survey_collect(Survey &V, SurveyRun &R);
+// stats of the batch's systems at stats arrays [stat_offset ..]
+int survey_finish(Survey &V, SurveyRun &R, mtgpu_survey_stats *stats, int stat_offset);
 int survey_spmv_timed(Survey &V, int reps, float *ms);
 int survey_spmv(Survey &V, const double2 *x_sys_major, double2 *y_sys_major);
 int survey_iter_timed(Survey &V, int reps, float *ms);

@@ -2,11 +2,13 @@
 
 All frequencies x polarisations of a survey share the mesh, hence the
 sparsity pattern and the matrices K and M of A(omega) = K + i omega M.
-Survey solves up to 32 such systems together with the reference's COCR,
-folded preconditioner and MRS stop test, one lane per system, in
-double-float arithmetic (FP32 pairs, 48-bit significand) on the FP32 pipes;
-with verify=True every system also reaches a true relative residual
-||b - A x|| / ||b|| below eps.
+Survey solves such systems together with the reference's COCR, folded
+preconditioner and MRS stop test, one lane per system in batches of up to
+32 (the batches run side by side on streams of their own), in double-float
+arithmetic (FP32 pairs, 48-bit significand) on the FP32 pipes; with
+verify=True every system also reaches a true relative residual
+||b - A x|| / ||b|| below eps.  Survey.multi puts systems of several meshes
+(uneven sizes) in one survey, their vectors packed one after the other.
 
 The reference solves the systems one by one in FP64 (CalcStarter runs
 COCR_FP per frequency and polarisation, Code/CalcStarter/main.cpp:311-325).
@@ -20,21 +22,37 @@ import numpy as np
 from . import _lib
 
 
-SPMV_VARIANTS = (0, 1, 2, 4, 8, 18, 20, 32, 33)   # include/mtgpu.h, mtgpu_survey_tuning
+SPMV_VARIANTS = (0, 1, 2, 4, 8, 18, 20, 32, 33, 34)   # include/mtgpu.h, mtgpu_survey_tuning
 
 
 class Survey:
-    def __init__(self, assembly, nus, stream=None):
+    def __init__(self, assembly, nus, stream=None, _parts=None):
         """assembly: an Assembly; nus: frequency [Hz] of every system."""
-        nus = np.ascontiguousarray(nus, np.float64)
+        parts = _parts if _parts is not None else [(assembly, nus)]
+        self._assemblies = [a for a, _ in parts]
+        counts = np.array([len(n) for _, n in parts], np.int32)
+        nus = np.ascontiguousarray(np.concatenate([np.asarray(n, np.float64) for _, n in parts]))
         self.S = len(nus)
-        self.nb = assembly.nb
-        self._assembly = assembly
+        self.nb = parts[0][0].nb
+        self._assembly = parts[0][0]
         h = C.c_void_p()
         sp = None if stream is None else C.c_void_p(stream.cuda_stream)
-        rc = _lib.lib().mtgpu_survey_create(assembly._h, self.S, nus, sp, C.byref(h))
-        _lib.check(rc, "mtgpu_survey_create")
+        arr = (C.c_void_p * len(parts))(*[a._h.value for a, _ in parts])
+        rc = _lib.lib().mtgpu_survey_create_multi(len(parts), arr, counts, nus, sp, C.byref(h))
+        _lib.check(rc, "mtgpu_survey_create_multi")
         self._h = h
+        off = (C.c_longlong * (self.S + 1))()
+        ng = C.c_int()
+        _lib.check(_lib.lib().mtgpu_survey_info(h, None, C.byref(ng), off), "mtgpu_survey_info")
+        self.offsets = np.array(off[:], np.int64)
+        self.batches = ng.value
+
+    @classmethod
+    def multi(cls, parts, stream=None):
+        """Systems on several meshes: parts = [(assembly, nus), ...].  The
+        right-hand sides and solutions are flat float64 tensors, system k
+        at [offsets[k], offsets[k + 1])."""
+        return cls(None, None, stream, _parts=list(parts))
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -65,7 +83,8 @@ class Survey:
         autotuning; variants 0 and 1 stage x in shared memory per tile,
         18 and 20 (two systems) run one thread per row for both systems, 32
         is the matrix-free SpMV of tensor meshes, 33 the same with two
-        systems per thread."""
+        systems per thread, 34 the same in one tiled kernel with the edge
+        values and face circulations in shared memory."""
         v = C.c_int()
         ms = (C.c_float * len(SPMV_VARIANTS))()
         _lib.check(_lib.lib().mtgpu_survey_tuning(self._h, C.byref(v), ms),
@@ -74,14 +93,17 @@ class Survey:
 
     def set_spmv_variant(self, variant):
         """Pin the SpMV variant (0 x and matrix staged, 1 x staged, 2, 4, 8
-        slots in flight, 18, 20 row per thread for two systems, 32, 33
+        slots in flight, 18, 20 row per thread for two systems, 32, 33, 34
         matrix-free) instead of the autotuned one."""
         _lib.check(_lib.lib().mtgpu_survey_set_spmv_variant(self._h, int(variant)),
                    "mtgpu_survey_set_spmv_variant")
 
     def solve(self, b, x, eps=1e-8, maxiter=20000, verify=True):
-        """b, x: torch CUDA float64 tensors shaped (S, 2 nb); x: initial
-        guesses in, solutions out.  Returns (code, stats dict)."""
+        """b, x: torch CUDA float64 tensors, (S, 2 nb) on one mesh or flat
+        with the packing `offsets`; x: initial guesses in, solutions out.
+        Returns (code, stats dict)."""
+        assert b.is_contiguous() and x.is_contiguous()
+        assert b.numel() == x.numel() == int(self.offsets[-1])
         st = _lib.SurveyStats()
         rc = _lib.lib().mtgpu_survey_solve(self._h, C.c_void_p(b.data_ptr()),
                                            C.c_void_p(x.data_ptr()), float(eps), int(maxiter),

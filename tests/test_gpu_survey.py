@@ -117,7 +117,7 @@ def test_spmv_variants_agree(gpu, name, S):
           np.stack([t[2] for t in tabs]), b)
     sv = survey.Survey(A, nus)
     ref = None
-    for v in (0, 1, 2, 4, 8, 32, 33) + ((18, 20) if S == 2 else ()):
+    for v in (0, 1, 2, 4, 8, 32, 33, 34) + ((18, 20) if S == 2 else ()):
         sv.set_spmv_variant(v)
         x = torch.zeros_like(b)
         code, st = sv.solve(b, x, eps=1e-8, maxiter=20000, verify=True)
@@ -169,7 +169,7 @@ def test_survey_iteration_guard_times_out(gpu, monkeypatch):
     A.close()
 
 
-@pytest.mark.parametrize("variant", [32, 33])
+@pytest.mark.parametrize("variant", [32, 33, 34])
 def test_matfree_operator_on_gradients(gpu, variant):
     """The matrix-free SpMV on discrete gradients x = grad(phi): the curl-curl
     part vanishes (curl grad = 0), so y = i omega M x checks the mass part
@@ -203,3 +203,109 @@ def test_matfree_operator_on_gradients(gpu, variant):
         assert np.max(np.abs(Y[k] - y_ref)) <= 1e-9 * np.max(np.abs(y_ref)), (variant, nu)
     sv.close()
     A.close()
+
+
+@pytest.mark.parametrize("name,S", [("tiny", 1), ("small", 3), ("c1", 2), ("c1", 5), ("small", 32)])
+def test_tiled_matfree_equals_two_kernel_form(gpu, name, S):
+    """Variant 34 (one tiled kernel, edge values and face circulations in
+    shared memory) sums in the order of variant 32 (faces through global
+    memory): the products agree to the last bit, for every layout width
+    (1 to 32 systems) and for tiles that overhang the mesh."""
+    torch = gpu
+    w = workloads.make(name)
+    nus = list(np.logspace(-2, 2, S))
+    A = assembly.Assembly(w.mesh)
+    sv = survey.Survey(A, nus)
+    rng = np.random.default_rng(S)
+    x = torch.tensor(rng.standard_normal((S, 2 * w.mesh.nb)), device="cuda")
+    y32, y34 = torch.empty_like(x), torch.empty_like(x)
+    sv.set_spmv_variant(32)
+    sv.spmv(x, y32)
+    sv.set_spmv_variant(34)
+    sv.spmv(x, y34)
+    assert torch.equal(y32, y34)
+    sv.close()
+    A.close()
+
+
+def _oracle_check(w, nu, alfa, tab, x, x_ref=None):
+    """FP64 true residual of x on the oracle's SLAE, and the oracle's own
+    FP64 solution for the comparison on earth edges."""
+    s = O.assemble(w.mesh, nu, alfa, *tab)
+    rel = np.linalg.norm(s.pr - O.spmv(s, x)) / np.linalg.norm(s.pr)
+    code, x64, _ = O.pcocr(s, slae_io.mesh_to_solve_mesh(w.mesh), nthreads=4)
+    assert code == 0
+    return rel, x64
+
+
+def test_survey_42_systems_in_one_survey(gpu):
+    """The published survey's size (21 frequencies x 2 polarisations, CalcStarter
+    runs them one by one, Code/CalcStarter/main.cpp:311-325) in one survey
+    object: two batches (32 + 10 systems) side by side; every system against
+    the oracle's FP64 solve."""
+    torch = gpu
+    w = workloads.make("small")
+    freqs = np.logspace(-2, 3, 21)
+    systems = [(f, a) for f in freqs for a in (1, 0)]
+    nus = [f for f, _ in systems]
+    tabs = {f: normal1d.solve_1d(f, [l.top for l in w.mesh.layers], [l.sigma for l in w.mesh.layers])
+            for f in freqs}
+    A = assembly.Assembly(w.mesh)
+    b = torch.empty(len(systems), 2 * w.mesh.nb, dtype=torch.float64, device="cuda")
+    A.rhs(nus, [a for _, a in systems], tabs[freqs[0]][0], np.stack([tabs[f][1] for f in nus]),
+          np.stack([tabs[f][2] for f in nus]), b)
+    x = torch.zeros_like(b)
+    sv = survey.Survey(A, nus)
+    assert sv.batches == 2
+    code, st = sv.solve(b, x, eps=1e-8, maxiter=20000, verify=True)
+    assert code == 0, st
+    X = x.cpu().numpy()
+    for k, (f, a) in enumerate(systems):
+        assert st["status"][k] == 0 and st["true_residual_rel"][k] < 1e-8
+        rel, x64 = _oracle_check(w, f, a, tabs[f], X[k])
+        assert rel < 1e-8, (f, a, rel)
+        _assert_close_in_earth(w, X[k], x64)
+    sv.close()
+    A.close()
+
+
+def test_survey_two_meshes_packed(gpu):
+    """Systems of two meshes of different sizes in one survey, their vectors
+    packed one after the other (offsets from the library); every system
+    against the oracle's FP64 solve on its own mesh."""
+    torch = gpu
+    parts = [("tiny", [1.0, 10.0]), ("small", [0.1, 0.1, 10.0])]
+    alfa_of = {("tiny", 0): 1, ("tiny", 1): 0, ("small", 0): 1, ("small", 1): 0, ("small", 2): 1}
+    ws, As, rhs, tabs = [], [], [], []
+    for name, nus in parts:
+        w = workloads.make(name)
+        t = [normal1d.solve_1d(f, [l.top for l in w.mesh.layers], [l.sigma for l in w.mesh.layers])
+             for f in nus]
+        A = assembly.Assembly(w.mesh)
+        b = torch.empty(len(nus), 2 * w.mesh.nb, dtype=torch.float64, device="cuda")
+        al = [alfa_of[(name, k)] for k in range(len(nus))]
+        A.rhs(nus, al, t[0][0], np.stack([q[1] for q in t]), np.stack([q[2] for q in t]), b)
+        ws.append(w)
+        As.append(A)
+        rhs.append(b.reshape(-1))
+        tabs.append(t)
+    sv = survey.Survey.multi([(A, nus) for A, (_, nus) in zip(As, parts)])
+    off = sv.offsets
+    assert off[-1] == sum(r.numel() for r in rhs)
+    b = torch.cat(rhs)
+    x = torch.zeros_like(b)
+    code, st = sv.solve(b, x, eps=1e-8, maxiter=20000, verify=True)
+    assert code == 0, st
+    X = x.cpu().numpy()
+    k = 0
+    for m, (name, nus) in enumerate(parts):
+        for j, nu in enumerate(nus):
+            xk = X[off[k]:off[k + 1]]
+            assert len(xk) == 2 * ws[m].mesh.nb
+            rel, x64 = _oracle_check(ws[m], nu, alfa_of[(name, j)], tabs[m][j], xk)
+            assert rel < 1e-8, (name, nu, rel)
+            _assert_close_in_earth(ws[m], xk, x64)
+            k += 1
+    sv.close()
+    for A in As:
+        A.close()

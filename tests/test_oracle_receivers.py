@@ -226,3 +226,46 @@ def test_driver_table_layout(tmp_path):
     tab = np.loadtxt(out, skiprows=1)
     np.testing.assert_allclose(tab[0], [1, -2, 0.1, 5, 6, 7, 8, 13, 14, 15, 16])
     np.testing.assert_allclose(tab[1], [1, -2, 10.0, 1, 2, 3, 4, 9, 10, 11, 12])
+
+
+def test_impedance_result_files(tmp_path):
+    """calcimpedance's result files and ImpedanceZToEdsAll's edsall0_0_imp
+    from MT records: 4-byte records receiver-major with the frequencies in
+    list order (calcimpedance.for:240-301, 430-465); edsall blocks per type
+    (|Z|, phase, rho_a, rho_a phase), component and receiver with the
+    frequencies reversed and the phases folded (main.cpp:318-347, 578-606).
+    The records come from the oracle's impedance solve on synthetic fields."""
+    from mtcalc_with_dfp_cocr_gb300 import edsall
+    rng = np.random.default_rng(3)
+    freqs = np.array([0.1, 1.0, 10.0])
+    rec = np.array([[100.0, -250.5, 0.0], [1.0e4, 2.0e3, -5.0]])
+    resp = np.zeros((3, 2, 34))
+    for f, nu in enumerate(freqs):
+        for r in range(2):
+            e0, h0, e1, h1 = (rng.standard_normal(3) + 1j * rng.standard_normal(3) for _ in range(4))
+            resp[f, r] = P.mt_response(e0, h0, e1, h1, 2 * np.pi * nu)
+    out = str(tmp_path)
+    names = edsall.write_results(out, freqs, rec, resp)
+    assert {"Zxy", "Fyx", "Rxx", "Fiyy", "Reff", "Fieff", "Wzx", "WFzy", "ZxyRe", "WzyIm"} <= set(names)
+    zxy = edsall.read_result(out, "Zxy", 2, 3)
+    np.testing.assert_allclose(zxy, resp[:, :, 13].T.astype(np.float32))
+    np.testing.assert_allclose(edsall.read_result(out, "Reff", 2, 3), resp[:, :, 28].T.astype(np.float32))
+    lines = open(os.path.join(out, "edsall0_0_imp")).read().splitlines()
+    block = 6 + len(freqs)
+    assert len(lines) == 4 * 4 * 2 * block
+    assert open(os.path.join(out, "ft0_0")).read().split() == [str(t) for t in (1, 2, 3, 4)
+                                                               for _ in range(4 * 2)]
+    # type 1 (|Z|), component xy (the second group of 2 receivers), receiver 1
+    b = lines[(1 * 2 + 1) * block:(1 * 2 + 2) * block]
+    assert b[0] == "10000 2000" and b[1] == "10000 2000 -5"
+    assert b[2:5] == ["1", "1 1 1 1", "1"] and b[5] == "\tnu\tUn\tUa\tUs"
+    rows = [list(map(float, l.split())) for l in b[6:]]
+    np.testing.assert_allclose([r_[0] for r_ in rows], freqs[::-1])
+    np.testing.assert_allclose([r_[2] for r_ in rows], zxy[1, ::-1], rtol=1e-5)
+    assert all(r_[1] == 0.0 and r_[2] == r_[3] for r_ in rows)
+    # type 2 (phase), component yx, receiver 0: -arg Zyx folded as the reference folds it
+    b = lines[(4 * 2 + 2 * 2) * block:(4 * 2 + 2 * 2 + 1) * block]
+    f = edsall.read_result(out, "Fyx", 2, 3)[0, ::-1].astype(np.float64)
+    f[f > 180.0] -= 180.0
+    f[f < -180.0] += 180.0
+    np.testing.assert_allclose([float(l.split()[2]) for l in b[6:]], f, rtol=1e-5, atol=1e-4)
