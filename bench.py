@@ -331,6 +331,7 @@ def gpu_arm(args):
         host[k] = A.block2x2(f, a, t[0], t[1], t[2], eps=eps, maxiter=maxiter)
     h2d = d2h = 0
     e2e_steps = max(1, min(args.steps, 3))
+    e2e_setup = e2e_solve = 0.0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -340,6 +341,8 @@ def gpu_arm(args):
                                                    stop_on_true_residual=True)
             if code != 0:
                 raise RuntimeError(f"e2e solve failed with code {code}")
+            e2e_setup += st.setup_seconds
+            e2e_solve += st.solve_seconds
             h2d += (s.ig.nbytes + s.jg.nbytes + s.idi.nbytes + s.ijg.nbytes + s.di.nbytes +
                     s.gg.nbytes + s.pr.nbytes + xh.nbytes)
             d2h += xh.nbytes
@@ -375,11 +378,17 @@ def gpu_arm(args):
                                "ms_per_launch": spmv64_ms},
         "e2e": {"value": e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d // e2e_steps,
                 "d2h_bytes_per_step": d2h // e2e_steps,
+                "setup_seconds_per_solve": e2e_setup / (e2e_steps * S),
+                "solve_seconds_per_solve": e2e_solve / (e2e_steps * S),
                 "path": "mtgpu_pcocr_2x2_folded_ex(double_float=1, stop_on_true_residual=1), host SLAE buffers"},
         "oracle_parity": oracle_err,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
+    if rank == 0 and world == 1 and not args.no_survey:
+        # the benchmark spec's survey case: 16 frequencies x 2 polarisations on
+        # the headline mesh in one batch, against the plain FP64 COCR
+        out["survey_c2s"] = survey_compare("c2s", 1, 0, setup_device=False)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         import tempfile
         s0 = host[0]
@@ -520,7 +529,7 @@ def reference_arm(args):
     print(json.dumps(out), flush=True)
 
 
-def survey_run(args):
+def survey_compare(name, steps, warmup, setup_device=True):
     """A whole survey in one batch (--survey WORKLOAD, default c2s: the c2
     mesh under 16 frequencies x 2 polarisations = 32 systems): the batched
     double-float solver against the plain FP64 COCR on every system, and the
@@ -529,9 +538,10 @@ def survey_run(args):
     import torch
     from mtcalc_with_dfp_cocr_gb300 import _lib, assembly, receivers, survey, workloads
     from mtcalc_with_dfp_cocr_gb300 import build as B
-    B.build()
-    torch.cuda.set_device(0)
-    w = workloads.make(args.survey)
+    if setup_device:
+        B.build()
+        torch.cuda.set_device(0)
+    w = workloads.make(name)
     systems = w.systems
     S = len(systems)
     tables = make_inputs(w)
@@ -569,13 +579,13 @@ def survey_run(args):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step_batched()
     l0 = _lib.kernel_launches()
     with ClockSampler(0) as clk:
-        ms_b = timed(step_batched, args.steps)
+        ms_b = timed(step_batched, steps)
     launches = _lib.kernel_launches() - l0
-    t_b = ms_b / 1e3 / (args.steps * S)
+    t_b = ms_b / 1e3 / (steps * S)
 
     x64 = torch.zeros_like(rhs)
     plain = {}
@@ -623,9 +633,9 @@ def survey_run(args):
                                 "phase_deg_max": float(ph_err[i].max())}
                 for i, nu in enumerate(freqs)}
     out = {
-        "survey": args.survey, "systems": S, "nb": nb, "receivers": len(w.receivers),
-        "steps": args.steps, "warmup": args.warmup,
-        "batched_s_per_solve": t_b, "batched_ms_per_survey": ms_b / args.steps,
+        "survey": name, "systems": S, "nb": nb, "receivers": len(w.receivers),
+        "steps": steps, "warmup": warmup,
+        "batched_s_per_solve": t_b, "batched_ms_per_survey": ms_b / steps,
         "plain_fp64_s_per_solve": t_p, "plain_fp64_ms_per_survey": ms_p,
         "speedup": t_p / t_b,
         "iterations_batched": {lab(f, a): it for (f, a), it in zip(systems, res["batched"]["iterations"])},
@@ -638,12 +648,15 @@ def survey_run(args):
             "Z_offdiag_rel_max": float(zerr.max()), "Z_diag_rel_to_offdiag_max": float(derr.max()),
             "rho_a_rel_max": float(rho_err.max()), "phase_deg_max": float(ph_err.max()),
             "per_frequency": per_freq},
-        "oracle_parity": oracle_err,
         "gpu_launches": int(launches), "clocks": clk.summary(),
     }
-    print(json.dumps(out), flush=True)
     R.close()
     A.close()
+    return out
+
+
+def survey_run(args):
+    print(json.dumps(survey_compare(args.survey, args.steps, args.warmup)), flush=True)
 
 
 def adjoint_run(args):
@@ -868,6 +881,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-survey", action="store_true",
+                    help="skip the 32-system survey comparison (c2s) of the default run")
     ap.add_argument("--profile", action="store_true",
                     help="short fixed run for ncu captures (see profile_run)")
     ap.add_argument("--workload", default=None, help="workload of --profile (default c3)")

@@ -1,5 +1,8 @@
 // extern "C" entry points of libmtgpu (declared in include/mtgpu.h).
 #include "mtgpu_internal.cuh"
+
+#include <map>
+#include <mutex>
 #include "survey.cuh"
 
 #include <algorithm>
@@ -129,6 +132,26 @@ int mtgpu::make_stream(mtgpu_cocr_s *c, void *stream)
 namespace {
 constexpr double kMu0 = 1.25663706143591729e-6;   // BuildMatrix/stdafx.h:31 (MU_0)
 
+// The SpMV variant the autotuning chose, per sparsity pattern and mesh, for
+// the reference-facing entry point: a drop-in caller solves one system per
+// call (every frequency and polarisation of a survey on the same mesh), so
+// the tuning of the first call serves the others.  The key samples the
+// pattern and the mesh; a new pattern with the same key would only be
+// solved with another variant than its own tuning might pick (every variant
+// computes the same operator).
+std::mutex g_tune_mu;
+std::map<std::vector<long long>, int> g_tuned;
+
+std::vector<long long> pattern_key(int nb, const int *ig, const int *jg, int kpar, int n_nodes_c,
+                                   const int *nver14, const double *xyz)
+{
+    std::vector<long long> k{nb, ig[nb], kpar, n_nodes_c, xyz != nullptr};
+    const long long nnz = ig[nb];
+    for (int t = 0; t < 64 && nnz > 0; t++) k.push_back(jg[(nnz - 1) * t / 63]);
+    for (int t = 0; t < 16 && kpar > 0; t++) k.push_back(nver14[(size_t)((kpar - 1) * (long long)t / 15) * 14]);
+    return k;
+}
+
 // One system through the double-float survey solver: K = Re A, M = Im A,
 // omega = 1, so A = K + i M exactly.
 int solve_double_float_host(int nb, const int *ig, const int *jg, const int *idi, const int *ijg,
@@ -180,7 +203,18 @@ int solve_double_float_host(int nb, const int *ig, const int *jg, const int *idi
             mm.idi = idi;
             mm.di = di;
         }
-        rc = survey_setup(P, mesh, 1, &one, V, st, nullptr, xyz ? &mm : nullptr);
+        const std::vector<long long> key = pattern_key(nb, ig, jg, kpar, n_nodes_c, nver14, xyz);
+        int pin = -1;
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            auto it = g_tuned.find(key);
+            if (it != g_tuned.end()) pin = it->second;
+        }
+        rc = survey_setup(P, mesh, 1, &one, V, st, nullptr, xyz ? &mm : nullptr, pin);
+        if (!rc && pin < 0) {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            g_tuned[key] = V.ch;
+        }
     }
     if (!rc && !(rc = upload(&db, (const double2 *)pr, nb, st)) &&
         !(rc = upload(&dx, (const double2 *)x, nb, st))) {

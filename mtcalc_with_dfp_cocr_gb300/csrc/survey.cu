@@ -2103,7 +2103,8 @@ int matfree_build(Survey &V, const MatFreeMesh &a, int kuz, int kpar, int nsm)
 }  // namespace
 
 int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const double *omega,
-                 Survey &V, cudaStream_t st, const mtgpu_assembly_s *a, const MatFreeMesh *mfm)
+                 Survey &V, cudaStream_t st, const mtgpu_assembly_s *a, const MatFreeMesh *mfm,
+                 int pin_variant)
 {
     V.release();
     MTGPU_CHECK_ARG(S >= 1 && S <= 32, "a survey batch holds 1 to 32 systems");
@@ -2208,6 +2209,9 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
     const char *pin = getenv("MTGPU_SPMV_VARIANT");
     if (pin && *pin && spmv_variant_available(V, atoi(pin))) {
         V.ch = atoi(pin);
+        MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+    } else if (pin_variant >= 0 && spmv_variant_available(V, pin_variant)) {
+        V.ch = pin_variant;
         MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
     } else {
         const int cand[kSpmvVariants] = {0, 1, 2, 4, 8, kRowVariant + 2, kRowVariant + 4, kMatFree,

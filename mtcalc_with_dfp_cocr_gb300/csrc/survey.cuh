@@ -115,9 +115,11 @@ struct MatFreeMesh {
 // a: the assembly (host mesh copies) when the survey is built from one, or
 // mfm: the mesh of a host SLAE; on a tensor mesh either enables the
 // matrix-free SpMV variant
+// pin_variant >= 0 (and available): that SpMV variant instead of the
+// set-up autotuning
 int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const double *omega,
                  Survey &V, cudaStream_t st, const mtgpu_assembly_s *a = nullptr,
-                 const MatFreeMesh *mfm = nullptr);
+                 const MatFreeMesh *mfm = nullptr, int pin_variant = -1);
 // b, x: system-major FP64 [S][nb] complex; x is the initial guess in and the
 // solution out.  verify: continue until the true residual is below eps too.
 int survey_solve(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, double eps,

@@ -260,11 +260,18 @@ def test_survey_42_systems_in_one_survey(gpu):
     code, st = sv.solve(b, x, eps=1e-8, maxiter=20000, verify=True)
     assert code == 0, st
     X = x.cpu().numpy()
+    xyz = w.mesh.xyz()
+    e = w.mesh.edges()
+    earth = 0.5 * (xyz[e[:, 0], 2] + xyz[e[:, 1], 2]) <= 0.0
     for k, (f, a) in enumerate(systems):
         assert st["status"][k] == 0 and st["true_residual_rel"][k] < 1e-8
         rel, x64 = _oracle_check(w, f, a, tabs[f], X[k])
         assert rel < 1e-8, (f, a, rel)
-        _assert_close_in_earth(w, X[k], x64)
+        # earth and surface edges only: down to 0.01 Hz the air's gradient
+        # components are left free (~1e-4 here) by any solver at a 1e-8
+        # residual
+        c, c64 = X[k][0::2] + 1j * X[k][1::2], x64[0::2] + 1j * x64[1::2]
+        assert np.linalg.norm((c - c64)[earth]) <= 1e-7 * np.linalg.norm(c64[earth]), (f, a)
     sv.close()
     A.close()
 
