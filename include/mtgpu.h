@@ -215,6 +215,21 @@ typedef struct mtgpu_assembly_s mtgpu_assembly;
 
 int mtgpu_assembly_create(const mtgpu_fem_mesh *mesh, mtgpu_assembly **out);
 
+/* The same assembly for a regular (tensor-product) mesh given by its node
+ * lines x[nx], y[ny], z[nz] (ascending): the mesh tables (node coordinates,
+ * cell nodes and edges, edge nodes, Dirichlet flags of the outer surface)
+ * are generated on the device with RegularMeshBuilder's numbering
+ * (Code/RegularMeshBuilder/main.cpp:923-1032: nodes x fastest, edges per
+ * node +x, +y, +z; the outer surface Dirichlet, :1706-1736) instead of being
+ * built and uploaded by the caller.  cell_material[(nx-1)(ny-1)(nz-1)]
+ * (0-based, cells x fastest); mu, sigma, sigma0 per material as in
+ * mtgpu_fem_mesh.  The result equals mtgpu_assembly_create's on the tables
+ * RegularMeshBuilder writes for the same lines. */
+int mtgpu_assembly_create_regular(int nx, int ny, int nz, const double *x, const double *y,
+                                  const double *z, const int *cell_material, int n_materials,
+                                  const double *mu, const double *sigma, const double *sigma0,
+                                  mtgpu_assembly **out);
+
 /* Sizes of the assembled system: full-storage complex/real entries, and the
  * lower-triangle block format (nnz_lower = ig[nb], gg_len = ijg[nnz_lower]). */
 int mtgpu_assembly_info(const mtgpu_assembly *a, long long *nnz_complex, long long *nnz_real,

@@ -97,6 +97,8 @@ SIGNATURES = {
     "mtgpu_cocr_info": (C.c_int, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
                                   C.POINTER(C.c_int)]),
     "mtgpu_cocr_destroy": (None, [_vp]),
+    "mtgpu_assembly_create_regular": (C.c_int, [C.c_int, C.c_int, C.c_int, _d, _d, _d, _i, C.c_int,
+                                                _d, _d, _d, C.POINTER(_vp)]),
     "mtgpu_assembly_create": (C.c_int, [C.POINTER(FemMesh), C.POINTER(_vp)]),
     "mtgpu_assembly_info": (C.c_int, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
                                       C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),

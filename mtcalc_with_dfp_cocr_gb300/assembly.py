@@ -21,19 +21,37 @@ MU_0 = 1.25663706143591729e-6   # Code/BuildMatrix/stdafx.h:31
 
 
 class Assembly:
-    def __init__(self, mesh, cell_sigma=None):
+    def __init__(self, mesh, cell_sigma=None, tables="device"):
         """mesh: a RegularMesh (mesh.py).  cell_sigma: optional conductivity
         of every cell (unrounded); then every cell is its own material, with
-        the mesh's background conductivity as its sigma0."""
+        the mesh's background conductivity as its sigma0.  tables: "device"
+        generates the mesh tables on the GPU from the node lines
+        (mtgpu_assembly_create_regular); "host" builds them here and uploads
+        them (mtgpu_assembly_create), as for a mesh read from files."""
         L = _lib.lib()
-        nver = np.ascontiguousarray(mesh.cell_nodes(), np.int32)
-        ed = np.ascontiguousarray(mesh.cell_edges(), np.int32)
         if cell_sigma is None:
             nvkat, sig, sig0 = mesh.nvkat, mesh.mat_sigma, mesh.mat_sigma0
         else:
             sig = np.asarray(cell_sigma, np.float64).reshape(mesh.kpar)
             nvkat = np.arange(mesh.kpar, dtype=np.int32)
             sig0 = mesh.cell_sigma0
+        self.nb = mesh.nb
+        if tables == "device":
+            f = lambda v: np.ascontiguousarray(v, np.float64)
+            self._arrays = dict(nvkat=np.ascontiguousarray(nvkat, np.int32), sigma=f(sig),
+                                sigma0=f(sig0), mu=np.full(len(sig), MU_0))
+            a = self._arrays
+            h = C.c_void_p()
+            _lib.check(L.mtgpu_assembly_create_regular(
+                mesh.nx, mesh.ny, mesh.nz, f(mesh.x), f(mesh.y), f(mesh.z), a["nvkat"],
+                len(a["sigma"]), a["mu"], a["sigma"], a["sigma0"], C.byref(h)),
+                "mtgpu_assembly_create_regular")
+            self._h = h
+            return
+        if tables != "host":
+            raise ValueError(f"tables must be 'device' or 'host', not {tables!r}")
+        nver = np.ascontiguousarray(mesh.cell_nodes(), np.int32)
+        ed = np.ascontiguousarray(mesh.cell_edges(), np.int32)
         self._arrays = dict(
             xyz=np.ascontiguousarray(mesh.xyz(), np.float64), nver=nver, ed=ed,
             edges=np.ascontiguousarray(mesh.edges(), np.int32),
@@ -50,7 +68,6 @@ class Assembly:
         h = C.c_void_p()
         _lib.check(L.mtgpu_assembly_create(C.byref(fm), C.byref(h)), "mtgpu_assembly_create")
         self._h = h
-        self.nb = mesh.nb
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:

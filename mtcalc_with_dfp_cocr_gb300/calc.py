@@ -19,6 +19,10 @@ the reference's last step: calcimpedance's 4-byte result files (|Z|, phases,
 rho_a, effective rho_a, the Wiese-Parkinson tipper and the complex values)
 and ImpedanceZToEdsAll's edsall0_0_imp / ft0_0 (edsall.py).
 
+Under torchrun (one process per GPU) the frequencies are split across the
+ranks in contiguous blocks and rank 0 gathers the responses and writes the
+files: the systems share no data, so no collective runs during the solves.
+
 The table has the layout of the reference's published results
 (CalculationResults/625_500_reg_R_Z.txt): per receiver and period,
 northing, easting, period, |Zxx| |Zxy| |Zyx| |Zyy| (Ohm) and the apparent
@@ -38,11 +42,59 @@ import numpy as np
 from . import edsall, meshbuilder, normal1d
 from .receivers import MT_RHO, MT_ZABS
 
+def rank_frequencies(nf, rank, world):
+    """The frequencies rank `rank` of `world` solves: contiguous, balanced
+    blocks (frequencies share no data, so a survey splits across GPUs
+    without any exchange until the responses are gathered)."""
+    base, extra = divmod(nf, world)
+    lo = rank * base + min(rank, extra)
+    return list(range(lo, lo + base + (1 if rank < extra else 0)))
+
+
+def gather_responses(local, idx, nf):
+    """Every rank's responses [len(idx)][nrec][34] of frequencies idx into
+    the survey's [nf][nrec][34] on rank 0 (None on the others), through
+    torch.distributed (any backend; the data are a few KB per frequency)."""
+    import torch.distributed as dist
+    parts = [None] * dist.get_world_size()
+    dist.all_gather_object(parts, (list(idx), np.asarray(local)))
+    if dist.get_rank() != 0:
+        return None
+    out = None
+    for ids, arr in parts:
+        if out is None and len(ids):
+            out = np.empty((nf,) + arr.shape[1:], arr.dtype)
+        for k, i in enumerate(ids):
+            out[i] = arr[k]
+    return out
+
+
 def run(case, eps=None, maxiter=None, device="cuda", log=None, output="smooth"):
     """Solve every frequency x polarisation of `case`; returns
     (responses [nf][nrec][34], stats dict).  output: "smooth", the
     reference's default receiver output (subdomain smoothing), or "direct"
-    (receivers.py)."""
+    (receivers.py).  Under torch.distributed (one process per GPU) every
+    rank solves its block of frequencies (rank_frequencies) and rank 0
+    returns the whole survey's responses (the others None, None)."""
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        import dataclasses
+        idx = rank_frequencies(len(case.freqs), dist.get_rank(), dist.get_world_size())
+        sub = dataclasses.replace(case, freqs=np.asarray(case.freqs, np.float64)[idx])
+        if idx:
+            resp, stats = run_local(sub, eps, maxiter, device, log, output)
+        else:
+            resp, stats = np.zeros((0, len(case.receivers), 34)), {"systems": []}
+        stats["frequencies"] = idx
+        allstats = [None] * dist.get_world_size()
+        dist.all_gather_object(allstats, stats)
+        full = gather_responses(resp, idx, len(case.freqs))
+        return full, ({"ranks": allstats} if dist.get_rank() == 0 else None)
+    return run_local(case, eps, maxiter, device, log, output)
+
+
+def run_local(case, eps=None, maxiter=None, device="cuda", log=None, output="smooth"):
+    """run() on this process's GPU for all of case's frequencies."""
     import torch
     from .assembly import Assembly
     from .receivers import Receivers
@@ -126,8 +178,15 @@ def main(argv=None):
                          "direct evaluation of the edge basis at the receiver")
     a = ap.parse_args(argv)
     case = meshbuilder.read_case(a.case)
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1:   # torchrun: one process per GPU
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
     resp, stats = run(case, a.eps, a.maxiter, log=lambda s: print(s, file=sys.stderr),
                       output=a.output)
+    if resp is None:   # ranks other than 0
+        return
     out = a.out or os.path.join(a.case, "results_R_Z.txt")
     write_table(out, case, resp)
     if a.results != "-":

@@ -467,15 +467,32 @@ int param_assemble(const mtgpu_fem_mesh &m, ParamMatrix &P, cudaStream_t st)
         (rc = up(&P.d_sig, m.sigma, (size_t)m.n_materials, st)) ||
         (rc = up(&P.d_sig0, m.sigma0, (size_t)m.n_materials, st)))
         return rc;
-    // Dirichlet edges: both nodes on the boundary (bound_cond_vec_harm.cpp:81-108)
     unsigned char *bnode = nullptr;
     int *d_bnd = nullptr;
-    if ((rc = dev_alloc(&bnode, m.kuzlov)) || (rc = dev_alloc(&P.d_bedge, nb))) return rc;
+    if ((rc = dev_alloc(&bnode, m.kuzlov))) return rc;
     MTGPU_TRY(cudaMemsetAsync(bnode, 0, m.kuzlov, st));
     if (m.n_bound > 0) {
-        if ((rc = up(&d_bnd, m.bound_nodes, (size_t)m.n_bound, st))) return rc;
+        if ((rc = up(&d_bnd, m.bound_nodes, (size_t)m.n_bound, st))) {
+            dev_free(bnode);
+            return rc;
+        }
         k_bnode<<<ceil_div(m.n_bound, kThreads), kThreads, 0, st>>>(m.n_bound, d_bnd, bnode);
     }
+    rc = param_build(P, bnode, st);
+    dev_free(bnode);
+    dev_free(d_bnd);
+    return rc;
+}
+
+// The device part of the assembly, from the mesh tables in P (d_xyz,
+// d_nver, d_ed, d_edges, d_nvkat, the materials) and the Dirichlet node
+// flags bnode[kuzlov]
+int param_build(ParamMatrix &P, const unsigned char *bnode, cudaStream_t st)
+{
+    const int nb = P.nb, kpar = P.kpar;
+    int rc;
+    // Dirichlet edges: both nodes on the boundary (bound_cond_vec_harm.cpp:81-108)
+    if ((rc = dev_alloc(&P.d_bedge, nb))) return rc;
     k_bedge<<<ceil_div(nb, kThreads), kThreads, 0, st>>>(nb, P.d_edges, bnode, P.d_bedge);
     // edge -> cells
     int *cnt = nullptr, *fill = nullptr, *overflow = nullptr;
@@ -486,7 +503,7 @@ int param_assemble(const mtgpu_fem_mesh &m, ParamMatrix &P, cudaStream_t st)
     MTGPU_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * (nb + 1), st));
     MTGPU_TRY(cudaMemsetAsync(fill, 0, sizeof(int) * nb, st));
     MTGPU_TRY(cudaMemsetAsync(overflow, 0, sizeof(int), st));
-    k_ec_count<<<ceil_div(kpar, kThreads), kThreads, 0, st>>>(kpar, P.d_ed, m.ed_stride, cnt);
+    k_ec_count<<<ceil_div(kpar, kThreads), kThreads, 0, st>>>(kpar, P.d_ed, P.ed_stride, cnt);
     {
         // cnt[e+1] holds the count of edge e; ptr = inclusive scan
         std::vector<int> h(nb + 1);
@@ -497,7 +514,7 @@ int param_assemble(const mtgpu_fem_mesh &m, ParamMatrix &P, cudaStream_t st)
         MTGPU_TRY(cudaMemcpyAsync(P.d_ec_ptr, h.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice, st));
         MTGPU_TRY(cudaStreamSynchronize(st));
     }
-    k_ec_fill<<<ceil_div(kpar, kThreads), kThreads, 0, st>>>(kpar, P.d_ed, m.ed_stride, P.d_ec_ptr,
+    k_ec_fill<<<ceil_div(kpar, kThreads), kThreads, 0, st>>>(kpar, P.d_ed, P.ed_stride, P.d_ec_ptr,
                                                               fill, P.d_ec_cell);
     k_ec_sort<<<ceil_div(nb, kThreads), kThreads, 0, st>>>(nb, P.d_ec_ptr, P.d_ec_cell);
     // pattern
@@ -509,7 +526,7 @@ int param_assemble(const mtgpu_fem_mesh &m, ParamMatrix &P, cudaStream_t st)
         return rc;
     MTGPU_TRY(cudaMemsetAsync(tot, 0, 2 * sizeof(unsigned long long), st));
     k_row_counts<<<ceil_div(nb, 128), 128, 0, st>>>(nb, P.d_ec_ptr, P.d_ec_cell, P.d_ed,
-                                                    m.ed_stride, P.d_nc, P.d_nr, overflow);
+                                                    P.ed_stride, P.d_nc, P.d_nr, overflow);
     k_widths2<<<ceil_div(P.nslices, kThreads), kThreads, 0, st>>>(nb, P.nslices, P.d_nc, P.d_nr,
                                                                    P.d_wc, P.d_wr, tot);
     MTGPU_TRY(cudaGetLastError());
@@ -521,7 +538,7 @@ int param_assemble(const mtgpu_fem_mesh &m, ParamMatrix &P, cudaStream_t st)
     MTGPU_TRY(cudaMemcpyAsync(htot, tot, sizeof(htot), cudaMemcpyDeviceToHost, st));
     MTGPU_TRY(cudaMemcpyAsync(&hover, overflow, sizeof(int), cudaMemcpyDeviceToHost, st));
     MTGPU_TRY(cudaStreamSynchronize(st));
-    dev_free(cnt); dev_free(fill); dev_free(tot); dev_free(overflow); dev_free(bnode); dev_free(d_bnd);
+    dev_free(cnt); dev_free(fill); dev_free(tot); dev_free(overflow);
     MTGPU_CHECK_ARG(hover == 0, "a matrix row has more than 64 distinct columns");
     std::vector<long long> pc(P.nslices + 1), pr(P.nslices + 1);
     pc[0] = pr[0] = 0;
@@ -540,7 +557,7 @@ int param_assemble(const mtgpu_fem_mesh &m, ParamMatrix &P, cudaStream_t st)
         (rc = dev_alloc(&P.d_kr, P.len_r)))
         return rc;
     k_row_fill<<<P.nslices * kSlice / 128 + 1, 128, 0, st>>>(
-        nb, P.nslices, P.d_ec_ptr, P.d_ec_cell, P.d_ed, m.ed_stride, P.d_nver, m.nver_stride,
+        nb, P.nslices, P.d_ec_ptr, P.d_ec_cell, P.d_ed, P.ed_stride, P.d_nver, P.nver_stride,
         P.d_xyz, P.d_nvkat, P.d_mu, P.d_sig, P.d_bedge, P.d_wc, P.d_wr, P.d_pc, P.d_pr,
         P.d_col_c, P.d_kc, P.d_mc, P.d_col_r, P.d_kr);
     MTGPU_TRY(cudaGetLastError());

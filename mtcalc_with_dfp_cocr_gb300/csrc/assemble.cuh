@@ -38,6 +38,13 @@ struct Block2x2Dev {
 };
 
 int param_assemble(const mtgpu_fem_mesh &m, ParamMatrix &P, cudaStream_t st);
+// the device part: P's mesh tables and sizes set, bnode[kuzlov] the Dirichlet node flags
+int param_build(ParamMatrix &P, const unsigned char *bnode, cudaStream_t st);
+// a regular mesh from its node lines: every table generated on the device (regular_mesh.cu)
+int param_assemble_regular(int nx, int ny, int nz, const double *x, const double *y,
+                           const double *z, const int *cell_material, int n_materials,
+                           const double *mu, const double *sigma, const double *sigma0,
+                           ParamMatrix &P, cudaStream_t st);
 // rhs[k] for S systems (omega, alfa, 1-D tables usin/ucos [S][n1d] on z1d);
 // layout: interleaved ? rhs[e * S + k] : rhs[k * rhs_stride + e]
 int param_rhs(const ParamMatrix &P, int S, const double *d_omega, const int *d_alfa, int n1d,

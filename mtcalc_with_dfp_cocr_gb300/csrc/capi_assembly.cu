@@ -51,6 +51,58 @@ int mtgpu_assembly_create(const mtgpu_fem_mesh *mesh, mtgpu_assembly **out)
     return MTGPU_OK;
 }
 
+int mtgpu_assembly_create_regular(int nx, int ny, int nz, const double *x, const double *y,
+                                  const double *z, const int *cell_material, int n_materials,
+                                  const double *mu, const double *sigma, const double *sigma0,
+                                  mtgpu_assembly **out)
+{
+    MTGPU_CHECK_ARG(out != nullptr, "null argument");
+    *out = nullptr;
+    auto *a = new mtgpu_assembly_s();
+    cudaError_t e = cudaStreamCreateWithFlags(&a->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete a;
+        set_last_error(e, "cudaStreamCreateWithFlags", __FILE__, __LINE__);
+        return MTGPU_ERR_CUDA;
+    }
+    int rc = param_assemble_regular(nx, ny, nz, x, y, z, cell_material, n_materials, mu, sigma,
+                                    sigma0, a->P, a->st);
+    if (rc) {
+        mtgpu_assembly_destroy(a);
+        return rc;
+    }
+    // host copies for the host-side set-up (preconditioner pattern, matrix-free
+    // tables, receiver location): the device's own tables, read back once
+    const ParamMatrix &P = a->P;
+    a->nver_stride = 8;
+    a->nver.resize((size_t)P.kpar * 8);
+    a->xyz.resize((size_t)P.kuzlov * 3);
+    a->edges.resize((size_t)P.nb * 2);
+    a->nvkat.assign(cell_material, cell_material + P.kpar);
+    auto dn = [&](void *h, const void *d, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, a->st);
+    };
+    dn(a->nver.data(), P.d_nver, sizeof(int) * a->nver.size());
+    dn(a->xyz.data(), P.d_xyz, sizeof(double) * a->xyz.size());
+    dn(a->edges.data(), P.d_edges, sizeof(int) * a->edges.size());
+    if (e == cudaSuccess) e = cudaStreamSynchronize(a->st);
+    if (e != cudaSuccess) {
+        set_last_error(e, "mtgpu_assembly_create_regular", __FILE__, __LINE__);
+        mtgpu_assembly_destroy(a);
+        return MTGPU_ERR_CUDA;
+    }
+    a->bound.assign(P.kuzlov, 0);
+    for (int k = 0, n = 0; k < nz; k++)
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++, n++)
+                a->bound[n] = i == 0 || j == 0 || k == 0 || i == nx - 1 || j == ny - 1 || k == nz - 1;
+    a->sigflag.resize(n_materials);
+    for (int i = 0; i < n_materials; i++) a->sigflag[i] = sigma[i] == 0.0 ? 0.0 : 1.0;
+    a->ig_t.assign(P.kuzlov + 1, 0);
+    *out = a;
+    return MTGPU_OK;
+}
+
 void mtgpu_assembly_destroy(mtgpu_assembly *a)
 {
     if (!a) return;

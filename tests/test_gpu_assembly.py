@@ -65,4 +65,32 @@ def test_assembly_rejects_bad_mesh(gpu):
     w.mesh.nvkat = w.mesh.nvkat.copy()
     w.mesh.nvkat[3] = 99
     with pytest.raises(_lib.MtgpuError, match="nvkat"):
-        assembly.Assembly(w.mesh)
+        assembly.Assembly(w.mesh, tables="host")
+    with pytest.raises(_lib.MtgpuError, match="cell material out of range"):
+        assembly.Assembly(w.mesh, tables="device")
+
+
+@pytest.mark.parametrize("name", ["small", "c1"])
+def test_device_mesh_tables_equal_host_tables(gpu, name):
+    """The mesh tables generated on the device from the node lines
+    (RegularMeshBuilder's numbering) give the same assembly, bit for bit, as
+    the tables built on the host and uploaded: the SLAE in the reference's
+    block format and the right-hand sides of both polarisations."""
+    torch = gpu
+    w = workloads.make(name)
+    nu = 1.0
+    z, us, uc = normal1d.solve_1d(nu, [l.top for l in w.mesh.layers], [l.sigma for l in w.mesh.layers])
+    Ad = assembly.Assembly(w.mesh, tables="device")
+    Ah = assembly.Assembly(w.mesh, tables="host")
+    for alfa in (1, 0):
+        sd = Ad.block2x2(nu, alfa, z, us, uc)
+        sh = Ah.block2x2(nu, alfa, z, us, uc)
+        for f in ("ig", "jg", "idi", "ijg", "di", "gg", "pr"):
+            assert np.array_equal(getattr(sd, f), getattr(sh, f)), f
+    bd = torch.empty(2, 2 * w.mesh.nb, dtype=torch.float64, device="cuda")
+    bh = torch.empty_like(bd)
+    Ad.rhs([nu, nu], [1, 0], z, np.stack([us, us]), np.stack([uc, uc]), bd)
+    Ah.rhs([nu, nu], [1, 0], z, np.stack([us, us]), np.stack([uc, uc]), bh)
+    assert torch.equal(bd, bh)
+    Ad.close()
+    Ah.close()
