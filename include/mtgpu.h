@@ -344,8 +344,11 @@ int mtgpu_survey_spmv(mtgpu_survey *s, const double *d_x, double *d_y);
  * 33: the same with two systems per thread, batches of 2 or more; 34: the
  * same operator in one kernel per launch, a block marching through the node
  * planes of its tile with the edge values and face circulations in shared
- * memory, bit-for-bit equal to 32) and the times it measured for the
- * variants 0, 1, 2, 4, 8, 18, 20, 32, 33, 34 (ms[10]: ms
+ * memory, bit-for-bit equal to 32; 35: the curl-curl part as D^T (F f), the
+ * face mass matrix applied once per face and each row the signed sum over
+ * its 4 faces, enabled where its set-up product agrees with 32's to 1e-12)
+ * and the times it measured for the variants 0, 1, 2, 4, 8, 18, 20, 32, 33,
+ * 34, 35 (ms[11]: ms
  * per whole iteration with that variant, so that each SpMV sees the cache as
  * the other kernels of an iteration leave it; 0 where a variant was not
  * available). */
@@ -355,7 +358,7 @@ int mtgpu_survey_tuning(const mtgpu_survey *s, int *variant, float *ms);
  * (for profiler runs: a profiler serialises and cold-starts every launch, and
  * would make the autotuning choose differently from a plain run). */
 
-/* Pins the SpMV variant (0, 1, 2, 4, 8, 18, 20, 32, 33 or 34) instead of the
+/* Pins the SpMV variant (0, 1, 2, 4, 8, 18, 20, 32, 33, 34 or 35) instead of the
  * autotuned choice.  The stored-matrix variants sum the same products in the
  * same order; the matrix-free one computes the same operator in another
  * order (it is enabled only where a set-up product agrees with the stored
@@ -363,7 +366,8 @@ int mtgpu_survey_tuning(const mtgpu_survey *s, int *variant, float *ms);
  * for this survey (0 and 1 need their tiles to fit shared memory, 18 and 20
  * two systems, 32 a survey created from an assembly of a tensor mesh with
  * RegularMeshBuilder's numbering and all outer nodes Dirichlet, 33 that and
- * at least two systems, 34 that and no Dirichlet node inside the mesh). */
+ * at least two systems, 34 that and no Dirichlet node inside the mesh, 35 a
+ * matrix-free survey whose set-up check passed). */
 int mtgpu_survey_set_spmv_variant(mtgpu_survey *s, int variant);
 
 void mtgpu_survey_destroy(mtgpu_survey *s);

@@ -65,8 +65,10 @@ void MatFree::release()
     dev_free(bedge);
     dev_free(w);
     dev_free(f);
+    dev_free(g);
     on = false;
     lattice = false;
+    gface = false;
 }
 
 namespace {
@@ -701,6 +703,7 @@ struct MF {
     const float2 *w;
     const unsigned char *bedge;
     float4 *f;
+    float4 *g;                 // F f (variant 35)
 };
 
 // edge of direction d leaving node (i, j, k): the node's first edge
@@ -1013,19 +1016,23 @@ k_mf_edges2(int nb, MF M, const float2 *__restrict__ omega, const float4 *__rest
                 if (on[u]) tail[u].row(i + u, y[u], sv[u], r, z, sm);
         }
     }
-    __shared__ double stage[3][SP];
-    for (int t = threadIdx.x; t < 3 * SP; t += kB) (&stage[0][0])[t] = 0.0;
-    __syncthreads();
+    // per-system sums in a fixed order (run-to-run identical): every
+    // thread's partials staged, then thread k < SP adds those of system k
+    // over the block's threads in thread order
+    __shared__ double stage[3][2][kB];
 #pragma unroll
     for (int u = 0; u < 2; u++) {
-        atomicAdd(&stage[0][k0 + u], tail[u].zsr.to_double());
-        atomicAdd(&stage[1][k0 + u], tail[u].zsi.to_double());
-        atomicAdd(&stage[2][k0 + u], tail[u].nn.to_double());
+        stage[0][u][threadIdx.x] = tail[u].zsr.to_double();
+        stage[1][u][threadIdx.x] = tail[u].zsi.to_double();
+        stage[2][u][threadIdx.x] = tail[u].nn.to_double();
     }
     __syncthreads();
     double v[3] = {0.0, 0.0, 0.0};
-    if (threadIdx.x < SP)
-        for (int n = 0; n < 3; n++) v[n] = stage[n][threadIdx.x];
+    if (threadIdx.x < SP) {
+        const int kk = threadIdx.x, u = kk & 1, slot = kk >> 1;   // k0 = 2 (t % H) + u
+        for (int t = slot; t < kB; t += H)
+            for (int n = 0; n < 3; n++) v[n] += stage[n][u][t];
+    }
     SpmvTail::finish_v<SP>(v, sys, partials, mode);
 }
 
@@ -1060,6 +1067,162 @@ k_mf_edges(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restr
             y = mf_row<SP, 1>(M, p, k, om, s);
         else
             y = mf_row<SP, 2>(M, p, k, om, s);
+        tail.row(i, y, sv4, r, z, sm);
+    }
+    tail.finish<SP>(sys, partials, mode);
+}
+
+// ---- the curl-curl part as D^T (F f) (variant 35)
+// The face mass matrix F couples each face only with its two neighbours
+// along its normal (the faces of the two cells it separates), so g = F f is
+// computed once per face: g = wa f_-1 + 2 (wa + wb) f_0 + wb f_+1 with wa, wb
+// the normal-direction weights of the cells before and after it.  Every
+// edge's curl-curl row is then the signed sum of g over its 4 faces, 8 adds
+// instead of the 24 multiply-adds of mf_row.  g is needed only on faces
+// whose position along the normal is interior (the faces of non-Dirichlet
+// edges); the others get 0.
+template <int SP>
+__global__ void __launch_bounds__(kB)
+k_mf_gface(MF M, const SysState *sys)
+{
+    const int k = threadIdx.x % SP;
+    if (sys[k].status != kRun) return;
+    const long long nf = M.nfx + M.nfy + M.nfz;
+    const int nc = (int)M.ncell;
+    auto cell = [&](int x, int y, int z) { return (z * (M.ny - 1) + y) * (M.nx - 1) + x; };
+    const int rpb = kB / SP;
+    for (long long t = (long long)blockIdx.x * rpb + threadIdx.x / SP; t < nf;
+         t += (long long)gridDim.x * rpb) {
+        long long q = t;
+        int n, i, j, kk;
+        if (q < M.nfx) {
+            n = 0;
+            i = (int)(q % M.nx);
+            q /= M.nx;
+            j = (int)(q % (M.ny - 1));
+            kk = (int)(q / (M.ny - 1));
+        } else if ((q -= M.nfx) < M.nfy) {
+            n = 1;
+            i = (int)(q % (M.nx - 1));
+            q /= (M.nx - 1);
+            j = (int)(q % M.ny);
+            kk = (int)(q / M.ny);
+        } else {
+            q -= M.nfy;
+            n = 2;
+            i = (int)(q % (M.nx - 1));
+            q /= (M.nx - 1);
+            j = (int)(q % (M.ny - 1));
+            kk = (int)(q / (M.ny - 1));
+        }
+        const int pos = n == 0 ? i : (n == 1 ? j : kk);
+        const int last = (n == 0 ? M.nx : (n == 1 ? M.ny : M.nz)) - 1;
+        float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (pos >= 1 && pos < last) {
+            // the neighbouring faces along the normal and the cells between
+            long long dm;
+            int cb, ca;
+            if (n == 0) {
+                dm = 1;
+                cb = cell(i - 1, j, kk);
+                ca = cell(i, j, kk);
+            } else if (n == 1) {
+                dm = M.nx - 1;
+                cb = cell(i, j - 1, kk);
+                ca = cell(i, j, kk);
+            } else {
+                dm = (long long)(M.nx - 1) * (M.ny - 1);
+                cb = cell(i, j, kk - 1);
+                ca = cell(i, j, kk);
+            }
+            const df wa = d2f(__ldg(M.w + n * nc + cb)), wb = d2f(__ldg(M.w + n * nc + ca));
+            const dfc fm = from4(__ldg(M.f + (t - dm) * SP + k));
+            const dfc f0 = from4(__ldg(M.f + t * SP + k));
+            const dfc fp = from4(__ldg(M.f + (t + dm) * SP + k));
+            const df c0 = scale(add(wa, wb), 2.f);
+            acc gr, gi;
+            gr.mac(wa, fm.re); gr.mac(c0, f0.re); gr.mac(wb, fp.re);
+            gi.mac(wa, fm.im); gi.mac(c0, f0.im); gi.mac(wb, fp.im);
+            out = to4(dfc{gr.get(), gi.get()});
+        }
+        M.g[t * SP + k] = out;
+    }
+}
+
+// one non-Dirichlet edge of direction D at lattice position p: the signed
+// sum of g over its 4 faces (the signs of mf_row's groups) plus the mass
+// part of mf_row
+template <int SP, int D>
+__device__ __forceinline__ dfc mf_row_g(const MF &M, Pos p, int k, df om, const float4 *__restrict__ x)
+{
+    constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
+    const int nc = (int)M.ncell;
+    auto cell = [&](Pos q) { return (q.z * (M.ny - 1) + q.y) * (M.nx - 1) + q.x; };
+    df wm[2][2];
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 2; b++)
+            wm[a][b] = d2f(__ldg(M.w + (3 + D) * nc + cell(mv<T2>(mv<T1>(p, a - 1), b - 1))));
+    const dfc g1a = from4(__ldg(M.g + mf_face_n<T1>(M, mv<T2>(p, -1)) * SP + k));
+    const dfc g1b = from4(__ldg(M.g + mf_face_n<T1>(M, p) * SP + k));
+    const dfc g2a = from4(__ldg(M.g + mf_face_n<T2>(M, mv<T1>(p, -1)) * SP + k));
+    const dfc g2b = from4(__ldg(M.g + mf_face_n<T2>(M, p) * SP + k));
+    acc kr, ki;
+    kr.add(g1a.re); kr.add(neg(g1b.re)); kr.add(neg(g2a.re)); kr.add(g2b.re);
+    ki.add(g1a.im); ki.add(neg(g1b.im)); ki.add(neg(g2a.im)); ki.add(g2b.im);
+    acc mr, mi;
+    const df s0_ = add(wm[0][0], wm[0][1]), s1_ = add(wm[1][0], wm[1][1]);
+    const df r0_ = add(wm[0][0], wm[1][0]), r1_ = add(wm[0][1], wm[1][1]);
+    const df cm[3][3] = {{wm[0][0], scale(s0_, 2.f), wm[0][1]},
+                         {scale(r0_, 2.f), scale(add(s0_, s1_), 4.f), scale(r1_, 2.f)},
+                         {wm[1][0], scale(s1_, 2.f), wm[1][1]}};
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            const Pos q = mv<T2>(mv<T1>(p, a - 1), b - 1);
+            const dfc xe = mf_x<SP>(M, x, mf_edge(M, D, q.x, q.y, q.z), k);
+            mr.mac(cm[a][b], xe.re);
+            mi.mac(cm[a][b], xe.im);
+        }
+    const df mxr = mr.get(), mxi = mi.get();
+    kr.mac(neg(om), mxi);
+    ki.mac(om, mxr);
+    return dfc{kr.get(), ki.get()};
+}
+
+// z = A s in the D^T (F f) form, with the SpMV tail of k_spmv
+template <int SP>
+__global__ void __launch_bounds__(kB)
+k_mf_edges_g(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restrict__ s,
+             const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
+             SysState *sys, double *partials, int mode)
+{
+    const int k = threadIdx.x % SP;
+    const bool on = sys[k].status == kRun;
+    const df om = d2f(omega[k]);
+    SpmvTail tail;
+    tail.mm = mode ? sys[k].mrs_mode : 0;
+    tail.wm = from_double(sys[k].mrs_w);
+    const int rpb = kB / SP;
+    for (int row = blockIdx.x * rpb + threadIdx.x / SP; row < nb; row += gridDim.x * rpb) {
+        if (!on) continue;
+        const int d = row < M.nex ? 0 : (row < M.nex + M.ney ? 1 : 2);
+        const unsigned c = __ldg(M.pos + row);
+        const Pos p{(int)(c & 1023u), (int)((c >> 10) & 1023u), (int)((c >> 20) & 1023u)};
+        const int e = mf_edge(M, d, p.x, p.y, p.z);
+        const long long i = (long long)e * SP + k;
+        const float4 sv4 = __ldg(s + i);
+        dfc y;
+        if (__ldg(M.bedge + e))
+            y = from4(sv4);
+        else if (d == 0)
+            y = mf_row_g<SP, 0>(M, p, k, om, s);
+        else if (d == 1)
+            y = mf_row_g<SP, 1>(M, p, k, om, s);
+        else
+            y = mf_row_g<SP, 2>(M, p, k, om, s);
         tail.row(i, y, sv4, r, z, sm);
     }
     tail.finish<SP>(sys, partials, mode);
@@ -1573,7 +1736,7 @@ struct Impl {
         return MF{F.nx, F.ny, F.nz, F.nfx, F.nfy, F.nfz,
                   (long long)(F.nx - 1) * (F.ny - 1) * (F.nz - 1),
                   (F.nx - 1) * F.ny * F.nz, F.nx * (F.ny - 1) * F.nz, F.rb, F.pos, F.w,
-                  F.bedge, F.f};
+                  F.bedge, F.f, F.g};
     }
     static void spmv(Survey &V, int mode)
     {
@@ -1582,6 +1745,14 @@ struct Impl {
             const MfTileGrid G{V.mft[0], V.mft[1], V.mft[2], V.mft[3], V.mft[4], V.mft[5], V.mft[6]};
             k_mf_tile<SP><<<V.g_mft, MfTile<SP>::NT, MfTile<SP>::SMEM, V.st>>>(
                 mfd(V), G, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode);
+            return;
+        }
+        if (V.ch == kMatFree + 3) {
+            const MF M = mfd(V);
+            k_mf_faces<SP><<<V.g_mff, kB, 0, V.st>>>(M, V.s, V.sys);
+            k_mf_gface<SP><<<V.g_mfg, kB, 0, V.st>>>(M, V.sys);
+            k_mf_edges_g<SP><<<V.g_mfe3, kB, 0, V.st>>>(V.nb, M, V.omega, V.s, V.r, V.z, V.sm, V.sys,
+                                                       V.partials, mode);
             return;
         }
         if (V.ch == kMatFree || V.ch == kMatFree + 1) {
@@ -1690,6 +1861,9 @@ struct Impl {
             V.g_mff = g((const void *)k_mf_faces<SP>, (int)std::min<long long>(
                                                           (nf + kB / SP - 1) / (kB / SP), INT_MAX));
             V.g_mfe = g((const void *)k_mf_edges<SP>, V.grid_rows);
+            V.g_mfg = g((const void *)k_mf_gface<SP>, (int)std::min<long long>(
+                                                          (nf + kB / SP - 1) / (kB / SP), INT_MAX));
+            V.g_mfe3 = g((const void *)k_mf_edges_g<SP>, V.grid_rows);
             if constexpr (SP >= 2) {
                 if (V.ch == kMatFree + 1)
                     V.g_mfe = g((const void *)k_mf_edges2<SP>,
@@ -2014,7 +2188,8 @@ int matfree_build(Survey &V, const MatFreeMesh &a, int kuz, int kpar, int nsm)
     if ((rc = dev_alloc(&F.rb, rb.size())) || (rc = dev_alloc(&F.pos, pos.size())) ||
         (rc = dev_alloc(&F.bedge, bedge.size())) ||
         (rc = dev_alloc(&F.w, w.size())) ||
-        (rc = dev_alloc(&F.f, (size_t)(F.nfx + F.nfy + F.nfz) * V.SP)))
+        (rc = dev_alloc(&F.f, (size_t)(F.nfx + F.nfy + F.nfz) * V.SP)) ||
+        (rc = dev_alloc(&F.g, (size_t)(F.nfx + F.nfy + F.nfz) * V.SP)))
         return rc;
     MTGPU_TRY(cudaMemcpyAsync(F.rb, rb.data(), sizeof(int) * rb.size(), cudaMemcpyHostToDevice, V.st));
     MTGPU_TRY(cudaMemcpyAsync(F.pos, pos.data(), sizeof(unsigned) * pos.size(),
@@ -2096,6 +2271,39 @@ int matfree_build(Survey &V, const MatFreeMesh &a, int kuz, int kpar, int nsm)
         }
         memcpy(&dm, &mx[0], sizeof(double));
         F.lattice = dm == 0.0;
+    }
+    {
+        // the D^T (F f) form rounds differently from variant 32 (products of
+        // the face values summed per face first): it must agree to 1e-12
+        F.gface = true;
+        k_pattern<<<4 * nsm, kB, 0, V.st>>>(n, V.s);
+        MTGPU_TRY(cudaMemcpyAsync(V.sys, init.data(), sizeof(SysState) * 32, cudaMemcpyHostToDevice, V.st));
+        V.ch = kMatFree;
+        MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+        MTGPU_SP_DISPATCH(V.SP, spmv_only(V));
+        MTGPU_TRY(cudaMemcpyAsync(V.w, V.z, sizeof(float4) * n, cudaMemcpyDeviceToDevice, V.st));
+        MTGPU_TRY(cudaMemcpyAsync(V.sys, init.data(), sizeof(SysState) * 32, cudaMemcpyHostToDevice, V.st));
+        V.ch = kMatFree + 3;
+        MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+        MTGPU_SP_DISPATCH(V.SP, spmv_only(V));
+        V.ch = ch;
+        MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+        if ((rc = dev_alloc(&d_mx, 2))) return rc;
+        MTGPU_TRY(cudaMemsetAsync(d_mx, 0, sizeof(unsigned long long) * 2, V.st));
+        k_maxdiff<<<4 * nsm, kB, 0, V.st>>>(n, V.z, V.w, d_mx);
+        note_launches(7);
+        err = cudaGetLastError();
+        if (err == cudaSuccess)
+            err = cudaMemcpyAsync(mx, d_mx, sizeof(mx), cudaMemcpyDeviceToHost, V.st);
+        if (err == cudaSuccess) err = cudaStreamSynchronize(V.st);
+        dev_free(d_mx);
+        if (err != cudaSuccess) {
+            set_last_error(err, "face-mass matrix-free SpMV set-up check", __FILE__, __LINE__);
+            return MTGPU_ERR_CUDA;
+        }
+        memcpy(&dm, &mx[0], sizeof(double));
+        memcpy(&bm, &mx[1], sizeof(double));
+        F.gface = bm > 0.0 && dm / bm < 1e-12;
     }
     return MTGPU_OK;
 }
@@ -2215,7 +2423,7 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
         MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
     } else {
         const int cand[kSpmvVariants] = {0, 1, 2, 4, 8, kRowVariant + 2, kRowVariant + 4, kMatFree,
-                                         kMatFree + 1, kMatFree + 2};
+                                         kMatFree + 1, kMatFree + 2, kMatFree + 3};
         float best = 1e30f;
         int best_ch = 4;
         for (int c = 0; c < kSpmvVariants; c++) {
@@ -2321,7 +2529,7 @@ int survey_iter_timed(Survey &V, int reps, float *ms)
     MTGPU_TRY(cudaEventCreate(&e1));
     MTGPU_TRY(cudaEventRecord(e0, V.st));
     for (int q = 0; q < reps; q++) MTGPU_SP_DISPATCH(V.SP, iteration(V));
-    note_launches((unsigned long long)reps * ((V.G.m > 0 ? 4 : 3) + (V.ch == kMatFree || V.ch == kMatFree + 1 ? 1 : 0)));
+    note_launches((unsigned long long)reps * ((V.G.m > 0 ? 4 : 3) + spmv_extra_launches(V.ch)));
     MTGPU_TRY(cudaEventRecord(e1, V.st));
     MTGPU_TRY(cudaEventSynchronize(e1));
     MTGPU_TRY(cudaEventElapsedTime(ms, e0, e1));
@@ -2484,7 +2692,7 @@ int survey_launch(Survey &V, SurveyRun &R)
         set_last_error(e, "cudaGraphLaunch", __FILE__, __LINE__);
         return MTGPU_ERR_CUDA;
     }
-    const unsigned long long kpi = (V.G.m > 0 ? 4 : 3) + (V.ch == kMatFree || V.ch == kMatFree + 1 ? 1 : 0);
+    const unsigned long long kpi = (V.G.m > 0 ? 4 : 3) + spmv_extra_launches(V.ch);
     note_launches(kpi * (unsigned long long)R.ipl + 1);
     R.guard += R.ipl;
     // the state arrives with the launch's end (read in survey_collect)

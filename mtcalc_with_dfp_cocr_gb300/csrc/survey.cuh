@@ -25,7 +25,7 @@ struct SysState {
 
 constexpr int kRowVariant = 16;    // + slots in flight: one thread per row, both systems
 constexpr int kMatFree = 32;       // matrix-free SpMV on tensor meshes (+1: two systems per thread)
-constexpr int kSpmvVariants = 10;  // 0, 1, 2, 4, 8, 18, 20, 32, 33, 34
+constexpr int kSpmvVariants = 11;  // 0, 1, 2, 4, 8, 18, 20, 32, 33, 34, 35
 
 // Matrix-free SpMV of a tensor (RegularMeshBuilder) mesh: K = D^T F D with D
 // the edge -> face circulations and F the face mass matrix, M the edge mass
@@ -39,8 +39,10 @@ struct MatFree {
     float2 *w = nullptr;             // [6][cells] double-float wF/3 (x, y, z), wM/9 (x, y, z)
     unsigned char *bedge = nullptr;  // [nb] Dirichlet edges
     float4 *f = nullptr;             // face circulations [faces][SP]
+    float4 *g = nullptr;             // face mass applied to them, F f [faces][SP] (variant 35)
     double check = -1.0;             // set-up check: max |A_mf s - A s| / max |A s|
     bool lattice = false;            // Dirichlet edges follow the lattice rule (variant 34)
+    bool gface = false;              // the D^T (F f) form agrees with variant 32 (variant 35)
     void release();
 };
 
@@ -58,10 +60,11 @@ struct Survey {
     int tile_T = 1, ntiles = 0, tile_smem = 0, tile_smem_x = 0, g_spmv_t = 0, g_spmv_tx = 0;
     int *uoff = nullptr, *ucol = nullptr;
     unsigned short *lc = nullptr, *lr = nullptr;
-    float tune_ms[kSpmvVariants] = {};   // SpMV times of the variants 0, 1, 2, 4, 8, 18, 20, 32, 33, 34
+    float tune_ms[kSpmvVariants] = {};   // SpMV times of the variants 0, 1, 2, 4, 8, 18, 20, 32, 33, 34, 35
     MatFree mf;
     int g_mff = 0, g_mfe = 0;                    // matrix-free launch grids (faces, edges)
     int g_mft = 0;                               // tiled matrix-free launch grid (variant 34)
+    int g_mfg = 0, g_mfe3 = 0;                   // face-mass and edge grids (variant 35)
     int mft[7] = {};                             // its tiles x, y, z chunks, groups, planes per chunk, tile columns x, y
     Folded G;                                    // pattern of G and G^T
     float2 *kc = nullptr, *mc = nullptr, *kr = nullptr;   // double-float K and M per slot
@@ -94,7 +97,15 @@ inline bool spmv_variant_available(const Survey &V, int v)
     if (v == kMatFree) return V.mf.on;
     if (v == kMatFree + 1) return V.mf.on && V.SP >= 2;
     if (v == kMatFree + 2) return V.mf.on && V.mf.lattice && V.g_mft > 0 && V.g_mft <= V.pblocks;
+    if (v == kMatFree + 3) return V.mf.on && V.mf.gface;
     return false;
+}
+
+// kernels an SpMV launch adds to the iteration's one: the face kernels of
+// the matrix-free forms
+inline int spmv_extra_launches(int v)
+{
+    return v == kMatFree || v == kMatFree + 1 ? 1 : (v == kMatFree + 3 ? 2 : 0);
 }
 
 // Host mesh description for the matrix-free SpMV (all arrays host, 0-based)

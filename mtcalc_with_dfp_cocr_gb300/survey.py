@@ -22,7 +22,7 @@ import numpy as np
 from . import _lib
 
 
-SPMV_VARIANTS = (0, 1, 2, 4, 8, 18, 20, 32, 33, 34)   # include/mtgpu.h, mtgpu_survey_tuning
+SPMV_VARIANTS = (0, 1, 2, 4, 8, 18, 20, 32, 33, 34, 35)   # include/mtgpu.h, mtgpu_survey_tuning
 
 
 class Survey:
@@ -84,7 +84,8 @@ class Survey:
         18 and 20 (two systems) run one thread per row for both systems, 32
         is the matrix-free SpMV of tensor meshes, 33 the same with two
         systems per thread, 34 the same in one tiled kernel with the edge
-        values and face circulations in shared memory."""
+        values and face circulations in shared memory, 35 the curl-curl part
+        as D^T (F f) with the face mass matrix applied once per face."""
         v = C.c_int()
         ms = (C.c_float * len(SPMV_VARIANTS))()
         _lib.check(_lib.lib().mtgpu_survey_tuning(self._h, C.byref(v), ms),
@@ -93,7 +94,7 @@ class Survey:
 
     def set_spmv_variant(self, variant):
         """Pin the SpMV variant (0 x and matrix staged, 1 x staged, 2, 4, 8
-        slots in flight, 18, 20 row per thread for two systems, 32, 33, 34
+        slots in flight, 18, 20 row per thread for two systems, 32-35
         matrix-free) instead of the autotuned one."""
         _lib.check(_lib.lib().mtgpu_survey_set_spmv_variant(self._h, int(variant)),
                    "mtgpu_survey_set_spmv_variant")

@@ -117,19 +117,22 @@ def test_spmv_variants_agree(gpu, name, S):
           np.stack([t[2] for t in tabs]), b)
     sv = survey.Survey(A, nus)
     ref = None
-    for v in (0, 1, 2, 4, 8, 32, 33, 34) + ((18, 20) if S == 2 else ()):
+    for v in (0, 1, 2, 4, 8, 32, 33, 34, 35) + ((18, 20) if S == 2 else ()):
         sv.set_spmv_variant(v)
         x = torch.zeros_like(b)
         code, st = sv.solve(b, x, eps=1e-8, maxiter=20000, verify=True)
         assert code == 0
         assert max(st["true_residual_rel"]) < 1e-8
         if ref is None:
-            ref = (x.clone(), st["iterations"])
+            ref = (x.clone(), st["iterations"], max(st["verifications"]))
             continue
-        # rounding moves the stop by a few iterations; the earth and surface
-        # edges agree (the air's gradient components are free at 1e-8)
-        for i, j in zip(st["iterations"], ref[1]):
-            assert abs(i - j) <= 3 + 0.03 * j, (v, st["iterations"], ref[1])
+        # rounding moves the stop by a few iterations (more when one run's
+        # first stop leaves its true residual just above eps and the
+        # continuation adds a round); the earth and surface edges agree (the
+        # air's gradient components are free at 1e-8)
+        for i, j, nv in zip(st["iterations"], ref[1], st["verifications"]):
+            slack = 0.03 if nv <= 1 and ref[2] <= 1 else 0.10
+            assert abs(i - j) <= 3 + slack * j, (v, st["iterations"], ref[1])
         xyz = w.mesh.xyz()
         e = w.mesh.edges()
         earth = 0.5 * (xyz[e[:, 0], 2] + xyz[e[:, 1], 2]) <= 0.0
@@ -169,7 +172,7 @@ def test_survey_iteration_guard_times_out(gpu, monkeypatch):
     A.close()
 
 
-@pytest.mark.parametrize("variant", [32, 33, 34])
+@pytest.mark.parametrize("variant", [32, 33, 34, 35])
 def test_matfree_operator_on_gradients(gpu, variant):
     """The matrix-free SpMV on discrete gradients x = grad(phi): the curl-curl
     part vanishes (curl grad = 0), so y = i omega M x checks the mass part
@@ -316,3 +319,27 @@ def test_survey_two_meshes_packed(gpu):
     sv.close()
     for A in As:
         A.close()
+
+
+@pytest.mark.parametrize("name,S", [("tiny", 1), ("small", 3), ("c1", 2), ("small", 32)])
+def test_face_mass_form_matches_two_kernel_form(gpu, name, S):
+    """Variant 35 applies the face mass matrix once per face (D^T (F f));
+    it sums the same terms in another grouping, so its product agrees with
+    variant 32's to the double-float rounding of the curl-curl sums, and
+    with the oracle's assembled matrix like variant 32."""
+    torch = gpu
+    w = workloads.make(name)
+    nus = list(np.logspace(-2, 2, S))
+    A = assembly.Assembly(w.mesh)
+    sv = survey.Survey(A, nus)
+    rng = np.random.default_rng(7 + S)
+    x = torch.tensor(rng.standard_normal((S, 2 * w.mesh.nb)), device="cuda")
+    y32, y35 = torch.empty_like(x), torch.empty_like(x)
+    sv.set_spmv_variant(32)
+    sv.spmv(x, y32)
+    sv.set_spmv_variant(35)
+    sv.spmv(x, y35)
+    d = (y35 - y32).abs().max().item()
+    assert d <= 1e-12 * y32.abs().max().item(), d
+    sv.close()
+    A.close()
