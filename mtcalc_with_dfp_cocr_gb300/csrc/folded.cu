@@ -16,7 +16,7 @@ namespace mtgpu {
 void Folded::release()
 {
     dev_free(d_gp); dev_free(d_gj); dev_free(d_gv);
-    dev_free(d_tp); dev_free(d_tj); dev_free(d_tv);
+    dev_free(d_tp); dev_free(d_tj); dev_free(d_tv); dev_free(d_tn);
     dev_free(d_da); dev_free(d_ds); dev_free(d_h);
     n = m = 0;
 }
@@ -42,6 +42,8 @@ int folded_build_g(const mtgpu_mesh_desc &mesh, Folded &P, cudaStream_t st)
     // beyond n_nodes_c are expanded through the T-matrix rows ig_t/jg_t/gg_t
     std::vector<int> tp(ne + 1, 0), tj;
     std::vector<double> tv;
+    std::vector<int2> tn(ne, make_int2(-1, -1));
+    bool compact = true;
     tj.reserve((size_t)ne * 2);
     tv.reserve((size_t)ne * 2);
     for (int e = 0; e < ne; e++) {
@@ -52,8 +54,10 @@ int folded_build_g(const mtgpu_mesh_desc &mesh, Folded &P, cudaStream_t st)
                 if (v >= 0 && in_sigma[v]) {
                     tj.push_back(renum[v]);
                     tv.push_back(sgn);
+                    (k == 0 ? tn[e].x : tn[e].y) = renum[v];
                 }
             } else {
+                compact = false;
                 for (int t = mesh.ig_t[v]; t < mesh.ig_t[v + 1]; t++)
                     if (in_sigma[mesh.jg_t[t]]) {
                         tj.push_back(renum[mesh.jg_t[t]]);
@@ -93,6 +97,10 @@ int folded_build_g(const mtgpu_mesh_desc &mesh, Folded &P, cudaStream_t st)
         MTGPU_TRY(cudaMemcpyAsync(P.d_tv, tv.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice, st));
     }
     MTGPU_TRY(cudaMemcpyAsync(P.d_tp, tp.data(), sizeof(int) * (ne + 1), cudaMemcpyHostToDevice, st));
+    if (compact) {
+        if ((rc = dev_alloc(&P.d_tn, ne))) return rc;
+        MTGPU_TRY(cudaMemcpyAsync(P.d_tn, tn.data(), sizeof(int2) * ne, cudaMemcpyHostToDevice, st));
+    }
     // the host vectors go out of scope: wait for the copies
     MTGPU_TRY(cudaStreamSynchronize(st));
     return MTGPU_OK;

@@ -74,6 +74,10 @@ struct Folded {
     int n = 0, m = 0;                  // edges, interior conductive nodes
     int *d_gp = nullptr, *d_gj = nullptr;   double *d_gv = nullptr;   // G   (CSR, m rows)
     int *d_tp = nullptr, *d_tj = nullptr;   double *d_tv = nullptr;   // G^T (CSR, n rows)
+    // G^T of a conforming mesh in compact form: per edge the G rows of its
+    // first (-1/2) and second (+1/2) node, -1 where the node has no row;
+    // null on meshes with T-matrix nodes
+    int2 *d_tn = nullptr;
     double2 *d_da = nullptr;           // 1/diag(A)
     double2 *d_ds = nullptr;           // 1/diag(G A G^T)
     double2 *d_h = nullptr;            // node work vector

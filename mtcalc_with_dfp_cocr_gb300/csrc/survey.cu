@@ -313,9 +313,9 @@ k_node(int m, const int *__restrict__ gp, const int *__restrict__ gj, const floa
 template <int SP>
 __global__ void __launch_bounds__(kB)
 k_edge(int n, const int *__restrict__ tp, const int *__restrict__ tj, const float *__restrict__ tv,
-       const float4 *__restrict__ da, const float4 *__restrict__ h, const float4 *__restrict__ src,
-       const float4 *__restrict__ z, float4 *__restrict__ p, float4 *__restrict__ a,
-       float4 *__restrict__ w, SysState *sys, double *partials, int mode)
+       const int2 *__restrict__ tn, const float4 *__restrict__ da, const float4 *__restrict__ h,
+       const float4 *__restrict__ src, const float4 *__restrict__ z, float4 *__restrict__ p,
+       float4 *__restrict__ a, float4 *__restrict__ w, SysState *sys, double *partials, int mode)
 {
     const int k = threadIdx.x % SP;
     const bool on = sys[k].status == kRun;
@@ -325,7 +325,18 @@ k_edge(int n, const int *__restrict__ tp, const int *__restrict__ tj, const floa
     for (int e = blockIdx.x * rpb + threadIdx.x / SP; e < n; e += gridDim.x * rpb) {
         if (!on) continue;
         const long long idx = (long long)e * SP + k;
-        const int j0 = __ldg(tp + e), j1 = __ldg(tp + e + 1);
+        // G^T row: compact (the rows of the edge's two nodes, -1/2 and +1/2
+        // in that order, one dependent load) or the CSR of T-matrix meshes
+        int j0, j1;
+        int2 r2 = make_int2(-1, -1);
+        if (tn) {
+            r2 = __ldg(tn + e);
+            j0 = 0;
+            j1 = (r2.x >= 0) + (r2.y >= 0);
+        } else {
+            j0 = __ldg(tp + e);
+            j1 = __ldg(tp + e + 1);
+        }
         const float4 srcv = src[idx], dav = __ldg(da + idx);
         float4 pv = make_float4(0.f, 0.f, 0.f, 0.f), zv = pv, av = pv;
         if (mode != 0) {
@@ -335,13 +346,26 @@ k_edge(int n, const int *__restrict__ tp, const int *__restrict__ tj, const floa
         }
         float4 hv0 = make_float4(0.f, 0.f, 0.f, 0.f), hv1 = hv0;
         float t0 = 0.f, t1 = 0.f;
-        if (j1 > j0) {
-            hv0 = __ldg(h + (long long)__ldg(tj + j0) * SP + k);
-            t0 = __ldg(tv + j0);
-        }
-        if (j1 > j0 + 1) {
-            hv1 = __ldg(h + (long long)__ldg(tj + j0 + 1) * SP + k);
-            t1 = __ldg(tv + j0 + 1);
+        if (tn) {
+            // entries in the CSR's order: the first node's (if any), then the second's
+            const int ra = r2.x >= 0 ? r2.x : r2.y, rb = r2.y;
+            if (j1 > 0) {
+                hv0 = __ldg(h + (long long)ra * SP + k);
+                t0 = r2.x >= 0 ? -0.5f : 0.5f;
+            }
+            if (j1 > 1) {
+                hv1 = __ldg(h + (long long)rb * SP + k);
+                t1 = 0.5f;
+            }
+        } else {
+            if (j1 > j0) {
+                hv0 = __ldg(h + (long long)__ldg(tj + j0) * SP + k);
+                t0 = __ldg(tv + j0);
+            }
+            if (j1 > j0 + 1) {
+                hv1 = __ldg(h + (long long)__ldg(tj + j0 + 1) * SP + k);
+                t1 = __ldg(tv + j0 + 1);
+            }
         }
         dfc an;
         if (mode == 0) {
@@ -363,7 +387,7 @@ k_edge(int n, const int *__restrict__ tp, const int *__restrict__ tj, const floa
             wr.macf(df{hv1.x, hv1.y}, t1);
             wi.macf(df{hv1.z, hv1.w}, t1);
         }
-        for (int j = j0 + 2; j < j1; j++) {       // T-matrix rows only
+        for (int j = j0 + 2; j < j1 && !tn; j++) {       // T-matrix rows only
             const float4 hv = __ldg(h + (long long)__ldg(tj + j) * SP + k);
             const float t = __ldg(tv + j);
             wr.macf(df{hv.x, hv.y}, t);
@@ -1800,7 +1824,7 @@ struct Impl {
         if (V.G.m > 0)
             k_node<SP><<<V.g_node, kB, 0, V.st>>>(V.G.m, V.G.d_gp, V.G.d_gj, V.gv32, V.ds, V.z, V.a,
                                                   V.h, V.sys, 1);
-        k_edge<SP><<<V.g_edge, kB, 0, V.st>>>(V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.da, V.h, V.s, V.z,
+        k_edge<SP><<<V.g_edge, kB, 0, V.st>>>(V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.G.d_tn, V.da, V.h, V.s, V.z,
                                               V.p, V.a, V.w, V.sys, V.partials, 1);
         k_update<SP><<<V.g_update, kB, 0, V.st>>>(V.nb, V.p, V.a, V.w, V.sm, V.x, V.r, V.s, V.sys,
                                                   V.partials);
@@ -1815,7 +1839,7 @@ struct Impl {
         if (V.G.m > 0)
             k_node<SP><<<V.g_node, kB, 0, V.st>>>(V.G.m, V.G.d_gp, V.G.d_gj, V.gv32, V.ds, V.r, V.a,
                                                   V.h, V.sys, 0);
-        k_edge<SP><<<V.g_edge, kB, 0, V.st>>>(V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.da, V.h, V.r, V.z,
+        k_edge<SP><<<V.g_edge, kB, 0, V.st>>>(V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.G.d_tn, V.da, V.h, V.r, V.z,
                                               V.p, V.a, V.s, V.sys, V.partials, 0);
         cudaMemsetAsync(V.p, 0, sizeof(float4) * (size_t)V.nb * SP, V.st);
         cudaMemsetAsync(V.a, 0, sizeof(float4) * (size_t)V.nb * SP, V.st);
