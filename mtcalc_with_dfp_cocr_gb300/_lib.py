@@ -113,6 +113,7 @@ SIGNATURES = {
     "mtgpu_survey_create_multi": (C.c_int, [C.c_int, C.POINTER(_vp), _i, _d, _vp, C.POINTER(_vp)]),
     "mtgpu_survey_info": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                     C.POINTER(C.c_longlong)]),
+    "mtgpu_survey_preconditioner": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_float)]),
     "mtgpu_survey_spmv": (C.c_int, [_vp, _vp, _vp]),
     "mtgpu_survey_spmv_timed": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_float)]),
     "mtgpu_survey_tuning": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_float)]),

@@ -405,6 +405,18 @@ int mtgpu_survey_tuning(const mtgpu_survey *s, int *variant, float *ms)
     return MTGPU_OK;
 }
 
+int mtgpu_survey_preconditioner(const mtgpu_survey *s, int *fused, float *ms)
+{
+    MTGPU_CHECK_ARG(s != nullptr, "null survey");
+    const mtgpu::Survey &V = *s->groups[0];
+    if (fused) *fused = V.prec_tile ? 1 : 0;
+    if (ms) {
+        ms[0] = V.prec_ms[0];
+        ms[1] = V.prec_ms[1];
+    }
+    return MTGPU_OK;
+}
+
 int mtgpu_survey_set_spmv_variant(mtgpu_survey *s, int variant)
 {
     MTGPU_CHECK_ARG(s != nullptr, "null survey");

@@ -47,7 +47,8 @@ void Survey::release()
     dev_free(omega); dev_free(omega64); dev_free(gkg); dev_free(gmg);
     dev_free(sys);
     dev_free(b); dev_free(x); dev_free(r); dev_free(s); dev_free(p); dev_free(a);
-    dev_free(z); dev_free(w); dev_free(sm); dev_free(h);
+    dev_free(z); dev_free(w); dev_free(sm); dev_free(h); dev_free(a2);
+    prec_tile = false;
     dev_free(b64); dev_free(xacc); dev_free(all_on);
     dev_free(uoff); dev_free(ucol); dev_free(lc); dev_free(lr);
     ntiles = 0;
@@ -1253,6 +1254,7 @@ k_mf_edges_g(int nb, MF M, const float2 *__restrict__ omega, const float4 *__res
 }
 
 #include "mf_tile.cuh"
+#include "prec_tile.cuh"
 
 // largest |a - b| and |b| over n float4 double-float pairs (as ordered bits
 // of non-negative doubles)
@@ -1819,8 +1821,20 @@ struct Impl {
         default: k_spmv<SP, 4><<<V.g_spmv, kB, 0, V.st>>>(V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode); break;
         }
     }
-    static void iteration(Survey &V)
+    // iteration t of a sequence: the fused preconditioner alternates a's
+    // buffers (t even reads a, writes a2; t odd the reverse)
+    static void iteration(Survey &V, int t)
     {
+        if (V.prec_tile) {
+            float4 *ain = (t & 1) ? V.a2 : V.a, *aout = (t & 1) ? V.a : V.a2;
+            const PrecGrid G{V.pt[0], V.pt[1], V.pt[2], V.pt[3], V.pt[4]};
+            k_prec_tile<SP><<<V.g_pt, PrecTile<SP>::NT, PrecTile<SP>::SMEM, V.st>>>(
+                mfd(V), G, V.ds, V.da, V.s, V.z, ain, aout, V.p, V.w, V.sys, V.partials);
+            k_update<SP><<<V.g_update, kB, 0, V.st>>>(V.nb, V.p, aout, V.w, V.sm, V.x, V.r, V.s,
+                                                      V.sys, V.partials);
+            spmv(V, 1);
+            return;
+        }
         if (V.G.m > 0)
             k_node<SP><<<V.g_node, kB, 0, V.st>>>(V.G.m, V.G.d_gp, V.G.d_gj, V.gv32, V.ds, V.z, V.a,
                                                   V.h, V.sys, 1);
@@ -1829,6 +1843,50 @@ struct Impl {
         k_update<SP><<<V.g_update, kB, 0, V.st>>>(V.nb, V.p, V.a, V.w, V.sm, V.x, V.r, V.s, V.sys,
                                                   V.partials);
         spmv(V, 1);
+    }
+    // one preconditioner step of the iteration (mode 1), unfused or fused
+    static void precond_step(Survey &V, bool fused, float4 *ain, float4 *aout)
+    {
+        if (fused) {
+            const PrecGrid G{V.pt[0], V.pt[1], V.pt[2], V.pt[3], V.pt[4]};
+            k_prec_tile<SP><<<V.g_pt, PrecTile<SP>::NT, PrecTile<SP>::SMEM, V.st>>>(
+                mfd(V), G, V.ds, V.da, V.s, V.z, ain, aout, V.p, V.w, V.sys, V.partials);
+            return;
+        }
+        if (V.G.m > 0)
+            k_node<SP><<<V.g_node, kB, 0, V.st>>>(V.G.m, V.G.d_gp, V.G.d_gj, V.gv32, V.ds, V.z, ain,
+                                                  V.h, V.sys, 1);
+        k_edge<SP><<<V.g_edge, kB, 0, V.st>>>(V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.G.d_tn, V.da, V.h,
+                                              V.s, V.z, V.p, ain, V.w, V.sys, V.partials, 1);
+    }
+    static void prec_grid(Survey &V, int nsm)
+    {
+        using T = PrecTile<SP>;
+        int res = 0;
+        if (cudaFuncSetAttribute((const void *)k_prec_tile<SP>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, T::SMEM) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&res, (const void *)k_prec_tile<SP>, T::NT,
+                                                          T::SMEM) != cudaSuccess ||
+            res < 1) {
+            cudaGetLastError();
+            res = 1;
+        }
+        const int tx = ceil_div(V.mf.nx, T::TX), ty = ceil_div(V.mf.ny, T::TY), grp = SP / T::SB;
+        const int bxy = tx * ty * grp;
+        int zc = 1;
+        long long best = -1;
+        for (int c = 1; c <= std::max(1, V.mf.nz / 4); c++) {
+            const long long waves = ceil_div(bxy * c, res * nsm);
+            const long long cost = waves * (ceil_div(V.mf.nz, c) + 1);
+            if (best < 0 || cost < best) {
+                best = cost;
+                zc = c;
+            }
+        }
+        const int kz = ceil_div(V.mf.nz, zc);
+        zc = ceil_div(V.mf.nz, kz);
+        V.pt[0] = tx; V.pt[1] = ty; V.pt[2] = zc; V.pt[3] = grp; V.pt[4] = kz;
+        V.g_pt = bxy * zc;
     }
     // stages 1-4 of PCOCR_RCI::Run: r = b - A x, x0 test, s = M^-1 r,
     // p = a = 0, z = A s, (z, s)
@@ -2334,6 +2392,98 @@ int matfree_build(Survey &V, const MatFreeMesh &a, int kuz, int kpar, int nsm)
 
 }  // namespace
 
+namespace {
+
+// The fused preconditioner (prec_tile.cuh), where the mesh allows it: a
+// tensor mesh with the lattice's Dirichlet edges, every interior node a row
+// of G in node order, the compact G^T.  A set-up check runs one step of both
+// forms on the same pseudo-random vectors and compares p, a and w bit for
+// bit; then whole iterations of both are timed and the faster kept.
+// MTGPU_PREC_TILE=0 / 1 (environment) forces the choice where allowed.
+int prec_tile_setup(Survey &V, int nsm)
+{
+    V.prec_tile = false;
+    if (!V.mf.on || !V.mf.lattice || !V.G.d_tn) return MTGPU_OK;
+    const long long mi = (long long)(V.mf.nx - 2) * (V.mf.ny - 2) * (V.mf.nz - 2);
+    if (V.G.m != mi) return MTGPU_OK;
+    MTGPU_SP_DISPATCH(V.SP, prec_grid(V, nsm));
+    if (V.g_pt < 1 || V.g_pt > V.pblocks) return MTGPU_OK;
+    const char *force = getenv("MTGPU_PREC_TILE");
+    if (force && *force == '0') return MTGPU_OK;
+    const long long n = (long long)V.nb * V.SP;
+    int rc;
+    if (!V.a2 && (rc = dev_alloc(&V.a2, (size_t)n))) return rc;
+    std::vector<SysState> init(32);
+    for (int k = 0; k < 32; k++) {
+        SysState q{};
+        q.status = k < V.S ? kRun : MTGPU_OK;
+        q.maxiter = INT_MAX;
+        q.zs = make_double2(1.0, 0.0);
+        q.beta = make_double2(0.375, -0.25);
+        init[k] = q;
+    }
+    float4 *ref = nullptr;
+    unsigned long long *d_mx = nullptr;
+    if ((rc = dev_alloc(&ref, (size_t)3 * n)) || (rc = dev_alloc(&d_mx, 2))) {
+        dev_free(ref);
+        return rc;
+    }
+    // the same inputs for both: s, z, a (V.a), p from the pattern, p saved
+    for (float4 *v : {V.s, V.z, V.a, V.p}) k_pattern<<<4 * nsm, kB, 0, V.st>>>(n, v);
+    note_launches(4);
+    MTGPU_TRY(cudaMemcpyAsync(V.a2, V.p, sizeof(float4) * n, cudaMemcpyDeviceToDevice, V.st));
+    MTGPU_TRY(cudaMemcpyAsync(V.sys, init.data(), sizeof(SysState) * 32, cudaMemcpyHostToDevice, V.st));
+    // unfused: k_edge updates a in place; keep a's input in ref[2]
+    MTGPU_TRY(cudaMemcpyAsync(ref + 2 * n, V.a, sizeof(float4) * n, cudaMemcpyDeviceToDevice, V.st));
+    MTGPU_SP_DISPATCH(V.SP, precond_step(V, false, V.a, V.a));
+    MTGPU_TRY(cudaMemcpyAsync(ref, V.p, sizeof(float4) * n, cudaMemcpyDeviceToDevice, V.st));
+    MTGPU_TRY(cudaMemcpyAsync(ref + n, V.w, sizeof(float4) * n, cudaMemcpyDeviceToDevice, V.st));
+    // fused: p restored, a's input back in V.a, a's output into ref[2]'s place after the copy
+    MTGPU_TRY(cudaMemcpyAsync(V.p, V.a2, sizeof(float4) * n, cudaMemcpyDeviceToDevice, V.st));
+    MTGPU_TRY(cudaMemcpyAsync(V.a2, V.a, sizeof(float4) * n, cudaMemcpyDeviceToDevice, V.st));   // a (unfused result)
+    MTGPU_TRY(cudaMemcpyAsync(V.a, ref + 2 * n, sizeof(float4) * n, cudaMemcpyDeviceToDevice, V.st));
+    MTGPU_TRY(cudaMemcpyAsync(ref + 2 * n, V.a2, sizeof(float4) * n, cudaMemcpyDeviceToDevice, V.st));
+    MTGPU_TRY(cudaMemcpyAsync(V.sys, init.data(), sizeof(SysState) * 32, cudaMemcpyHostToDevice, V.st));
+    MTGPU_SP_DISPATCH(V.SP, precond_step(V, true, V.a, V.a2));
+    MTGPU_TRY(cudaMemsetAsync(d_mx, 0, sizeof(unsigned long long) * 2, V.st));
+    k_maxdiff<<<4 * nsm, kB, 0, V.st>>>(n, V.p, ref, d_mx);
+    k_maxdiff<<<4 * nsm, kB, 0, V.st>>>(n, V.w, ref + n, d_mx);
+    k_maxdiff<<<4 * nsm, kB, 0, V.st>>>(n, V.a2, ref + 2 * n, d_mx);
+    note_launches(6);
+    unsigned long long mx[2] = {1, 1};
+    cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess) err = cudaMemcpyAsync(mx, d_mx, sizeof(mx), cudaMemcpyDeviceToHost, V.st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(V.st);
+    dev_free(ref);
+    dev_free(d_mx);
+    if (err != cudaSuccess) {
+        set_last_error(err, "fused preconditioner set-up check", __FILE__, __LINE__);
+        return MTGPU_ERR_CUDA;
+    }
+    double dm;
+    memcpy(&dm, &mx[0], sizeof(double));
+    if (dm != 0.0) {   // not bit-equal: keep the two-kernel form
+        dev_free(V.a2);
+        return MTGPU_OK;
+    }
+    bool use = true;
+    if (!(force && *force == '1')) {
+        float t_un = 0.f, t_fu = 0.f;
+        V.prec_tile = false;
+        if ((rc = survey_iter_timed(V, 2, &t_un)) || (rc = survey_iter_timed(V, 4, &t_un))) return rc;
+        V.prec_tile = true;
+        if ((rc = survey_iter_timed(V, 2, &t_fu)) || (rc = survey_iter_timed(V, 4, &t_fu))) return rc;
+        use = t_fu < t_un;
+        V.prec_ms[0] = t_un / 4.f;
+        V.prec_ms[1] = t_fu / 4.f;
+    }
+    V.prec_tile = use;
+    if (!use) dev_free(V.a2);
+    return MTGPU_OK;
+}
+
+}  // namespace
+
 int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const double *omega,
                  Survey &V, cudaStream_t st, const mtgpu_assembly_s *a, const MatFreeMesh *mfm,
                  int pin_variant)
@@ -2466,7 +2616,7 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
         V.ch = best_ch;
         MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
     }
-    return MTGPU_OK;
+    return prec_tile_setup(V, nsm);
 }
 
 int survey_set_variant(Survey &V, int variant)
@@ -2552,8 +2702,8 @@ int survey_iter_timed(Survey &V, int reps, float *ms)
     MTGPU_TRY(cudaEventCreate(&e0));
     MTGPU_TRY(cudaEventCreate(&e1));
     MTGPU_TRY(cudaEventRecord(e0, V.st));
-    for (int q = 0; q < reps; q++) MTGPU_SP_DISPATCH(V.SP, iteration(V));
-    note_launches((unsigned long long)reps * ((V.G.m > 0 ? 4 : 3) + spmv_extra_launches(V.ch)));
+    for (int q = 0; q < reps; q++) MTGPU_SP_DISPATCH(V.SP, iteration(V, q));
+    note_launches((unsigned long long)reps * iteration_launches(V));
     MTGPU_TRY(cudaEventRecord(e1, V.st));
     MTGPU_TRY(cudaEventSynchronize(e1));
     MTGPU_TRY(cudaEventElapsedTime(ms, e0, e1));
@@ -2648,7 +2798,7 @@ int survey_begin(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, do
     R.verify = verify;
     V.eps = eps;
     if (iters_per_launch <= 0) iters_per_launch = 16;
-    R.ipl = iters_per_launch;
+    R.ipl = iters_per_launch + (iters_per_launch & 1);
     for (int k = 0; k < 32; k++) {
         SysState s{};
         s.status = k < V.S ? kRun : MTGPU_OK;
@@ -2685,7 +2835,8 @@ int survey_begin(Survey &V, const double2 *b_sys_major, double2 *x_sys_major, do
         V.graph = nullptr;
         cudaGraph_t g;
         MTGPU_TRY(cudaStreamBeginCapture(V.st, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < R.ipl; k++) MTGPU_SP_DISPATCH(V.SP, iteration(V));
+        // an even count: the fused preconditioner's a is back in V.a after the graph
+        for (int k = 0; k < R.ipl; k++) MTGPU_SP_DISPATCH(V.SP, iteration(V, k));
         // group update: the double-float increment of x goes into the FP64 x
         MTGPU_SP_DISPATCH(V.SP, fold(V, V.all_on));
         MTGPU_TRY(cudaStreamEndCapture(V.st, &g));
@@ -2716,7 +2867,7 @@ int survey_launch(Survey &V, SurveyRun &R)
         set_last_error(e, "cudaGraphLaunch", __FILE__, __LINE__);
         return MTGPU_ERR_CUDA;
     }
-    const unsigned long long kpi = (V.G.m > 0 ? 4 : 3) + spmv_extra_launches(V.ch);
+    const unsigned long long kpi = iteration_launches(V);
     note_launches(kpi * (unsigned long long)R.ipl + 1);
     R.guard += R.ipl;
     // the state arrives with the launch's end (read in survey_collect)

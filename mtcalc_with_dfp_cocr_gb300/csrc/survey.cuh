@@ -77,6 +77,13 @@ struct Survey {
     float4 *b = nullptr, *x = nullptr, *r = nullptr, *s = nullptr, *p = nullptr, *a = nullptr,
            *z = nullptr, *w = nullptr, *sm = nullptr;     // [row][SP]
     float4 *h = nullptr;                          // [node][SP]
+    // the fused preconditioner of tensor meshes (prec_tile.cuh): its launch
+    // grid, tiles x, y, z chunks, groups, planes per chunk, and the second
+    // buffer of a (read and written in different buffers, alternating)
+    bool prec_tile = false;
+    int g_pt = 0, pt[5] = {};
+    float prec_ms[2] = {};                        // set-up timing: ms per iteration unfused, fused
+    float4 *a2 = nullptr;
     double2 *b64 = nullptr, *xacc = nullptr;      // FP64 b and accumulated x: [row][SP]
     int *all_on = nullptr;                        // 32 flags, all set
     double *partials = nullptr;
@@ -159,6 +166,11 @@ int survey_finish(Survey &V, SurveyRun &R, mtgpu_survey_stats *stats, int stat_o
 int survey_spmv_timed(Survey &V, int reps, float *ms);
 int survey_spmv(Survey &V, const double2 *x_sys_major, double2 *y_sys_major);
 int survey_iter_timed(Survey &V, int reps, float *ms);
+// kernels one iteration launches
+inline int iteration_launches(const Survey &V)
+{
+    return (V.prec_tile ? 3 : (V.G.m > 0 ? 4 : 3)) + spmv_extra_launches(V.ch);
+}
 int survey_set_variant(Survey &V, int variant);
 
 }  // namespace mtgpu

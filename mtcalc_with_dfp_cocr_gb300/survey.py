@@ -92,6 +92,15 @@ class Survey:
                    "mtgpu_survey_tuning")
         return v.value, {c: ms[i] for i, c in enumerate(SPMV_VARIANTS) if ms[i] > 0}
 
+    def preconditioner(self):
+        """(fused, (ms per iteration unfused, fused)): whether the iteration's
+        folded preconditioner runs as one fused kernel (tensor meshes)."""
+        f = C.c_int()
+        ms = (C.c_float * 2)()
+        _lib.check(_lib.lib().mtgpu_survey_preconditioner(self._h, C.byref(f), ms),
+                   "mtgpu_survey_preconditioner")
+        return bool(f.value), (ms[0], ms[1])
+
     def set_spmv_variant(self, variant):
         """Pin the SpMV variant (0 x and matrix staged, 1 x staged, 2, 4, 8
         slots in flight, 18, 20 row per thread for two systems, 32-35

@@ -343,3 +343,43 @@ def test_face_mass_form_matches_two_kernel_form(gpu, name, S):
     assert d <= 1e-12 * y32.abs().max().item(), d
     sv.close()
     A.close()
+
+
+@pytest.mark.parametrize("name,systems", [("small", [(0.1, 1), (0.1, 0), (10.0, 1)]),
+                                          ("c1", [(1.0, 1), (1.0, 0)])])
+def test_fused_preconditioner(gpu, monkeypatch, name, systems):
+    """The folded preconditioner in one kernel (h of a tile's nodes in shared
+    memory) is enabled on these tensor meshes only after a set-up step of it
+    equals the node and edge kernels' bit for bit; forced on and off, the
+    solves reach the FP64 true residual with the same iteration counts up to
+    rounding (the (a, w) sums are grouped differently)."""
+    torch = gpu
+    res = {}
+    for force in ("1", "0"):
+        monkeypatch.setenv("MTGPU_PREC_TILE", force)
+        w = workloads.make(name)
+        nus = [f for f, _ in systems]
+        tabs = _tables(w, nus)
+        A = assembly.Assembly(w.mesh)
+        b = torch.empty(len(systems), 2 * w.mesh.nb, dtype=torch.float64, device="cuda")
+        A.rhs(nus, [a for _, a in systems], tabs[0][0], np.stack([t[1] for t in tabs]),
+              np.stack([t[2] for t in tabs]), b)
+        x = torch.zeros_like(b)
+        sv = survey.Survey(A, nus)
+        fused, _ = sv.preconditioner()
+        assert fused == (force == "1")
+        code, st = sv.solve(b, x, eps=1e-8, maxiter=20000, verify=True)
+        assert code == 0 and max(st["true_residual_rel"]) < 1e-8
+        res[force] = (st["iterations"], x.cpu().numpy())
+        sv.close()
+        A.close()
+    for i, j in zip(res["1"][0], res["0"][0]):
+        assert abs(i - j) <= 3 + 0.03 * j
+    w = workloads.make(name)
+    xyz = w.mesh.xyz()
+    e = w.mesh.edges()
+    earth = 0.5 * (xyz[e[:, 0], 2] + xyz[e[:, 1], 2]) <= 0.0
+    for k in range(len(systems)):
+        a = res["1"][1][k].view(np.complex128)[earth]
+        r = res["0"][1][k].view(np.complex128)[earth]
+        assert np.linalg.norm(a - r) <= 1e-7 * np.linalg.norm(r)
