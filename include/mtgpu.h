@@ -371,11 +371,11 @@ int mtgpu_survey_tuning(const mtgpu_survey *s, int *variant, float *ms);
 int mtgpu_survey_set_spmv_variant(mtgpu_survey *s, int variant);
 
 /* Whether the first batch runs the folded preconditioner of the iteration
- * as one fused kernel (*fused = 1: tensor meshes where a set-up step of it
- * equals the node and edge kernels' bit for bit and whole iterations with it
- * timed faster; the environment variable MTGPU_PREC_TILE=0 / 1 forces the
- * choice where it is allowed) and the set-up's ms per iteration without and
- * with it (ms[2], 0 when not timed).  No counterpart in the reference, whose
+ * as one fused kernel (*fused = 1; on request: the environment variable
+ * MTGPU_PREC_TILE=1 at mtgpu_survey_create, on tensor meshes where a set-up
+ * step of it equals the node and edge kernels' bit for bit — on GB300 it
+ * measured slower than them) and the set-up's ms per iteration without and
+ * with it (ms[2], 0 when not requested).  No counterpart in the reference, whose
  * ApplyPreconditionerComplex (Code/COCR_FP/FoldedPreconditioner.cpp:578-630)
  * runs G x, D_S and G^T as separate loops. */
 int mtgpu_survey_preconditioner(const mtgpu_survey *s, int *fused, float *ms);

@@ -2394,22 +2394,24 @@ int matfree_build(Survey &V, const MatFreeMesh &a, int kuz, int kpar, int nsm)
 
 namespace {
 
-// The fused preconditioner (prec_tile.cuh), where the mesh allows it: a
-// tensor mesh with the lattice's Dirichlet edges, every interior node a row
-// of G in node order, the compact G^T.  A set-up check runs one step of both
-// forms on the same pseudo-random vectors and compares p, a and w bit for
-// bit; then whole iterations of both are timed and the faster kept.
-// MTGPU_PREC_TILE=0 / 1 (environment) forces the choice where allowed.
+// The fused preconditioner (prec_tile.cuh), on request (MTGPU_PREC_TILE=1
+// in the environment: on GB300 it measured slower than the node and edge
+// kernels on every benchmark workload, 0.72 against 0.59 ms per iteration
+// on c2 at 2 systems, 3.8 against 2.1 ms on c3 at 32) and where the mesh
+// allows it: a tensor mesh with the lattice's Dirichlet edges, every
+// interior node a row of G in node order, the compact G^T.  A set-up check
+// runs one step of both forms on the same pseudo-random vectors and keeps
+// the fused one only if p, a and w agree bit for bit.
 int prec_tile_setup(Survey &V, int nsm)
 {
     V.prec_tile = false;
+    const char *force = getenv("MTGPU_PREC_TILE");
+    if (!force || *force != '1') return MTGPU_OK;
     if (!V.mf.on || !V.mf.lattice || !V.G.d_tn) return MTGPU_OK;
     const long long mi = (long long)(V.mf.nx - 2) * (V.mf.ny - 2) * (V.mf.nz - 2);
     if (V.G.m != mi) return MTGPU_OK;
     MTGPU_SP_DISPATCH(V.SP, prec_grid(V, nsm));
     if (V.g_pt < 1 || V.g_pt > V.pblocks) return MTGPU_OK;
-    const char *force = getenv("MTGPU_PREC_TILE");
-    if (force && *force == '0') return MTGPU_OK;
     const long long n = (long long)V.nb * V.SP;
     int rc;
     if (!V.a2 && (rc = dev_alloc(&V.a2, (size_t)n))) return rc;
@@ -2466,19 +2468,14 @@ int prec_tile_setup(Survey &V, int nsm)
         dev_free(V.a2);
         return MTGPU_OK;
     }
-    bool use = true;
-    if (!(force && *force == '1')) {
-        float t_un = 0.f, t_fu = 0.f;
-        V.prec_tile = false;
-        if ((rc = survey_iter_timed(V, 2, &t_un)) || (rc = survey_iter_timed(V, 4, &t_un))) return rc;
-        V.prec_tile = true;
-        if ((rc = survey_iter_timed(V, 2, &t_fu)) || (rc = survey_iter_timed(V, 4, &t_fu))) return rc;
-        use = t_fu < t_un;
-        V.prec_ms[0] = t_un / 4.f;
-        V.prec_ms[1] = t_fu / 4.f;
-    }
-    V.prec_tile = use;
-    if (!use) dev_free(V.a2);
+    // both forms' whole iterations timed, for the record
+    float t_un = 0.f, t_fu = 0.f;
+    V.prec_tile = false;
+    if ((rc = survey_iter_timed(V, 2, &t_un)) || (rc = survey_iter_timed(V, 4, &t_un))) return rc;
+    V.prec_tile = true;
+    if ((rc = survey_iter_timed(V, 2, &t_fu)) || (rc = survey_iter_timed(V, 4, &t_fu))) return rc;
+    V.prec_ms[0] = t_un / 4.f;
+    V.prec_ms[1] = t_fu / 4.f;
     return MTGPU_OK;
 }
 
