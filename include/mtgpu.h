@@ -255,6 +255,12 @@ int mtgpu_assembly_rhs(mtgpu_assembly *a, int S, const double *nu, const int *al
 int mtgpu_cocr_create_from_assembly(mtgpu_assembly *a, double nu, void *stream,
                                     mtgpu_cocr **out);
 
+/* Self-check of the solver set-up: builds the folded preconditioner's G
+ * and G^T for the assembly's mesh on the device (as every solver set-up
+ * does) and by the host construction, and sets *equal = 1 if they agree
+ * entry for entry (row pointers, columns, values, order), else 0. */
+int mtgpu_assembly_check_preconditioner(mtgpu_assembly *a, int *equal);
+
 void mtgpu_assembly_destroy(mtgpu_assembly *a);
 
 /* ------------------------------------------------------------------------

@@ -106,6 +106,7 @@ SIGNATURES = {
                                           _i, _i, _i, _i, _d, _d, _d]),
     "mtgpu_assembly_rhs": (C.c_int, [_vp, C.c_int, _d, _i, C.c_int, _d, _d, _d, _vp]),
     "mtgpu_cocr_create_from_assembly": (C.c_int, [_vp, C.c_double, _vp, C.POINTER(_vp)]),
+    "mtgpu_assembly_check_preconditioner": (C.c_int, [_vp, C.POINTER(C.c_int)]),
     "mtgpu_assembly_destroy": (None, [_vp]),
     "mtgpu_survey_create": (C.c_int, [_vp, C.c_int, _d, _vp, C.POINTER(_vp)]),
     "mtgpu_survey_solve": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int, C.c_int,

@@ -86,6 +86,14 @@ class Assembly:
                                                   C.byref(d)), "mtgpu_assembly_info")
         return dict(nnz_complex=a.value, nnz_real=b.value, nnz_lower=c.value, gg_len=d.value)
 
+    def check_preconditioner(self):
+        """True if the folded preconditioner's G and G^T built on the device
+        (every solver set-up) equal the host construction entry for entry."""
+        eq = C.c_int()
+        _lib.check(_lib.lib().mtgpu_assembly_check_preconditioner(self._h, C.byref(eq)),
+                   "mtgpu_assembly_check_preconditioner")
+        return bool(eq.value)
+
     def block2x2(self, nu, alfa, z1d, usin, ucos, eps=1e-8, maxiter=10000) -> BlockSLAE:
         inf = self.info()
         nb, nnz = self.nb, inf["nnz_lower"]

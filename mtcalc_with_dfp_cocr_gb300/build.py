@@ -20,7 +20,7 @@ LIB = os.path.join(OUT, "libmtgpu.so")
 EXE = os.path.join(OUT, "mtgpu_cocr_fp")
 
 CU_SOURCES = ["sell.cu", "folded.cu", "cocr.cu", "assemble.cu", "survey.cu", "capi.cu", "capi_assembly.cu",
-              "noalloc.cu", "receivers.cu", "adjoint.cu", "smoothing.cu", "regular_mesh.cu"]
+              "noalloc.cu", "receivers.cu", "adjoint.cu", "smoothing.cu", "regular_mesh.cu", "scan.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

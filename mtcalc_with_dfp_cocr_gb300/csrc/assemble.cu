@@ -34,6 +34,7 @@ void ParamMatrix::release()
     dev_free(d_xyz); dev_free(d_nver); dev_free(d_ed); dev_free(d_edges); dev_free(d_nvkat);
     dev_free(d_mu); dev_free(d_sig); dev_free(d_sig0);
     dev_free(d_bedge);
+    dev_free(d_bnode);
     nb = nslices = 0;
 }
 
@@ -479,7 +480,7 @@ int param_assemble(const mtgpu_fem_mesh &m, ParamMatrix &P, cudaStream_t st)
         k_bnode<<<ceil_div(m.n_bound, kThreads), kThreads, 0, st>>>(m.n_bound, d_bnd, bnode);
     }
     rc = param_build(P, bnode, st);
-    dev_free(bnode);
+    P.d_bnode = bnode;   // kept for the solver set-up (preconditioner, matrix-free tables)
     dev_free(d_bnd);
     return rc;
 }

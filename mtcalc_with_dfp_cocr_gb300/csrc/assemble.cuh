@@ -26,6 +26,7 @@ struct ParamMatrix {
     int *d_nver = nullptr, *d_ed = nullptr, *d_edges = nullptr, *d_nvkat = nullptr;
     double *d_mu = nullptr, *d_sig = nullptr, *d_sig0 = nullptr;
     unsigned char *d_bedge = nullptr;                  // Dirichlet edges
+    unsigned char *d_bnode = nullptr;                  // Dirichlet nodes
     void release();
 };
 

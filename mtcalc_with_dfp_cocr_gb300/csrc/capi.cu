@@ -193,11 +193,8 @@ int solve_double_float_host(int nb, const int *ig, const int *jg, const int *idi
             int nmat = 0;
             for (int c = 0; c < kpar; c++) nmat = std::max(nmat, nvkat[c] + 1);
             mm.xyz = xyz;
-            mm.nver = nver14;
             mm.nver_stride = 14;
             mm.nvkat = nvkat;
-            mm.edges = edges2;
-            mm.bound = is_node_bound;
             mm.mu.assign(nmat, kMu0);
             mm.sigma.assign(sigma3d, sigma3d + nmat);
             mm.idi = idi;

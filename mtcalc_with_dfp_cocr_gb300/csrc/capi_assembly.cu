@@ -112,6 +112,52 @@ void mtgpu_assembly_destroy(mtgpu_assembly *a)
     delete a;
 }
 
+int mtgpu_assembly_check_preconditioner(mtgpu_assembly *a, int *equal)
+{
+    MTGPU_CHECK_ARG(a && equal, "null argument");
+    *equal = 0;
+    const ParamMatrix &P = a->P;
+    const mtgpu_mesh_desc mesh{P.kpar, P.nb, P.kuzlov, a->nvkat.data(), a->nver.data(),
+                               a->sigflag.data(), a->edges.data(), a->ig_t.data(), a->ig_t.data(),
+                               nullptr, a->bound.data(), a->nver_stride};
+    Folded H, D;
+    DevMeshUpload dmu;
+    bool conforming = false;
+    int rc;
+    if ((rc = folded_build_g(mesh, H, a->st)) ||
+        (rc = dmu.over_device(P.kpar, P.nb, P.kuzlov, P.nver_stride, P.d_xyz, P.d_nver, P.d_nvkat,
+                              P.d_edges, P.d_bnode, a->sigflag.data(), (int)a->sigflag.size(),
+                              a->st)) ||
+        (rc = folded_build_g_device(dmu.view, D, a->st, &conforming)))
+        return rc;
+    if (!conforming || H.n != D.n || H.m != D.m || !H.d_tn || !D.d_tn) return MTGPU_OK;
+    const int n = H.n, m = H.m;
+    int nnz_h = 0, nnz_d = 0;
+    MTGPU_TRY(cudaMemcpyAsync(&nnz_h, H.d_gp + m, sizeof(int), cudaMemcpyDeviceToHost, a->st));
+    MTGPU_TRY(cudaMemcpyAsync(&nnz_d, D.d_gp + m, sizeof(int), cudaMemcpyDeviceToHost, a->st));
+    MTGPU_TRY(cudaStreamSynchronize(a->st));
+    if (nnz_h != nnz_d) return MTGPU_OK;
+    bool same = true;
+    auto cmp = [&](const void *dh, const void *dd, size_t bytes) -> int {
+        if (!same || bytes == 0) return MTGPU_OK;
+        std::vector<unsigned char> x(bytes), y(bytes);
+        MTGPU_TRY(cudaMemcpyAsync(x.data(), dh, bytes, cudaMemcpyDeviceToHost, a->st));
+        MTGPU_TRY(cudaMemcpyAsync(y.data(), dd, bytes, cudaMemcpyDeviceToHost, a->st));
+        MTGPU_TRY(cudaStreamSynchronize(a->st));
+        same = x == y;
+        return MTGPU_OK;
+    };
+    const size_t nz = (size_t)nnz_h;
+    if ((rc = cmp(H.d_gp, D.d_gp, sizeof(int) * ((size_t)m + 1))) ||
+        (rc = cmp(H.d_gj, D.d_gj, sizeof(int) * nz)) || (rc = cmp(H.d_gv, D.d_gv, sizeof(double) * nz)) ||
+        (rc = cmp(H.d_tp, D.d_tp, sizeof(int) * ((size_t)n + 1))) ||
+        (rc = cmp(H.d_tj, D.d_tj, sizeof(int) * nz)) || (rc = cmp(H.d_tv, D.d_tv, sizeof(double) * nz)) ||
+        (rc = cmp(H.d_tn, D.d_tn, sizeof(int2) * (size_t)n)))
+        return rc;
+    *equal = same ? 1 : 0;
+    return MTGPU_OK;
+}
+
 int mtgpu_assembly_info(const mtgpu_assembly *a, long long *nnz_complex, long long *nnz_real,
                         int *nnz_lower, long long *gg_len)
 {
@@ -420,6 +466,10 @@ int mtgpu_survey_preconditioner(const mtgpu_survey *s, int *fused, float *ms)
 int mtgpu_survey_set_spmv_variant(mtgpu_survey *s, int variant)
 {
     MTGPU_CHECK_ARG(s != nullptr, "null survey");
+    for (auto &g : s->groups) {
+        const int rc = survey_prepare_variant(*g, variant);
+        if (rc) return rc;
+    }
     for (auto &g : s->groups)
         MTGPU_CHECK_ARG(spmv_variant_available(*g, variant),
                         "unknown SpMV variant, or not available for this survey");

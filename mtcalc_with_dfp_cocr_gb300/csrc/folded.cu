@@ -106,6 +106,242 @@ int folded_build_g(const mtgpu_mesh_desc &mesh, Folded &P, cudaStream_t st)
     return MTGPU_OK;
 }
 
+// ------------------------------------------------ G on the device
+namespace {
+
+// nodes of conductive cells that are not Dirichlet get a G row
+__global__ void k_g_mark(int kpar, const int *__restrict__ nver, int stride,
+                         const int *__restrict__ nvkat, const double *__restrict__ sigflag, int nmat,
+                         int nn, const unsigned char *__restrict__ bnode, int *in_sig)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= kpar) return;
+    const int mat = nvkat[c];
+    if (mat < 0 || mat >= nmat || !(sigflag[mat] > 0.0)) return;
+    for (int j = 0; j < 8; j++) {
+        const int v = nver[(size_t)c * stride + j];
+        if (v >= 0 && v < nn && !bnode[v]) in_sig[v] = 1;
+    }
+}
+
+// per edge its two nodes' G rows (-1 where none), the G^T row length and
+// the G row lengths; *beyond counts edges with a node past nn
+__global__ void k_g_edges(int ne, const int *__restrict__ edges, int nn, const int *__restrict__ in_sig,
+                          const int *__restrict__ renum, int2 *tn, int *cnt_t, int *deg, int *beyond)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    int r[2];
+    for (int k = 0; k < 2; k++) {
+        const int v = edges[2 * e + k];
+        if (v >= nn) atomicAdd(beyond, 1);
+        r[k] = v >= 0 && v < nn && in_sig[v] ? renum[v] : -1;
+    }
+    tn[e] = make_int2(r[0], r[1]);
+    cnt_t[e] = (r[0] >= 0) + (r[1] >= 0);
+    if (r[0] >= 0) atomicAdd(&deg[r[0]], 1);
+    if (r[1] >= 0) atomicAdd(&deg[r[1]], 1);
+}
+
+// G^T rows in place (first node -1/2, then second +1/2); G entries at
+// claimed positions of their rows (sorted afterwards)
+__global__ void k_g_fill(int ne, const int2 *__restrict__ tn, const int *__restrict__ tp,
+                         const int *__restrict__ gp, int *fill, int *tj, double *tv, int *gj,
+                         double *gv)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    const int2 r = tn[e];
+    int t = tp[e];
+    const int rr[2] = {r.x, r.y};
+    for (int k = 0; k < 2; k++) {
+        if (rr[k] < 0) continue;
+        const double g = k == 0 ? -0.5 : 0.5;
+        tj[t] = rr[k];
+        tv[t] = g;
+        t++;
+        const int q = gp[rr[k]] + atomicAdd(&fill[rr[k]], 1);
+        gj[q] = e;
+        gv[q] = g;
+    }
+}
+
+// every G row by increasing edge (the order of the host construction)
+__global__ void k_g_sort(int m, const int *__restrict__ gp, int *gj, double *gv)
+{
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= m) return;
+    const int b = gp[v], e = gp[v + 1];
+    for (int i = b + 1; i < e; i++) {
+        const int kj = gj[i];
+        const double kv = gv[i];
+        int j = i - 1;
+        while (j >= b && gj[j] > kj) {
+            gj[j + 1] = gj[j];
+            gv[j + 1] = gv[j];
+            j--;
+        }
+        gj[j + 1] = kj;
+        gv[j + 1] = kv;
+    }
+}
+
+__global__ void k_int_to_flag(int n, const int *__restrict__ in, unsigned char *out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = in[i] != 0;
+}
+
+}  // namespace
+
+int folded_build_g_device(const DevMesh &dm, Folded &P, cudaStream_t st, bool *conforming)
+{
+    P.release();
+    *conforming = true;
+    const int ne = dm.nb, nn = dm.nn;
+    MTGPU_CHECK_ARG(ne > 0 && nn > 0, "empty mesh");
+    MTGPU_CHECK_ARG(dm.nver && dm.nvkat && dm.edges && dm.sigflag && dm.bnode, "mesh tables missing");
+    int *in_sig = nullptr, *renum = nullptr, *cnt_t = nullptr, *deg = nullptr, *fill = nullptr,
+        *beyond = nullptr;
+    auto done = [&](int code) {
+        dev_free(in_sig); dev_free(renum); dev_free(cnt_t); dev_free(deg); dev_free(fill);
+        dev_free(beyond);
+        if (code != MTGPU_OK || !*conforming) P.release();
+        return code;
+    };
+    int rc;
+    if ((rc = dev_alloc(&in_sig, nn)) || (rc = dev_alloc(&renum, (size_t)nn + 1)) ||
+        (rc = dev_alloc(&beyond, 1)))
+        return done(rc);
+    MTGPU_TRY(cudaMemsetAsync(in_sig, 0, sizeof(int) * nn, st));
+    MTGPU_TRY(cudaMemsetAsync(beyond, 0, sizeof(int), st));
+    if (dm.kpar > 0)
+        k_g_mark<<<ceil_div(dm.kpar, kThreads), kThreads, 0, st>>>(dm.kpar, dm.nver, dm.nver_stride,
+                                                                  dm.nvkat, dm.sigflag, dm.nmat, nn,
+                                                                  dm.bnode, in_sig);
+    note_launches(1);
+    long long m64 = 0;
+    if ((rc = dev_exclusive_scan(in_sig, nn, renum, &m64, st))) return done(rc);
+    const int m = (int)m64;
+    if ((rc = dev_alloc(&cnt_t, ne)) || (rc = dev_alloc(&deg, std::max(m, 1))) ||
+        (rc = dev_alloc(&fill, std::max(m, 1))) || (rc = dev_alloc(&P.d_tn, ne)) ||
+        (rc = dev_alloc(&P.d_tp, (size_t)ne + 1)) || (rc = dev_alloc(&P.d_gp, (size_t)m + 1)))
+        return done(rc);
+    MTGPU_TRY(cudaMemsetAsync(deg, 0, sizeof(int) * std::max(m, 1), st));
+    MTGPU_TRY(cudaMemsetAsync(fill, 0, sizeof(int) * std::max(m, 1), st));
+    k_g_edges<<<ceil_div(ne, kThreads), kThreads, 0, st>>>(ne, dm.edges, nn, in_sig, renum, P.d_tn,
+                                                          cnt_t, deg, beyond);
+    note_launches(1);
+    int nbeyond = 0;
+    MTGPU_TRY(cudaMemcpyAsync(&nbeyond, beyond, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MTGPU_TRY(cudaStreamSynchronize(st));
+    if (nbeyond > 0) {
+        *conforming = false;
+        return done(MTGPU_OK);
+    }
+    long long nnz = 0, nnz_g = 0;
+    if ((rc = dev_exclusive_scan(cnt_t, ne, P.d_tp, &nnz, st)) ||
+        (rc = dev_exclusive_scan(deg, m, P.d_gp, &nnz_g, st)))
+        return done(rc);
+    MTGPU_CHECK_ARG(nnz == nnz_g, "G and G^T entry counts differ");
+    if ((rc = dev_alloc(&P.d_tj, nnz)) || (rc = dev_alloc(&P.d_tv, nnz)) ||
+        (rc = dev_alloc(&P.d_gj, nnz)) || (rc = dev_alloc(&P.d_gv, nnz)) ||
+        (rc = dev_alloc(&P.d_da, ne)) || (rc = dev_alloc(&P.d_ds, m)) || (rc = dev_alloc(&P.d_h, m)))
+        return done(rc);
+    k_g_fill<<<ceil_div(ne, kThreads), kThreads, 0, st>>>(ne, P.d_tn, P.d_tp, P.d_gp, fill, P.d_tj,
+                                                         P.d_tv, P.d_gj, P.d_gv);
+    if (m > 0) k_g_sort<<<ceil_div(m, kThreads), kThreads, 0, st>>>(m, P.d_gp, P.d_gj, P.d_gv);
+    note_launches(2);
+    MTGPU_TRY(cudaGetLastError());
+    P.n = ne;
+    P.m = m;
+    return done(MTGPU_OK);
+}
+
+void DevMeshUpload::release()
+{
+    dev_free(nver); dev_free(nvkat); dev_free(edges); dev_free(xyz); dev_free(sigflag);
+    dev_free(bnode);
+    view = DevMesh{};
+}
+
+int DevMeshUpload::upload(const mtgpu_mesh_desc &m, const double *xyz_host, cudaStream_t st)
+{
+    release();
+    int nmat = 0;
+    for (int c = 0; c < m.kpar; c++) nmat = std::max(nmat, m.nvkat[c] + 1);
+    nmat = std::max(nmat, 1);
+    int *bound_i = nullptr;
+    int rc;
+    if ((rc = dev_alloc(&nver, (size_t)m.kpar * m.nver_stride)) ||
+        (rc = dev_alloc(&nvkat, (size_t)m.kpar)) || (rc = dev_alloc(&edges, (size_t)m.n_edges_c * 2)) ||
+        (rc = dev_alloc(&sigflag, (size_t)nmat)) || (rc = dev_alloc(&bnode, (size_t)m.n_nodes_c)) ||
+        (rc = dev_alloc(&bound_i, (size_t)m.n_nodes_c)) ||
+        (xyz_host && (rc = dev_alloc(&xyz, (size_t)m.n_nodes_c * 3)))) {
+        dev_free(bound_i);
+        return rc;
+    }
+    cudaError_t e = cudaSuccess;
+    auto up = [&](void *d, const void *h, size_t bytes) {
+        if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, st);
+    };
+    up(nver, m.nver14, sizeof(int) * (size_t)m.kpar * m.nver_stride);
+    up(nvkat, m.nvkat, sizeof(int) * (size_t)m.kpar);
+    up(edges, m.edges2, sizeof(int) * (size_t)m.n_edges_c * 2);
+    up(sigflag, m.sigma3d, sizeof(double) * (size_t)nmat);
+    up(bound_i, m.is_node_bound, sizeof(int) * (size_t)m.n_nodes_c);
+    if (xyz_host) up(xyz, xyz_host, sizeof(double) * (size_t)m.n_nodes_c * 3);
+    if (e == cudaSuccess) {
+        k_int_to_flag<<<ceil_div(m.n_nodes_c, kThreads), kThreads, 0, st>>>(m.n_nodes_c, bound_i, bnode);
+        note_launches(1);
+        e = cudaGetLastError();
+    }
+    // the host arrays are the caller's: the copies must end before it returns
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    dev_free(bound_i);
+    if (e != cudaSuccess) {
+        set_last_error(e, "mesh upload", __FILE__, __LINE__);
+        return MTGPU_ERR_CUDA;
+    }
+    view.kpar = m.kpar;
+    view.nb = m.n_edges_c;
+    view.nn = m.n_nodes_c;
+    view.nver_stride = m.nver_stride;
+    view.nmat = nmat;
+    view.xyz = xyz;
+    view.nver = nver;
+    view.nvkat = nvkat;
+    view.edges = edges;
+    view.sigflag = sigflag;
+    view.bnode = bnode;
+    return MTGPU_OK;
+}
+
+int DevMeshUpload::over_device(int kpar, int nb, int nn, int nver_stride, const double *d_xyz,
+                               const int *d_nver, const int *d_nvkat, const int *d_edges,
+                               const unsigned char *d_bnode, const double *sigflag_host, int nmat,
+                               cudaStream_t st)
+{
+    release();
+    nmat = std::max(nmat, 1);
+    int rc = dev_alloc(&sigflag, (size_t)nmat);
+    if (rc) return rc;
+    MTGPU_TRY(cudaMemcpyAsync(sigflag, sigflag_host, sizeof(double) * nmat, cudaMemcpyHostToDevice, st));
+    MTGPU_TRY(cudaStreamSynchronize(st));
+    view.kpar = kpar;
+    view.nb = nb;
+    view.nn = nn;
+    view.nver_stride = nver_stride;
+    view.nmat = nmat;
+    view.xyz = d_xyz;
+    view.nver = d_nver;
+    view.nvkat = d_nvkat;
+    view.edges = d_edges;
+    view.sigflag = sigflag;
+    view.bnode = d_bnode;
+    return MTGPU_OK;
+}
+
 namespace {
 
 __device__ inline long long slot(const long long *p, int row, int k)

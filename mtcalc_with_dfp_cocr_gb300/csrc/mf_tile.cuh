@@ -184,7 +184,7 @@ k_mf_tile(MF M, MfTileGrid G, const float2 *__restrict__ omega, const float4 *__
                                : d == 1 ? (i == 0 || i == nx - 1 || P == 0 || P == nz - 1)
                                         : (i == 0 || i == nx - 1 || j == 0 || j == ny - 1);
                 if (has && !dir) {
-                    int e = __ldg(M.rb + P * ny + j) + i * (1 + ey + ezp);
+                    int e = mf_line(M, j, P) + i * (1 + ey + ezp);
                     if (d >= 1) e += ex;
                     if (d == 2) e += ey;
                     src = s + (long long)e * SP + sys0 + u;
@@ -249,7 +249,7 @@ k_mf_tile(MF M, MfTileGrid G, const float2 *__restrict__ omega, const float4 *__
         __syncthreads();
         if (col && on) {
             const int ex = i < nx - 1, ey = j < ny - 1, ezp = k < nz - 1;
-            const int base = __ldg(M.rb + k * ny + j) + i * (1 + ey + ezp);
+            const int base = mf_line(M, j, k) + i * (1 + ey + ezp);
             // x-edge (D = 0, T1 = y, T2 = z)
             if (ex) {
                 const long long idx = (long long)base * SP + kme;

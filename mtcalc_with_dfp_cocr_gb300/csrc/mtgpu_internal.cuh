@@ -87,6 +87,39 @@ struct Folded {
 // Host construction of G and G^T (FoldedPreconditioner.cpp:68-259 semantics),
 // uploaded to the device.
 int folded_build_g(const mtgpu_mesh_desc &mesh, Folded &P, cudaStream_t st);
+
+// Device copies of the mesh tables that the set-up stages read (0-based)
+struct DevMesh {
+    int kpar = 0, nb = 0, nn = 0, nver_stride = 8, nmat = 0;
+    const double *xyz = nullptr;            // [nn][3]; null where not needed
+    const int *nver = nullptr;              // [kpar][nver_stride]
+    const int *nvkat = nullptr;             // [kpar]
+    const int *edges = nullptr;             // [nb][2]
+    const double *sigflag = nullptr;        // [nmat]: > 0 for conductive materials
+    const unsigned char *bnode = nullptr;   // [nn]: Dirichlet nodes
+};
+// A DevMesh over uploads of a host mesh description (or over tables
+// already on the device plus the uploaded material flags); the uploads are
+// freed with the object
+struct DevMeshUpload {
+    DevMesh view;
+    int *nver = nullptr, *nvkat = nullptr, *edges = nullptr;
+    double *xyz = nullptr, *sigflag = nullptr;
+    unsigned char *bnode = nullptr;
+    int upload(const mtgpu_mesh_desc &m, const double *xyz_host, cudaStream_t st);
+    int over_device(int kpar, int nb, int nn, int nver_stride, const double *d_xyz,
+                    const int *d_nver, const int *d_nvkat, const int *d_edges,
+                    const unsigned char *d_bnode, const double *sigflag_host, int nmat,
+                    cudaStream_t st);
+    void release();
+    ~DevMeshUpload() { release(); }
+};
+// G and G^T built on the device (same rows, entries and order as
+// folded_build_g); *conforming = false, and nothing built, when an edge
+// has a node beyond nn (T-matrix meshes: folded_build_g handles them)
+int folded_build_g_device(const DevMesh &dm, Folded &P, cudaStream_t st, bool *conforming);
+// exclusive prefix sum: out[0..n] (out[n] = total), *total on the host
+int dev_exclusive_scan(const int *d_in, long long n, int *d_out, long long *total, cudaStream_t st);
 // D_A and D_S from the device matrix.
 int folded_build_diag(const SellMatrix &A, Folded &P, cudaStream_t st);
 // y = D_A x + G^T D_S G x

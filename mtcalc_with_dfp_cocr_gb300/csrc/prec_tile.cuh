@@ -91,7 +91,7 @@ k_prec_tile(MF M, PrecGrid G, const float4 *__restrict__ ds, const float4 *__res
             if (P >= 0 && P < nz && i >= 0 && i < nx && j >= 0 && j < ny) {
                 const int ex = i < nx - 1, ey = j < ny - 1, ezp = P < nz - 1;
                 if (d == 0 ? ex : (d == 1 ? ey : ezp)) {
-                    int e = __ldg(M.rb + P * ny + j) + i * (1 + ey + ezp);
+                    int e = mf_line(M, j, P) + i * (1 + ey + ezp);
                     if (d >= 1) e += ex;
                     if (d == 2) e += ey;
                     const long long idx = (long long)e * SP + sys0 + u;
@@ -146,7 +146,7 @@ k_prec_tile(MF M, PrecGrid G, const float4 *__restrict__ ds, const float4 *__res
         __syncthreads();
         if (col) {
             const int ex = i < nx - 1, ey = j < ny - 1, ezp = k < nz - 1;
-            const int base = __ldg(M.rb + k * ny + j) + i * (1 + ey + ezp);
+            const int base = mf_line(M, j, k) + i * (1 + ey + ezp);
 #pragma unroll
             for (int d = 0; d < 3; d++) {
                 if (!(d == 0 ? ex : (d == 1 ? ey : ezp))) continue;

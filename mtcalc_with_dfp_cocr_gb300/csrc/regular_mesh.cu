@@ -157,6 +157,8 @@ int param_assemble_regular(int nx, int ny, int nz, const double *x, const double
         return done(MTGPU_ERR_CUDA);
     }
     rc = param_build(P, bnode, st);
+    P.d_bnode = bnode;   // kept for the solver set-up (preconditioner, matrix-free tables)
+    bnode = nullptr;
     return done(rc);
 }
 

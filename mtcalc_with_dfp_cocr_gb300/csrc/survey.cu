@@ -29,6 +29,7 @@
 #include "dfloat.cuh"
 
 #include <algorithm>
+#include <chrono>
 #include <climits>
 #include <cstdlib>
 #include <cstring>
@@ -52,6 +53,7 @@ void Survey::release()
     dev_free(b64); dev_free(xacc); dev_free(all_on);
     dev_free(uoff); dev_free(ucol); dev_free(lc); dev_free(lr);
     ntiles = 0;
+    tiles_built = false;
     dev_free(partials);
     if (hsys) cudaFreeHost(hsys);
     hsys = nullptr;
@@ -61,7 +63,6 @@ void Survey::release()
 
 void MatFree::release()
 {
-    dev_free(rb);
     dev_free(pos);
     dev_free(bedge);
     dev_free(w);
@@ -69,6 +70,8 @@ void MatFree::release()
     dev_free(g);
     on = false;
     lattice = false;
+    tiled = false;
+    tile_checked = false;
     gface = false;
 }
 
@@ -723,7 +726,8 @@ struct MF {
     int nx, ny, nz;
     long long nfx, nfy, nfz, ncell;
     int nex, ney;              // x- and y-edges: the first two segments of the row order
-    const int *rb;
+    int plane, l3, l2;         // edges per node plane below the top one; per node line below / in it
+    int lat;                   // Dirichlet edges are the lattice's (every surface node Dirichlet)
     const unsigned *pos;       // row (direction-major order) -> i | j << 10 | k << 20
     const float2 *w;
     const unsigned char *bedge;
@@ -731,16 +735,37 @@ struct MF {
     float4 *g;                 // F f (variant 35)
 };
 
+// first edge of node line (j, k): the node planes below, then the lines
+// before it in its plane (edges are numbered node by node, each node's +x,
+// +y, +z edge where present; the set-up verified this numbering)
+__device__ __forceinline__ int mf_line(const MF &M, int j, int k)
+{
+    return k * M.plane + j * (k < M.nz - 1 ? M.l3 : M.l2);
+}
+
 // edge of direction d leaving node (i, j, k): the node's first edge
-// rb + i (1 + [j < ny-1] + [k < nz-1]), then +x, +y, +z as present
+// mf_line + i (1 + [j < ny-1] + [k < nz-1]), then +x, +y, +z as present
 // (32-bit: the set-up keeps edges x systems and faces x systems below 2^31)
 __device__ __forceinline__ int mf_edge(const MF &M, int d, int i, int j, int k)
 {
     const int ey = j < M.ny - 1, ex = i < M.nx - 1;
-    int e = __ldg(M.rb + k * M.ny + j) + i * (1 + ey + (k < M.nz - 1));
+    int e = mf_line(M, j, k) + i * (1 + ey + (k < M.nz - 1));
     if (d >= 1) e += ex;
     if (d == 2) e += ey;
     return e;
+}
+
+// whether the +d edge e of node (i, j, k) is Dirichlet: on lattice meshes
+// iff one of its two transverse node lines lies on the surface, else the
+// per-edge flag (both nodes flagged)
+__device__ __forceinline__ bool mf_dirichlet(const MF &M, int d, int i, int j, int k, int e)
+{
+    if (M.lat) {
+        const bool bi = i == 0 || i == M.nx - 1, bj = j == 0 || j == M.ny - 1,
+                   bk = k == 0 || k == M.nz - 1;
+        return d == 0 ? (bj || bk) : (d == 1 ? (bi || bk) : (bi || bj));
+    }
+    return __ldg(M.bedge + e) != 0;
 }
 
 // face of normal n at (i, j, k): line index along n, cell indices across
@@ -751,10 +776,13 @@ __device__ __forceinline__ int mf_face(const MF &M, int n, int i, int j, int k)
     return (int)(M.nfx + M.nfy) + (k * (M.ny - 1) + j) * (M.nx - 1) + i;
 }
 
+// x of the +d edge of node (i, j, kk) for system k, 0 on Dirichlet edges
 template <int SP>
-__device__ __forceinline__ dfc mf_x(const MF &M, const float4 *__restrict__ x, int e, int k)
+__device__ __forceinline__ dfc mf_x(const MF &M, const float4 *__restrict__ x, int d, int i, int j,
+                                    int kk, int k)
 {
-    if (__ldg(M.bedge + e)) return dfc{df{0.f, 0.f}, df{0.f, 0.f}};
+    const int e = mf_edge(M, d, i, j, kk);
+    if (mf_dirichlet(M, d, i, j, kk, e)) return dfc{df{0.f, 0.f}, df{0.f, 0.f}};
     return from4(__ldg(x + e * SP + k));
 }
 
@@ -792,25 +820,23 @@ k_mf_faces(MF M, const float4 *__restrict__ x, const SysState *sys)
             j = (int)(q % (M.ny - 1));
             kk = (int)(q / (M.ny - 1));
         }
-        int e0, e1, e2, e3;
+        dfc a, b, c, d;
         if (n == 0) {
-            e0 = mf_edge(M, 1, i, j, kk);
-            e1 = mf_edge(M, 2, i, j + 1, kk);
-            e2 = mf_edge(M, 1, i, j, kk + 1);
-            e3 = mf_edge(M, 2, i, j, kk);
+            a = mf_x<SP>(M, x, 1, i, j, kk, k);
+            b = mf_x<SP>(M, x, 2, i, j + 1, kk, k);
+            c = mf_x<SP>(M, x, 1, i, j, kk + 1, k);
+            d = mf_x<SP>(M, x, 2, i, j, kk, k);
         } else if (n == 1) {
-            e0 = mf_edge(M, 2, i, j, kk);
-            e1 = mf_edge(M, 0, i, j, kk + 1);
-            e2 = mf_edge(M, 2, i + 1, j, kk);
-            e3 = mf_edge(M, 0, i, j, kk);
+            a = mf_x<SP>(M, x, 2, i, j, kk, k);
+            b = mf_x<SP>(M, x, 0, i, j, kk + 1, k);
+            c = mf_x<SP>(M, x, 2, i + 1, j, kk, k);
+            d = mf_x<SP>(M, x, 0, i, j, kk, k);
         } else {
-            e0 = mf_edge(M, 0, i, j, kk);
-            e1 = mf_edge(M, 1, i + 1, j, kk);
-            e2 = mf_edge(M, 0, i, j + 1, kk);
-            e3 = mf_edge(M, 1, i, j, kk);
+            a = mf_x<SP>(M, x, 0, i, j, kk, k);
+            b = mf_x<SP>(M, x, 1, i + 1, j, kk, k);
+            c = mf_x<SP>(M, x, 0, i, j + 1, kk, k);
+            d = mf_x<SP>(M, x, 1, i, j, kk, k);
         }
-        const dfc a = mf_x<SP>(M, x, e0, k), b = mf_x<SP>(M, x, e1, k);
-        const dfc c = mf_x<SP>(M, x, e2, k), d = mf_x<SP>(M, x, e3, k);
         acc fr, fi;
         fr.add(a.re); fr.add(b.re); fr.add(neg(c.re)); fr.add(neg(d.re));
         fi.add(a.im); fi.add(b.im); fi.add(neg(c.im)); fi.add(neg(d.im));
@@ -901,7 +927,7 @@ __device__ __forceinline__ dfc mf_row(const MF &M, Pos p, int k, df om, const fl
 #pragma unroll
         for (int b = 0; b < 3; b++) {
             const Pos q = mv<T2>(mv<T1>(p, a - 1), b - 1);
-            const dfc xe = mf_x<SP>(M, x, mf_edge(M, D, q.x, q.y, q.z), k);
+            const dfc xe = mf_x<SP>(M, x, D, q.x, q.y, q.z, k);
             mr.mac(cm[a][b], xe.re);
             mi.mac(cm[a][b], xe.im);
         }
@@ -978,7 +1004,7 @@ __device__ __forceinline__ void mf_row2(const MF &M, Pos p, int k0, const df (&o
         for (int b = 0; b < 3; b++) {
             const Pos q = mv<T2>(mv<T1>(p, a - 1), b - 1);
             const int e = mf_edge(M, D, q.x, q.y, q.z);
-            if (__ldg(M.bedge + e)) continue;
+            if (mf_dirichlet(M, D, q.x, q.y, q.z, e)) continue;
 #pragma unroll
             for (int u = 0; u < 2; u++) {
                 const dfc xe = from4(__ldg(x + e * SP + k0 + u));
@@ -1026,7 +1052,7 @@ k_mf_edges2(int nb, MF M, const float2 *__restrict__ omega, const float4 *__rest
             const long long i = (long long)e * SP + k0;
             const float4 sv[2] = {__ldg(s + i), __ldg(s + i + 1)};
             dfc y[2];
-            if (__ldg(M.bedge + e)) {
+            if (mf_dirichlet(M, d, p.x, p.y, p.z, e)) {
                 y[0] = from4(sv[0]);
                 y[1] = from4(sv[1]);
             } else if (d == 0) {
@@ -1084,7 +1110,7 @@ k_mf_edges(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restr
         const long long i = (long long)e * SP + k;
         const float4 sv4 = __ldg(s + i);
         dfc y;
-        if (__ldg(M.bedge + e))
+        if (mf_dirichlet(M, d, p.x, p.y, p.z, e))
             y = from4(sv4);
         else if (d == 0)
             y = mf_row<SP, 0>(M, p, k, om, s);
@@ -1207,7 +1233,7 @@ __device__ __forceinline__ dfc mf_row_g(const MF &M, Pos p, int k, df om, const 
 #pragma unroll
         for (int b = 0; b < 3; b++) {
             const Pos q = mv<T2>(mv<T1>(p, a - 1), b - 1);
-            const dfc xe = mf_x<SP>(M, x, mf_edge(M, D, q.x, q.y, q.z), k);
+            const dfc xe = mf_x<SP>(M, x, D, q.x, q.y, q.z, k);
             mr.mac(cm[a][b], xe.re);
             mi.mac(cm[a][b], xe.im);
         }
@@ -1240,7 +1266,7 @@ k_mf_edges_g(int nb, MF M, const float2 *__restrict__ omega, const float4 *__res
         const long long i = (long long)e * SP + k;
         const float4 sv4 = __ldg(s + i);
         dfc y;
-        if (__ldg(M.bedge + e))
+        if (mf_dirichlet(M, d, p.x, p.y, p.z, e))
             y = from4(sv4);
         else if (d == 0)
             y = mf_row_g<SP, 0>(M, p, k, om, s);
@@ -1761,8 +1787,9 @@ struct Impl {
         const MatFree &F = V.mf;
         return MF{F.nx, F.ny, F.nz, F.nfx, F.nfy, F.nfz,
                   (long long)(F.nx - 1) * (F.ny - 1) * (F.nz - 1),
-                  (F.nx - 1) * F.ny * F.nz, F.nx * (F.ny - 1) * F.nz, F.rb, F.pos, F.w,
-                  F.bedge, F.f, F.g};
+                  (F.nx - 1) * F.ny * F.nz, F.nx * (F.ny - 1) * F.nz,
+                  (F.ny - 1) * (3 * F.nx - 1) + (2 * F.nx - 1), 3 * F.nx - 1, 2 * F.nx - 1,
+                  F.lattice ? 1 : 0, F.pos, F.w, F.bedge, F.f, F.g};
     }
     static void spmv(Survey &V, int mode)
     {
@@ -2120,20 +2147,108 @@ int build_tiles(Survey &V, int nsm)
 
 namespace {
 
+// Set-up of the matrix-free tables on the device.  k_mfb_nodes checks
+// every node against the lattice (coordinates on the node lines, surface
+// nodes Dirichlet) and every edge against RegularMeshBuilder's numbering
+// (the +d edge of node (i, j, k) at its closed-form number joins n and its
+// +d neighbour), and writes the edge's Dirichlet flag and its row position;
+// k_mfb_cells checks the cells' nodes and materials and writes the weights.
+// bad[0] counts mismatches of the structure, bad[1] Dirichlet flags that
+// differ from the lattice rule.
+struct MfbLines {
+    const double *x, *y, *z;   // node lines
+    const double *mu, *sigma;  // per material
+    int nmat;
+};
+
+__global__ void k_mfb_nodes(MF M, MfbLines L, int nb, const double *__restrict__ xyz,
+                            const unsigned char *__restrict__ bnode, const int *__restrict__ edges,
+                            unsigned char *bedge, unsigned *pos, int *bad)
+{
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int nx = M.nx, ny = M.ny, nz = M.nz;
+    if (n >= (long long)nx * ny * nz) return;
+    const int i = (int)(n % nx), j = (int)((n / nx) % ny), k = (int)(n / ((long long)nx * ny));
+    int nbad = 0, nlat = 0;
+    if (xyz[3 * n] != L.x[i] || xyz[3 * n + 1] != L.y[j] || xyz[3 * n + 2] != L.z[k]) nbad++;
+    const bool bi = i == 0 || i == nx - 1, bj = j == 0 || j == ny - 1, bk = k == 0 || k == nz - 1;
+    if ((bi || bj || bk) && !bnode[n]) nbad++;
+    const int step[3] = {1, nx, nx * ny};
+    const bool has[3] = {i < nx - 1, j < ny - 1, k < nz - 1};
+    const bool want[3] = {bj || bk, bi || bk, bi || bj};
+    for (int d = 0; d < 3; d++) {
+        if (!has[d]) continue;
+        const int e = mf_edge(M, d, i, j, k);
+        if (e < 0 || e >= nb) {
+            nbad++;
+            continue;
+        }
+        const int n2 = (int)n + step[d];
+        if (edges[2 * e] != (int)n || edges[2 * e + 1] != n2) nbad++;
+        const bool be = bnode[n] && bnode[n2];
+        bedge[e] = be;
+        if (be != want[d]) nlat++;
+        long long row;
+        if (d == 0) row = ((long long)k * ny + j) * (nx - 1) + i;
+        else if (d == 1) row = M.nex + ((long long)k * (ny - 1) + j) * nx + i;
+        else row = (long long)M.nex + M.ney + ((long long)k * ny + j) * nx + i;
+        pos[row] = (unsigned)i | ((unsigned)j << 10) | ((unsigned)k << 20);
+    }
+    if (nbad) atomicAdd(&bad[0], nbad);
+    if (nlat) atomicAdd(&bad[1], nlat);
+}
+
+// weights of cell c: wF / 3 = 2 h_d / (h_t1 h_t2) / mu / 3 and
+// wM / 9 = sigma h_t1 h_t2 / h_d / 9 (times omega of a host SLAE), the
+// expressions and their order as FP64 on the host
+__global__ void k_mfb_cells(MF M, MfbLines L, const int *__restrict__ nver, int stride,
+                            const int *__restrict__ nvkat, double om, int scale, float2 *w, int *bad)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int nx = M.nx, ny = M.ny, nxy = nx * ny;
+    const int cx = nx - 1, cy = ny - 1;
+    if (c >= M.ncell) return;
+    const int i = (int)(c % cx), j = (int)((c / cx) % cy), k = (int)(c / ((long long)cx * cy));
+    int nbad = 0;
+    const int n0 = (k * ny + j) * nx + i;
+    const int want[8] = {n0, n0 + 1, n0 + nx, n0 + nx + 1,
+                         n0 + nxy, n0 + nxy + 1, n0 + nxy + nx, n0 + nxy + nx + 1};
+    for (int t = 0; t < 8; t++)
+        if (nver[(size_t)c * stride + t] != want[t]) nbad++;
+    const int mat = nvkat[c];
+    if (mat < 0 || mat >= L.nmat || !(L.mu[mat] > 0.0)) {
+        atomicAdd(&bad[0], nbad + 1);
+        return;
+    }
+    if (nbad) atomicAdd(&bad[0], nbad);
+    const double h[3] = {L.x[i + 1] - L.x[i], L.y[j + 1] - L.y[j], L.z[k + 1] - L.z[k]};
+    for (int d = 0; d < 3; d++) {
+        const int t1 = (d + 1) % 3, t2 = (d + 2) % 3;
+        const double wf = 2.0 * h[d] / (h[t1] * h[t2]) / L.mu[mat] / 3.0;
+        double wm = L.sigma[mat] * h[t1] * h[t2] / h[d] / 9.0;
+        if (scale) wm *= om;
+        const df f = from_double(wf), m = from_double(wm);
+        w[(size_t)d * M.ncell + c] = make_float2(f.h, f.l);
+        w[(size_t)(3 + d) * M.ncell + c] = make_float2(m.h, m.l);
+    }
+}
+
 // The matrix-free variant's tables, when the assembly's mesh is a tensor
 // mesh numbered as RegularMeshBuilder numbers it (nodes x fastest, cells
 // likewise, edges per node +x, +y, +z, every node of the outer surface a
-// Dirichlet node); anything else leaves the variant off.  A set-up check
-// compares one matrix-free product with the stored-matrix product and
-// leaves the variant off unless they agree to 1e-9.
-int matfree_build(Survey &V, const MatFreeMesh &a, int kuz, int kpar, int nsm)
+// Dirichlet node); anything else leaves the variant off.  The node lines
+// come from the host coordinates, every table check and every table from
+// the device mesh tables.  A set-up check compares one matrix-free product
+// with the stored-matrix product and leaves the variant off unless they
+// agree to 1e-9.
+int matfree_build(Survey &V, const MatFreeMesh &a, const DevMesh &dm, int kuz, int kpar, int nsm)
 {
     MatFree &F = V.mf;
     F.release();
     const ParamMatrix &P = *V.P;
-    const int ns = a.nver_stride;
     const double *xyz = a.xyz;
-    if (!xyz || !a.nver || !a.nvkat || !a.edges || !a.bound || kuz < 27 || ns < 8)
+    if (!xyz || !dm.xyz || !dm.nver || !dm.nvkat || !dm.edges || !dm.bnode || kuz < 27 ||
+        a.nver_stride < 8 || dm.nn != kuz)
         return MTGPU_OK;
     int nx = 1;
     while (nx < kuz && xyz[3 * nx + 1] == xyz[1] && xyz[3 * nx + 2] == xyz[2]) nx++;
@@ -2142,24 +2257,19 @@ int matfree_build(Survey &V, const MatFreeMesh &a, int kuz, int kpar, int nsm)
     if (nxy % nx || kuz % nxy) return MTGPU_OK;
     const int ny = nxy / nx, nz = kuz / nxy;
     if (nx < 3 || ny < 3 || nz < 3 || nx > 1024 || ny > 1024 || nz > 1024) return MTGPU_OK;
-    std::vector<double> X(nx), Y(ny), Z(nz);
+    std::vector<double> lines((size_t)nx + ny + nz);
+    double *X = lines.data(), *Y = X + nx, *Z = Y + ny;
     for (int i = 0; i < nx; i++) X[i] = xyz[3 * i];
     for (int j = 0; j < ny; j++) Y[j] = xyz[3 * (j * nx) + 1];
     for (int k = 0; k < nz; k++) Z[k] = xyz[3 * (k * nxy) + 2];
     for (int i = 1; i < nx; i++) if (!(X[i] > X[i - 1])) return MTGPU_OK;
     for (int j = 1; j < ny; j++) if (!(Y[j] > Y[j - 1])) return MTGPU_OK;
     for (int k = 1; k < nz; k++) if (!(Z[k] > Z[k - 1])) return MTGPU_OK;
-    for (int k = 0, n = 0; k < nz; k++)
-        for (int j = 0; j < ny; j++)
-            for (int i = 0; i < nx; i++, n++) {
-                if (xyz[3 * n] != X[i] || xyz[3 * n + 1] != Y[j] || xyz[3 * n + 2] != Z[k])
-                    return MTGPU_OK;
-                const bool surf = i == 0 || j == 0 || k == 0 || i == nx - 1 || j == ny - 1 ||
-                                  k == nz - 1;
-                if (surf && !a.bound[n]) return MTGPU_OK;
-            }
     const long long ncell = (long long)(nx - 1) * (ny - 1) * (nz - 1);
     if (ncell != kpar) return MTGPU_OK;
+    const long long nex = (long long)(nx - 1) * ny * nz, ney = (long long)nx * (ny - 1) * nz,
+                    nez = (long long)nx * ny * (nz - 1);
+    if (nex + ney + nez != P.nb) return MTGPU_OK;
     // 32-bit indexing in the kernels: edges, faces and weights times systems
     const long long nfaces = (long long)nx * (ny - 1) * (nz - 1) +
                              (long long)(nx - 1) * ny * (nz - 1) +
@@ -2167,117 +2277,94 @@ int matfree_build(Survey &V, const MatFreeMesh &a, int kuz, int kpar, int nsm)
     if ((long long)P.nb * V.SP >= (1LL << 31) || 6 * ncell >= (1LL << 31) ||
         nfaces * V.SP >= (1LL << 31))
         return MTGPU_OK;
-    for (int k = 0, c = 0; k < nz - 1; k++)
-        for (int j = 0; j < ny - 1; j++)
-            for (int i = 0; i < nx - 1; i++, c++) {
-                const int n0 = (k * ny + j) * nx + i;
-                const int want[8] = {n0, n0 + 1, n0 + nx, n0 + nx + 1,
-                                     n0 + nxy, n0 + nxy + 1, n0 + nxy + nx, n0 + nxy + nx + 1};
-                for (int t = 0; t < 8; t++)
-                    if (a.nver[(size_t)c * ns + t] != want[t]) return MTGPU_OK;
-            }
-    // edges: node order, +x, +y, +z per node
-    std::vector<int> rb((size_t)ny * nz);
-    // rows direction by direction: x-edges, y-edges, z-edges, each i fastest
-    std::vector<unsigned> pos;
-    pos.reserve(P.nb);
-    for (int d = 0; d < 3; d++)
-        for (int k = 0; k < nz - (d == 2); k++)
-            for (int j = 0; j < ny - (d == 1); j++)
-                for (int i = 0; i < nx - (d == 0); i++)
-                    pos.push_back((unsigned)i | ((unsigned)j << 10) | ((unsigned)k << 20));
-    long long e = 0;
-    for (int k = 0; k < nz; k++)
-        for (int j = 0; j < ny; j++) {
-            rb[(size_t)k * ny + j] = (int)e;
-            for (int i = 0; i < nx; i++) {
-                const int n = (k * ny + j) * nx + i;
-                const int step[3] = {1, nx, nxy};
-                const bool has[3] = {i < nx - 1, j < ny - 1, k < nz - 1};
-                for (int d = 0; d < 3; d++) {
-                    if (!has[d]) continue;
-                    if (e >= P.nb || a.edges[2 * e] != n || a.edges[2 * e + 1] != n + step[d])
-                        return MTGPU_OK;
-                    e++;
-                }
-            }
-        }
-    if (e != P.nb || (long long)pos.size() != P.nb) return MTGPU_OK;
-    // Dirichlet edges: both nodes flagged
-    std::vector<unsigned char> bedge(P.nb);
-    for (long long q = 0; q < P.nb; q++)
-        bedge[q] = a.bound[a.edges[2 * q]] && a.bound[a.edges[2 * q + 1]];
-    // the tiled variant derives the Dirichlet edges from the lattice: an edge
-    // is Dirichlet iff one of its two transverse node lines is on the surface
-    bool lattice = true;
-    for (int k = 0, q = 0; k < nz && lattice; k++)
-        for (int j = 0; j < ny && lattice; j++)
-            for (int i = 0; i < nx; i++) {
-                const bool bi = i == 0 || i == nx - 1, bj = j == 0 || j == ny - 1,
-                           bk = k == 0 || k == nz - 1;
-                const bool want[3] = {bj || bk, bi || bk, bi || bj};
-                const bool has[3] = {i < nx - 1, j < ny - 1, k < nz - 1};
-                for (int d = 0; d < 3; d++)
-                    if (has[d] && (bool)bedge[q++] != want[d]) lattice = false;
-                if (!lattice) break;
-            }
-    // per-cell weights from the materials' mu and sigma
     const int nmat = (int)std::min(a.mu.size(), a.sigma.size());
-    std::vector<double> wf((size_t)3 * ncell), wmv((size_t)3 * ncell);
-    for (int k = 0, c = 0; k < nz - 1; k++)
-        for (int j = 0; j < ny - 1; j++)
-            for (int i = 0; i < nx - 1; i++, c++) {
-                const int mat = a.nvkat[c];
-                if (mat < 0 || mat >= nmat || !(a.mu[mat] > 0.0)) return MTGPU_OK;
-                const double h[3] = {X[i + 1] - X[i], Y[j + 1] - Y[j], Z[k + 1] - Z[k]};
-                for (int d = 0; d < 3; d++) {
-                    const int t1 = (d + 1) % 3, t2 = (d + 2) % 3;
-                    wf[(size_t)d * ncell + c] = 2.0 * h[d] / (h[t1] * h[t2]) / a.mu[mat] / 3.0;
-                    wmv[(size_t)d * ncell + c] = a.sigma[mat] * h[t1] * h[t2] / h[d] / 9.0;
-                }
-            }
+    if (nmat < 1) return MTGPU_OK;
     // a host SLAE's M carries omega_true: the ratio of its diagonal to the
     // mass coefficient of the edge itself (4 times the 4 cells' wM) on an
     // interior x-edge; the set-up check below confirms it on every row
-    if (a.idi && a.di) {
+    double om = 1.0;
+    const int scale = a.idi && a.di;
+    if (scale) {
         const int i = (nx - 1) / 2, j = ny / 2, k = nz / 2;
-        const int e = rb[(size_t)k * ny + j] + i * 3;   // +x edge of an interior node
+        const long long e = (long long)k * ((ny - 1) * (3LL * nx - 1) + (2LL * nx - 1)) +
+                            (long long)j * (3LL * nx - 1) + 3LL * i;   // +x edge of an interior node
         double wsum = 0.0;
         for (int b1 = -1; b1 <= 0; b1++)
             for (int b2 = -1; b2 <= 0; b2++) {
                 const size_t c = ((size_t)(k + b2) * (ny - 1) + (j + b1)) * (nx - 1) + i;
-                wsum += wmv[c];
+                const int mat = a.nvkat[c];
+                if (mat < 0 || mat >= nmat) return MTGPU_OK;
+                const double h[3] = {X[i + 1] - X[i], Y[j + b1 + 1] - Y[j + b1], Z[k + b2 + 1] - Z[k + b2]};
+                wsum += a.sigma[mat] * h[1] * h[2] / h[0] / 9.0;
             }
         if (a.idi[e + 1] - a.idi[e] != 2 || !(wsum > 0.0)) return MTGPU_OK;
-        const double om = a.di[a.idi[e] + 1] / (4.0 * wsum);
+        om = a.di[a.idi[e] + 1] / (4.0 * wsum);
         if (!(om > 0.0)) return MTGPU_OK;
-        for (double &v : wmv) v *= om;
-    }
-    std::vector<float2> w((size_t)6 * ncell);
-    for (size_t t = 0; t < (size_t)3 * ncell; t++) {
-        const dfl::df f = dfl::from_double(wf[t]), m = dfl::from_double(wmv[t]);
-        w[t] = make_float2(f.h, f.l);
-        w[(size_t)3 * ncell + t] = make_float2(m.h, m.l);
     }
     F.nx = nx;
     F.ny = ny;
     F.nz = nz;
-    F.lattice = lattice;
     F.nfx = (long long)nx * (ny - 1) * (nz - 1);
     F.nfy = (long long)(nx - 1) * ny * (nz - 1);
     F.nfz = (long long)(nx - 1) * (ny - 1) * nz;
+    double *d_lines = nullptr;
+    int *d_bad = nullptr;
     int rc;
-    if ((rc = dev_alloc(&F.rb, rb.size())) || (rc = dev_alloc(&F.pos, pos.size())) ||
-        (rc = dev_alloc(&F.bedge, bedge.size())) ||
-        (rc = dev_alloc(&F.w, w.size())) ||
+    if ((rc = dev_alloc(&F.pos, (size_t)P.nb)) || (rc = dev_alloc(&F.bedge, (size_t)P.nb)) ||
+        (rc = dev_alloc(&F.w, (size_t)6 * ncell)) ||
         (rc = dev_alloc(&F.f, (size_t)(F.nfx + F.nfy + F.nfz) * V.SP)) ||
-        (rc = dev_alloc(&F.g, (size_t)(F.nfx + F.nfy + F.nfz) * V.SP)))
+        (rc = dev_alloc(&F.g, (size_t)(F.nfx + F.nfy + F.nfz) * V.SP)) ||
+        (rc = dev_alloc(&d_lines, lines.size() + 2 * (size_t)nmat)) || (rc = dev_alloc(&d_bad, 2))) {
+        dev_free(d_lines);
+        F.release();
         return rc;
-    MTGPU_TRY(cudaMemcpyAsync(F.rb, rb.data(), sizeof(int) * rb.size(), cudaMemcpyHostToDevice, V.st));
-    MTGPU_TRY(cudaMemcpyAsync(F.pos, pos.data(), sizeof(unsigned) * pos.size(),
-                              cudaMemcpyHostToDevice, V.st));
-    MTGPU_TRY(cudaMemcpyAsync(F.w, w.data(), sizeof(float2) * w.size(), cudaMemcpyHostToDevice, V.st));
-    MTGPU_TRY(cudaMemcpyAsync(F.bedge, bedge.data(), bedge.size(), cudaMemcpyHostToDevice, V.st));
+    }
+    cudaError_t err = cudaMemcpyAsync(d_lines, lines.data(), sizeof(double) * lines.size(),
+                                      cudaMemcpyHostToDevice, V.st);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(d_lines + lines.size(), a.mu.data(), sizeof(double) * nmat,
+                              cudaMemcpyHostToDevice, V.st);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(d_lines + lines.size() + nmat, a.sigma.data(), sizeof(double) * nmat,
+                              cudaMemcpyHostToDevice, V.st);
+    if (err == cudaSuccess) err = cudaMemsetAsync(d_bad, 0, sizeof(int) * 2, V.st);
+    int bad[2] = {0, 0};
+    if (err == cudaSuccess) {
+        MF M{};
+        M.nx = nx;
+        M.ny = ny;
+        M.nz = nz;
+        M.ncell = ncell;
+        M.nex = (int)nex;
+        M.ney = (int)ney;
+        M.plane = (ny - 1) * (3 * nx - 1) + (2 * nx - 1);
+        M.l3 = 3 * nx - 1;
+        M.l2 = 2 * nx - 1;
+        const MfbLines L{d_lines, d_lines + nx, d_lines + nx + ny, d_lines + lines.size(),
+                         d_lines + lines.size() + nmat, nmat};
+        k_mfb_nodes<<<ceil_div(kuz, kB), kB, 0, V.st>>>(M, L, P.nb, dm.xyz, dm.bnode, dm.edges,
+                                                       F.bedge, F.pos, d_bad);
+        k_mfb_cells<<<ceil_div(ncell, kB), kB, 0, V.st>>>(M, L, dm.nver, dm.nver_stride, dm.nvkat, om,
+                                                         scale, F.w, d_bad);
+        note_launches(2);
+        err = cudaGetLastError();
+    }
+    if (err == cudaSuccess) err = cudaMemcpyAsync(bad, d_bad, sizeof(bad), cudaMemcpyDeviceToHost, V.st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(V.st);
+    dev_free(d_lines);
+    dev_free(d_bad);
+    if (err != cudaSuccess) {
+        F.release();
+        set_last_error(err, "matrix-free tables", __FILE__, __LINE__);
+        return MTGPU_ERR_CUDA;
+    }
+    if (bad[0] != 0) {
+        F.release();   // not a tensor mesh in the builder's numbering: variant off
+        return MTGPU_OK;
+    }
+    // the tiled variant derives the Dirichlet edges from the lattice: an edge
+    // is Dirichlet iff one of its two transverse node lines is on the surface
+    F.lattice = bad[1] == 0;
     F.on = true;
     // set-up check against the stored-matrix SpMV on a test vector
     const int ch = V.ch;
@@ -2305,7 +2392,7 @@ int matfree_build(Survey &V, const MatFreeMesh &a, int kuz, int kpar, int nsm)
     k_maxdiff<<<4 * nsm, kB, 0, V.st>>>(n, V.z, V.w, d_mx);
     note_launches(5);
     unsigned long long mx[2] = {0, 0};
-    cudaError_t err = cudaGetLastError();
+    err = cudaGetLastError();
     if (err == cudaSuccess)
         err = cudaMemcpyAsync(mx, d_mx, sizeof(mx), cudaMemcpyDeviceToHost, V.st);
     if (err == cudaSuccess) err = cudaStreamSynchronize(V.st);
@@ -2316,10 +2403,10 @@ int matfree_build(Survey &V, const MatFreeMesh &a, int kuz, int kpar, int nsm)
         set_last_error(err, "matrix-free SpMV set-up check", __FILE__, __LINE__);
         return MTGPU_ERR_CUDA;
     }
-    double dm, bm;
-    memcpy(&dm, &mx[0], sizeof(double));
-    memcpy(&bm, &mx[1], sizeof(double));
-    const double check = bm > 0.0 ? dm / bm : 1.0;
+    double dmax, bmax;
+    memcpy(&dmax, &mx[0], sizeof(double));
+    memcpy(&bmax, &mx[1], sizeof(double));
+    const double check = bmax > 0.0 ? dmax / bmax : 1.0;
     if (!(check < 1e-9)) {
         F.release();   // not this matrix's operator: variant off, memory back
         F.check = check;
@@ -2327,33 +2414,6 @@ int matfree_build(Survey &V, const MatFreeMesh &a, int kuz, int kpar, int nsm)
     }
     F.check = check;
     MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
-    if (F.lattice && !spmv_variant_available(V, kMatFree + 2)) F.lattice = false;
-    if (F.lattice) {
-        // the tiled variant sums in the same order: its product must equal
-        // the two-kernel one to the last bit
-        MTGPU_TRY(cudaMemcpyAsync(V.w, V.z, sizeof(float4) * n, cudaMemcpyDeviceToDevice, V.st));
-        MTGPU_TRY(cudaMemcpyAsync(V.sys, init.data(), sizeof(SysState) * 32, cudaMemcpyHostToDevice, V.st));
-        V.ch = kMatFree + 2;
-        MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
-        MTGPU_SP_DISPATCH(V.SP, spmv_only(V));
-        V.ch = ch;
-        MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
-        if ((rc = dev_alloc(&d_mx, 2))) return rc;
-        MTGPU_TRY(cudaMemsetAsync(d_mx, 0, sizeof(unsigned long long) * 2, V.st));
-        k_maxdiff<<<4 * nsm, kB, 0, V.st>>>(n, V.z, V.w, d_mx);
-        note_launches(2);
-        err = cudaGetLastError();
-        if (err == cudaSuccess)
-            err = cudaMemcpyAsync(mx, d_mx, sizeof(mx), cudaMemcpyDeviceToHost, V.st);
-        if (err == cudaSuccess) err = cudaStreamSynchronize(V.st);
-        dev_free(d_mx);
-        if (err != cudaSuccess) {
-            set_last_error(err, "tiled matrix-free SpMV set-up check", __FILE__, __LINE__);
-            return MTGPU_ERR_CUDA;
-        }
-        memcpy(&dm, &mx[0], sizeof(double));
-        F.lattice = dm == 0.0;
-    }
     {
         // the D^T (F f) form rounds differently from variant 32 (products of
         // the face values summed per face first): it must agree to 1e-12
@@ -2383,14 +2443,83 @@ int matfree_build(Survey &V, const MatFreeMesh &a, int kuz, int kpar, int nsm)
             set_last_error(err, "face-mass matrix-free SpMV set-up check", __FILE__, __LINE__);
             return MTGPU_ERR_CUDA;
         }
-        memcpy(&dm, &mx[0], sizeof(double));
-        memcpy(&bm, &mx[1], sizeof(double));
-        F.gface = bm > 0.0 && dm / bm < 1e-12;
+        memcpy(&dmax, &mx[0], sizeof(double));
+        memcpy(&bmax, &mx[1], sizeof(double));
+        F.gface = bmax > 0.0 && dmax / bmax < 1e-12;
     }
     return MTGPU_OK;
 }
 
+// Variant 34 sums in the same order as variant 32: it is enabled only if
+// its product on a pseudo-random vector equals variant 32's bit for bit.
+// Run on the first request of the variant.
+int matfree_tile_check(Survey &V, int nsm)
+{
+    MatFree &F = V.mf;
+    F.tile_checked = true;
+    F.tiled = F.on && F.lattice && V.g_mft > 0 && V.g_mft <= V.pblocks;
+    if (!F.tiled) return MTGPU_OK;
+    std::vector<SysState> init(32);
+    for (int k = 0; k < 32; k++) {
+        SysState q{};
+        q.status = k < V.S ? kRun : MTGPU_OK;
+        q.maxiter = 1;
+        init[k] = q;
+    }
+    const int ch = V.ch;
+    const long long n = (long long)V.nb * V.SP;
+    k_pattern<<<4 * nsm, kB, 0, V.st>>>(n, V.s);
+    MTGPU_TRY(cudaMemcpyAsync(V.sys, init.data(), sizeof(SysState) * 32, cudaMemcpyHostToDevice, V.st));
+    V.ch = kMatFree;
+    MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+    MTGPU_SP_DISPATCH(V.SP, spmv_only(V));
+    MTGPU_TRY(cudaMemcpyAsync(V.w, V.z, sizeof(float4) * n, cudaMemcpyDeviceToDevice, V.st));
+    MTGPU_TRY(cudaMemcpyAsync(V.sys, init.data(), sizeof(SysState) * 32, cudaMemcpyHostToDevice, V.st));
+    V.ch = kMatFree + 2;
+    MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+    MTGPU_SP_DISPATCH(V.SP, spmv_only(V));
+    V.ch = ch;
+    MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+    unsigned long long *d_mx = nullptr;
+    int rc = dev_alloc(&d_mx, 2);
+    if (rc) return rc;
+    MTGPU_TRY(cudaMemsetAsync(d_mx, 0, sizeof(unsigned long long) * 2, V.st));
+    k_maxdiff<<<4 * nsm, kB, 0, V.st>>>(n, V.z, V.w, d_mx);
+    note_launches(4 + spmv_extra_launches(kMatFree));
+    unsigned long long mx[2] = {0, 0};
+    cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess) err = cudaMemcpyAsync(mx, d_mx, sizeof(mx), cudaMemcpyDeviceToHost, V.st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(V.st);
+    dev_free(d_mx);
+    if (err != cudaSuccess) {
+        F.tiled = false;
+        set_last_error(err, "tiled matrix-free SpMV set-up check", __FILE__, __LINE__);
+        return MTGPU_ERR_CUDA;
+    }
+    double dm;
+    memcpy(&dm, &mx[0], sizeof(double));
+    F.tiled = dm == 0.0;
+    return MTGPU_OK;
+}
+
 }  // namespace
+
+// What variant v needs beyond the set-up, built on its first request: the
+// stored matrix's tiles (variants 0, 1), the tiled variant's check (34)
+int survey_prepare_variant(Survey &V, int v)
+{
+    int dev = 0, nsm = 0;
+    MTGPU_TRY(cudaGetDevice(&dev));
+    MTGPU_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    int rc;
+    if ((v == 0 || v == 1) && !V.tiles_built) {
+        V.tiles_built = true;
+        if ((rc = build_tiles(V, nsm))) return rc;
+        MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
+    }
+    if (v == kMatFree + 2 && !V.mf.tile_checked && (rc = matfree_tile_check(V, nsm))) return rc;
+    return MTGPU_OK;
+}
 
 namespace {
 
@@ -2481,10 +2610,37 @@ int prec_tile_setup(Survey &V, int nsm)
 
 }  // namespace
 
+namespace {
+// MTGPU_TRACE=1 (environment): the set-up's phases on stderr, each after a
+// synchronisation of the stream so that device work is charged to its phase
+struct PhaseTrace {
+    bool on;
+    cudaStream_t st;
+    std::chrono::steady_clock::time_point t0, last;
+    explicit PhaseTrace(cudaStream_t s) : st(s)
+    {
+        const char *e = getenv("MTGPU_TRACE");
+        on = e && *e == '1';
+        t0 = last = std::chrono::steady_clock::now();
+    }
+    void mark(const char *what)
+    {
+        if (!on) return;
+        cudaStreamSynchronize(st);
+        const auto now = std::chrono::steady_clock::now();
+        fprintf(stderr, "[mtgpu] survey set-up %-22s %8.2f ms (total %8.2f)\n", what,
+                std::chrono::duration<double, std::milli>(now - last).count(),
+                std::chrono::duration<double, std::milli>(now - t0).count());
+        last = now;
+    }
+};
+}  // namespace
+
 int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const double *omega,
                  Survey &V, cudaStream_t st, const mtgpu_assembly_s *a, const MatFreeMesh *mfm,
                  int pin_variant)
 {
+    PhaseTrace trace(st);
     V.release();
     MTGPU_CHECK_ARG(S >= 1 && S <= 32, "a survey batch holds 1 to 32 systems");
     V.P = &P;
@@ -2499,7 +2655,20 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
     const int rpb = kB / V.SP;
     V.grid_rows = std::max(1, ceil_div(V.nb, rpb));
     int rc;
-    if ((rc = folded_build_g(mesh, V.G, st))) return rc;
+    // the mesh tables on the device: the assembly's own, or uploads of a
+    // host SLAE's mesh
+    DevMeshUpload dmu;
+    if (a && P.d_nver && P.d_nvkat && P.d_edges && P.d_bnode && P.d_xyz)
+        rc = dmu.over_device(P.kpar, P.nb, P.kuzlov, P.nver_stride, P.d_xyz, P.d_nver, P.d_nvkat,
+                             P.d_edges, P.d_bnode, a->sigflag.data(), (int)a->sigflag.size(), st);
+    else
+        rc = dmu.upload(mesh, mfm ? mfm->xyz : nullptr, st);
+    if (rc) return rc;
+    trace.mark("mesh tables");
+    bool conforming = false;
+    if ((rc = folded_build_g_device(dmu.view, V.G, st, &conforming))) return rc;
+    if (!conforming && (rc = folded_build_g(mesh, V.G, st))) return rc;
+    trace.mark("preconditioner G");
     const int m = V.G.m, mm = std::max(m, 1);
     V.grid_nodes = std::max(1, ceil_div(mm, rpb));
     MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
@@ -2538,10 +2707,9 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
     k_diag_a<<<(unsigned)((nv + kB - 1) / kB), kB, 0, st>>>(V.nb, V.SP, P.d_nc, P.d_pc, P.d_col_c,
                                                           P.d_kc, P.d_mc, V.omega64, V.da);
     {
-        std::vector<int> gp(m + 1);
-        MTGPU_TRY(cudaMemcpyAsync(gp.data(), V.G.d_gp, sizeof(int) * (m + 1), cudaMemcpyDeviceToHost, st));
+        int nnz = 0;
+        MTGPU_TRY(cudaMemcpyAsync(&nnz, V.G.d_gp + m, sizeof(int), cudaMemcpyDeviceToHost, st));
         MTGPU_TRY(cudaStreamSynchronize(st));
-        const int nnz = gp[m];
         if ((rc = dev_alloc(&V.gv32, std::max(nnz, 1))) || (rc = dev_alloc(&V.tv32, std::max(nnz, 1))))
             return rc;
         if (nnz > 0) {
@@ -2559,15 +2727,12 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
     MTGPU_TRY(cudaGetLastError());
     MTGPU_TRY(cudaStreamSynchronize(st));
     note_launches(8);
-    if ((rc = build_tiles(V, nsm))) return rc;
+    trace.mark("vectors, diagonals");
     if (a) {
         MatFreeMesh mm;
         mm.xyz = a->xyz.data();
-        mm.nver = a->nver.data();
         mm.nver_stride = a->nver_stride;
         mm.nvkat = a->nvkat.data();
-        mm.edges = a->edges.data();
-        mm.bound = a->bound.data();
         mm.mu.resize(P.n_materials);
         mm.sigma.resize(P.n_materials);
         MTGPU_TRY(cudaMemcpyAsync(mm.mu.data(), P.d_mu, sizeof(double) * P.n_materials,
@@ -2576,29 +2741,45 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
                                   cudaMemcpyDeviceToHost, st));
         MTGPU_TRY(cudaStreamSynchronize(st));
         if ((long long)a->xyz.size() == 3LL * P.kuzlov &&
-            (rc = matfree_build(V, mm, P.kuzlov, P.kpar, nsm)))
+            (rc = matfree_build(V, mm, dmu.view, P.kuzlov, P.kpar, nsm)))
             return rc;
-    } else if (mfm && (rc = matfree_build(V, *mfm, mesh.n_nodes_c, mesh.kpar, nsm))) {
+    } else if (mfm && (rc = matfree_build(V, *mfm, dmu.view, mesh.n_nodes_c, mesh.kpar, nsm))) {
         return rc;
     }
+    trace.mark("matrix-free tables");
+    // the stored matrix's tiles (variants 0, 1) where there is no
+    // matrix-free operator; with one they are built only on request
+    if (!V.mf.on && (rc = survey_prepare_variant(V, 0))) return rc;
+    trace.mark("SpMV tiles");
     // autotune the SpMV variant: time each candidate, keep the fastest.
     // MTGPU_SPMV_VARIANT (environment) pins an available variant instead:
     // runs under a profiler, which serialises and cold-starts every launch,
     // would otherwise tune to other variants than plain runs do
     const char *pin = getenv("MTGPU_SPMV_VARIANT");
-    if (pin && *pin && spmv_variant_available(V, atoi(pin))) {
-        V.ch = atoi(pin);
+    const int pin_env = pin && *pin ? atoi(pin) : -1;
+    if (pin_env >= 0 && (rc = survey_prepare_variant(V, pin_env))) return rc;
+    if (pin_variant >= 0 && (rc = survey_prepare_variant(V, pin_variant))) return rc;
+    if (pin_env >= 0 && spmv_variant_available(V, pin_env)) {
+        V.ch = pin_env;
         MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
     } else if (pin_variant >= 0 && spmv_variant_available(V, pin_variant)) {
         V.ch = pin_variant;
         MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
     } else {
+        // with the matrix-free operator the stored-matrix variants (staged
+        // tiles, 2 or 8 slots in flight, a row per thread) and the tiled
+        // matrix-free one measured slower on every tensor mesh, so only the
+        // 4-slot stored variant stays as a fallback candidate
         const int cand[kSpmvVariants] = {0, 1, 2, 4, 8, kRowVariant + 2, kRowVariant + 4, kMatFree,
                                          kMatFree + 1, kMatFree + 2, kMatFree + 3};
+        auto tried = [&](int v) {
+            if (!V.mf.on) return true;
+            return v == 4 || v == kMatFree || v == kMatFree + 1 || v == kMatFree + 3;
+        };
         float best = 1e30f;
         int best_ch = 4;
         for (int c = 0; c < kSpmvVariants; c++) {
-            if (!spmv_variant_available(V, cand[c])) continue;
+            if (!tried(cand[c]) || !spmv_variant_available(V, cand[c])) continue;
             V.ch = cand[c];
             MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
             float ms = 0.f;
@@ -2613,7 +2794,10 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
         V.ch = best_ch;
         MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
     }
-    return prec_tile_setup(V, nsm);
+    trace.mark("SpMV autotuning");
+    rc = prec_tile_setup(V, nsm);
+    trace.mark("fused preconditioner");
+    return rc;
 }
 
 int survey_set_variant(Survey &V, int variant)

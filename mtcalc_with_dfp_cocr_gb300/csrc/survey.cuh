@@ -34,14 +34,15 @@ struct MatFree {
     bool on = false;
     int nx = 0, ny = 0, nz = 0;      // lines per axis
     long long nfx = 0, nfy = 0, nfz = 0;
-    int *rb = nullptr;               // [nz][ny] number of the first edge of node (0, j, k)
     unsigned *pos = nullptr;         // [nb] rows x-, y-, z-edges: i | j << 10 | k << 20
     float2 *w = nullptr;             // [6][cells] double-float wF/3 (x, y, z), wM/9 (x, y, z)
     unsigned char *bedge = nullptr;  // [nb] Dirichlet edges
     float4 *f = nullptr;             // face circulations [faces][SP]
     float4 *g = nullptr;             // face mass applied to them, F f [faces][SP] (variant 35)
     double check = -1.0;             // set-up check: max |A_mf s - A s| / max |A s|
-    bool lattice = false;            // Dirichlet edges follow the lattice rule (variant 34)
+    bool lattice = false;            // Dirichlet edges follow the lattice rule
+    bool tiled = false;              // variant 34 equals variant 32 bit for bit
+    bool tile_checked = false;       // ... and that was checked (on first request)
     bool gface = false;              // the D^T (F f) form agrees with variant 32 (variant 35)
     void release();
 };
@@ -58,6 +59,7 @@ struct Survey {
     int ch = 4;
     // SpMV tiles: T consecutive SELL slices, their distinct columns, per-slot local indices
     int tile_T = 1, ntiles = 0, tile_smem = 0, tile_smem_x = 0, g_spmv_t = 0, g_spmv_tx = 0;
+    bool tiles_built = false;        // the stored matrix's tiles (variants 0, 1) were built
     int *uoff = nullptr, *ucol = nullptr;
     unsigned short *lc = nullptr, *lr = nullptr;
     float tune_ms[kSpmvVariants] = {};   // SpMV times of the variants 0, 1, 2, 4, 8, 18, 20, 32, 33, 34, 35
@@ -103,7 +105,7 @@ inline bool spmv_variant_available(const Survey &V, int v)
     if (v == kRowVariant + 2 || v == kRowVariant + 4) return V.SP == 2;
     if (v == kMatFree) return V.mf.on;
     if (v == kMatFree + 1) return V.mf.on && V.SP >= 2;
-    if (v == kMatFree + 2) return V.mf.on && V.mf.lattice && V.g_mft > 0 && V.g_mft <= V.pblocks;
+    if (v == kMatFree + 2) return V.mf.on && V.mf.tiled && V.g_mft > 0 && V.g_mft <= V.pblocks;
     if (v == kMatFree + 3) return V.mf.on && V.mf.gface;
     return false;
 }
@@ -115,14 +117,12 @@ inline int spmv_extra_launches(int v)
     return v == kMatFree || v == kMatFree + 1 ? 1 : (v == kMatFree + 3 ? 2 : 0);
 }
 
-// Host mesh description for the matrix-free SpMV (all arrays host, 0-based)
+// The host side of the matrix-free set-up (the tables themselves are
+// checked and built from the device copies of the mesh)
 struct MatFreeMesh {
-    const double *xyz = nullptr;       // [kuzlov][3]
-    const int *nver = nullptr;         // [kpar][nver_stride]
+    const double *xyz = nullptr;       // [kuzlov][3]: the node lines
     int nver_stride = 14;
     const int *nvkat = nullptr;        // [kpar]
-    const int *edges = nullptr;        // [nb][2]
-    const int *bound = nullptr;        // [kuzlov] Dirichlet node flags
     std::vector<double> mu, sigma;     // per material: mu3d * MU_0, sigma3d
     // the survey's M holds omega_true sigma C (a host SLAE at one frequency,
     // solved with omega = 1): omega_true is read from the SLAE's diagonal
@@ -172,5 +172,8 @@ inline int iteration_launches(const Survey &V)
     return (V.prec_tile ? 3 : (V.G.m > 0 ? 4 : 3)) + spmv_extra_launches(V.ch);
 }
 int survey_set_variant(Survey &V, int variant);
+// builds what `variant` needs beyond the set-up (on its first request);
+// spmv_variant_available tells afterwards whether it can run
+int survey_prepare_variant(Survey &V, int variant);
 
 }  // namespace mtgpu

@@ -94,3 +94,17 @@ def test_device_mesh_tables_equal_host_tables(gpu, name):
     assert torch.equal(bd, bh)
     Ad.close()
     Ah.close()
+
+
+@pytest.mark.parametrize("name,tables", [("tiny", "host"), ("small", "device"), ("c1", "device"),
+                                         ("c1", "host")])
+def test_device_preconditioner_g_equals_host(gpu, name, tables):
+    """The folded preconditioner's G (rows of the interior nodes of
+    conductive cells, -1/2 and +1/2 per edge, FoldedPreconditioner.cpp:68-259)
+    and G^T, built on the device by every solver set-up, equal the host
+    construction entry for entry, including the order of every row (the
+    D_S sums and the node gathers run in that order)."""
+    w = workloads.make(name)
+    A = assembly.Assembly(w.mesh, tables=tables)
+    assert A.check_preconditioner()
+    A.close()
