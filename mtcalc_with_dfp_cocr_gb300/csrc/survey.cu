@@ -64,7 +64,6 @@ void Survey::release()
 void MatFree::release()
 {
     dev_free(pos);
-    dev_free(bedge);
     dev_free(w);
     dev_free(f);
     dev_free(g);
@@ -727,13 +726,38 @@ struct MF {
     long long nfx, nfy, nfz, ncell;
     int nex, ney;              // x- and y-edges: the first two segments of the row order
     int plane, l3, l2;         // edges per node plane below the top one; per node line below / in it
-    int lat;                   // Dirichlet edges are the lattice's (every surface node Dirichlet)
+    // strides of the index grids along x, y, z: faces of normal n (fs[n]),
+    // cells (cs), and the edges of one direction away from the surface
+    // (es = 3, l3, plane: every node before them has its +x, +y, +z edge)
+    int fs[3][3], cs[3], es[3];
+    int fb[3];                 // first face of each normal
     const unsigned *pos;       // row (direction-major order) -> i | j << 10 | k << 20
     const float2 *w;
-    const unsigned char *bedge;
     float4 *f;
     float4 *g;                 // F f (variant 35)
 };
+
+// the edge counts and index strides of M from its node lines nx, ny, nz
+inline void mf_strides(MF &M)
+{
+    const int nx = M.nx, ny = M.ny;
+    M.plane = (ny - 1) * (3 * nx - 1) + (2 * nx - 1);
+    M.l3 = 3 * nx - 1;
+    M.l2 = 2 * nx - 1;
+    const int fsv[3][3] = {{1, nx, nx * (ny - 1)}, {1, nx - 1, (nx - 1) * ny},
+                           {1, nx - 1, (nx - 1) * (ny - 1)}};
+    for (int n = 0; n < 3; n++)
+        for (int a = 0; a < 3; a++) M.fs[n][a] = fsv[n][a];
+    M.cs[0] = 1;
+    M.cs[1] = nx - 1;
+    M.cs[2] = (nx - 1) * (ny - 1);
+    M.es[0] = 3;
+    M.es[1] = M.l3;
+    M.es[2] = M.plane;
+    M.fb[0] = 0;
+    M.fb[1] = (int)M.nfx;
+    M.fb[2] = (int)(M.nfx + M.nfy);
+}
 
 // first edge of node line (j, k): the node planes below, then the lines
 // before it in its plane (edges are numbered node by node, each node's +x,
@@ -755,25 +779,21 @@ __device__ __forceinline__ int mf_edge(const MF &M, int d, int i, int j, int k)
     return e;
 }
 
-// whether the +d edge e of node (i, j, k) is Dirichlet: on lattice meshes
-// iff one of its two transverse node lines lies on the surface, else the
-// per-edge flag (both nodes flagged)
-__device__ __forceinline__ bool mf_dirichlet(const MF &M, int d, int i, int j, int k, int e)
+// The matrix-free operator runs on lattice meshes only: every node of the
+// outer surface, and no other, is a Dirichlet node, so the +d edge of node
+// (i, j, k) is Dirichlet iff one of its two transverse node lines lies on
+// the surface.  Every other edge has its two transverse coordinates inside,
+// so its node and all nodes before it on its line have three edges: its
+// number is k plane + j l3 + 3 i + d, and moving it by one node along an
+// axis adds es[axis].
+__device__ __forceinline__ bool mf_dirichlet(const MF &M, int d, int i, int j, int k)
 {
-    if (M.lat) {
-        const bool bi = i == 0 || i == M.nx - 1, bj = j == 0 || j == M.ny - 1,
-                   bk = k == 0 || k == M.nz - 1;
-        return d == 0 ? (bj || bk) : (d == 1 ? (bi || bk) : (bi || bj));
-    }
-    return __ldg(M.bedge + e) != 0;
+    const bool bi = i == 0 || i == M.nx - 1, bj = j == 0 || j == M.ny - 1, bk = k == 0 || k == M.nz - 1;
+    return d == 0 ? (bj || bk) : (d == 1 ? (bi || bk) : (bi || bj));
 }
-
-// face of normal n at (i, j, k): line index along n, cell indices across
-__device__ __forceinline__ int mf_face(const MF &M, int n, int i, int j, int k)
+__device__ __forceinline__ int mf_edge_in(const MF &M, int d, int i, int j, int k)
 {
-    if (n == 0) return (k * (M.ny - 1) + j) * M.nx + i;
-    if (n == 1) return (int)M.nfx + (k * M.ny + j) * (M.nx - 1) + i;
-    return (int)(M.nfx + M.nfy) + (k * (M.ny - 1) + j) * (M.nx - 1) + i;
+    return k * M.plane + j * M.l3 + 3 * i + d;
 }
 
 // x of the +d edge of node (i, j, kk) for system k, 0 on Dirichlet edges
@@ -781,9 +801,8 @@ template <int SP>
 __device__ __forceinline__ dfc mf_x(const MF &M, const float4 *__restrict__ x, int d, int i, int j,
                                     int kk, int k)
 {
-    const int e = mf_edge(M, d, i, j, kk);
-    if (mf_dirichlet(M, d, i, j, kk, e)) return dfc{df{0.f, 0.f}, df{0.f, 0.f}};
-    return from4(__ldg(x + e * SP + k));
+    if (mf_dirichlet(M, d, i, j, kk)) return dfc{df{0.f, 0.f}, df{0.f, 0.f}};
+    return from4(__ldg(x + mf_edge_in(M, d, i, j, kk) * SP + k));
 }
 
 // f = D s: x(e0) + x(e1) - x(e2) - x(e3) around every face (counterclockwise
@@ -846,39 +865,72 @@ k_mf_faces(MF M, const float4 *__restrict__ x, const SysState *sys)
 
 __device__ __forceinline__ df scale(df a, float s) { return df{a.h * s, a.l * s}; }   // s = +-1, 2, 4
 
-// one non-Dirichlet edge of direction D at lattice position p (p[D] the
-// cell index along D, the others line indices): (K + i omega M) s.  D, and
-// with it the two transverse axes T1 = D+1, T2 = D+2 (mod 3), are compile-
-// time constants: the rows run direction by direction, so warps are uniform.
+// lattice position of an edge: along its direction the cell index, across
+// it node indices
 struct Pos {
     int x, y, z;
 };
+// Index context of a non-Dirichlet edge of direction D at lattice position
+// p (p along D a cell index, along T1 = D+1 and T2 = D+2 (mod 3) node
+// indices): the cell, T1-normal face and T2-normal face at p, the edge, and
+// whether the node lines one below / above along T1 (T2) lie on the
+// surface.  Every neighbour the row reads is one of these plus strides.
+template <int D>
+struct MfRow {
+    static constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
+    int cell, f1, f2, e;
+    bool lo1, hi1, lo2, hi2;
+};
 template <int A>
-__device__ __forceinline__ Pos mv(Pos p, int o)
+__device__ __forceinline__ int coord(Pos p) { return A == 0 ? p.x : (A == 1 ? p.y : p.z); }
+template <int A>
+__device__ __forceinline__ int extent(const MF &M) { return A == 0 ? M.nx : (A == 1 ? M.ny : M.nz); }
+template <int D>
+__device__ __forceinline__ MfRow<D> mf_rowctx(const MF &M, Pos p)
 {
-    return Pos{p.x + (A == 0 ? o : 0), p.y + (A == 1 ? o : 0), p.z + (A == 2 ? o : 0)};
+    constexpr int T1 = MfRow<D>::T1, T2 = MfRow<D>::T2;
+    MfRow<D> r;
+    r.cell = p.x * M.cs[0] + p.y * M.cs[1] + p.z * M.cs[2];
+    r.f1 = M.fb[T1] + p.x * M.fs[T1][0] + p.y * M.fs[T1][1] + p.z * M.fs[T1][2];
+    r.f2 = M.fb[T2] + p.x * M.fs[T2][0] + p.y * M.fs[T2][1] + p.z * M.fs[T2][2];
+    r.e = mf_edge_in(M, D, p.x, p.y, p.z);
+    const int t1 = coord<T1>(p), t2 = coord<T2>(p);
+    r.lo1 = t1 == 1;
+    r.hi1 = t1 == extent<T1>(M) - 2;
+    r.lo2 = t2 == 1;
+    r.hi2 = t2 == extent<T2>(M) - 2;
+    return r;
 }
-template <int N>
-__device__ __forceinline__ int mf_face_n(const MF &M, Pos q)
+// the 3 x 3 parallel edges around the row (grid position (a, b) along
+// (T1, T2), the row at (1, 1)): Dirichlet, and the edge number otherwise
+template <int D>
+__device__ __forceinline__ bool mf_mass_dir(const MfRow<D> &r, int a, int b)
 {
-    if (N == 0) return (q.z * (M.ny - 1) + q.y) * M.nx + q.x;
-    if (N == 1) return (int)M.nfx + (q.z * M.ny + q.y) * (M.nx - 1) + q.x;
-    return (int)(M.nfx + M.nfy) + (q.z * (M.ny - 1) + q.y) * (M.nx - 1) + q.x;
+    return (a == 0 && r.lo1) || (a == 2 && r.hi1) || (b == 0 && r.lo2) || (b == 2 && r.hi2);
+}
+template <int D>
+__device__ __forceinline__ int mf_mass_edge(const MF &M, const MfRow<D> &r, int a, int b)
+{
+    return r.e + (a - 1) * M.es[MfRow<D>::T1] + (b - 1) * M.es[MfRow<D>::T2];
 }
 
+// one non-Dirichlet edge of direction D at lattice position p:
+// (K + i omega M) s.  D, and with it the two transverse axes T1 = D+1,
+// T2 = D+2 (mod 3), are compile-time constants: the rows run direction by
+// direction, so warps are uniform.
 template <int SP, int D>
 __device__ __forceinline__ dfc mf_row(const MF &M, Pos p, int k, df om, const float4 *__restrict__ x)
 {
     constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
     const int nc = (int)M.ncell;
-    auto cell = [&](Pos q) { return (q.z * (M.ny - 1) + q.y) * (M.nx - 1) + q.x; };
+    const MfRow<D> r = mf_rowctx<D>(M, p);
     // weights of the 4 cells around the edge, offsets (a - 1, b - 1) along (T1, T2)
     df w1[2][2], w2[2][2], wm[2][2];
 #pragma unroll
     for (int a = 0; a < 2; a++)
 #pragma unroll
         for (int b = 0; b < 2; b++) {
-            const int cc = cell(mv<T2>(mv<T1>(p, a - 1), b - 1));
+            const int cc = r.cell + (a - 1) * M.cs[T1] + (b - 1) * M.cs[T2];
             w1[a][b] = d2f(__ldg(M.w + T1 * nc + cc));
             w2[a][b] = d2f(__ldg(M.w + T2 * nc + cc));
             wm[a][b] = d2f(__ldg(M.w + (3 + D) * nc + cc));
@@ -890,24 +942,24 @@ __device__ __forceinline__ dfc mf_row(const MF &M, Pos p, int k, df om, const fl
     // after it along the normal
 #pragma unroll
     for (int b = 0; b < 2; b++) {
-        const Pos q = mv<T2>(p, b - 1);
+        const int q = r.f1 + (b - 1) * M.fs[T1][T2];
         const float sg = b == 0 ? 1.f : -1.f;
         const df wa = w1[0][b], wb = w1[1][b];
-        const dfc fm = from4(__ldg(M.f + mf_face_n<T1>(M, mv<T1>(q, -1)) * SP + k));
-        const dfc f0 = from4(__ldg(M.f + mf_face_n<T1>(M, q) * SP + k));
-        const dfc fp = from4(__ldg(M.f + mf_face_n<T1>(M, mv<T1>(q, 1)) * SP + k));
+        const dfc fm = from4(__ldg(M.f + (q - M.fs[T1][T1]) * SP + k));
+        const dfc f0 = from4(__ldg(M.f + q * SP + k));
+        const dfc fp = from4(__ldg(M.f + (q + M.fs[T1][T1]) * SP + k));
         const df ca = scale(wa, sg), cb = scale(wb, sg), c0 = scale(add(wa, wb), 2.f * sg);
         kr.mac(ca, fm.re); kr.mac(c0, f0.re); kr.mac(cb, fp.re);
         ki.mac(ca, fm.im); ki.mac(c0, f0.im); ki.mac(cb, fp.im);
     }
 #pragma unroll
     for (int a = 0; a < 2; a++) {
-        const Pos q = mv<T1>(p, a - 1);
+        const int q = r.f2 + (a - 1) * M.fs[T2][T1];
         const float sg = a == 0 ? -1.f : 1.f;
         const df wa = w2[a][0], wb = w2[a][1];
-        const dfc fm = from4(__ldg(M.f + mf_face_n<T2>(M, mv<T2>(q, -1)) * SP + k));
-        const dfc f0 = from4(__ldg(M.f + mf_face_n<T2>(M, q) * SP + k));
-        const dfc fp = from4(__ldg(M.f + mf_face_n<T2>(M, mv<T2>(q, 1)) * SP + k));
+        const dfc fm = from4(__ldg(M.f + (q - M.fs[T2][T2]) * SP + k));
+        const dfc f0 = from4(__ldg(M.f + q * SP + k));
+        const dfc fp = from4(__ldg(M.f + (q + M.fs[T2][T2]) * SP + k));
         const df ca = scale(wa, sg), cb = scale(wb, sg), c0 = scale(add(wa, wb), 2.f * sg);
         kr.mac(ca, fm.re); kr.mac(c0, f0.re); kr.mac(cb, fp.re);
         ki.mac(ca, fm.im); ki.mac(c0, f0.im); ki.mac(cb, fp.im);
@@ -926,8 +978,8 @@ __device__ __forceinline__ dfc mf_row(const MF &M, Pos p, int k, df om, const fl
     for (int a = 0; a < 3; a++)
 #pragma unroll
         for (int b = 0; b < 3; b++) {
-            const Pos q = mv<T2>(mv<T1>(p, a - 1), b - 1);
-            const dfc xe = mf_x<SP>(M, x, D, q.x, q.y, q.z, k);
+            dfc xe{df{0.f, 0.f}, df{0.f, 0.f}};
+            if (!mf_mass_dir(r, a, b)) xe = from4(__ldg(x + mf_mass_edge(M, r, a, b) * SP + k));
             mr.mac(cm[a][b], xe.re);
             mi.mac(cm[a][b], xe.im);
         }
@@ -946,13 +998,13 @@ __device__ __forceinline__ void mf_row2(const MF &M, Pos p, int k0, const df (&o
 {
     constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
     const int nc = (int)M.ncell;
-    auto cell = [&](Pos q) { return (q.z * (M.ny - 1) + q.y) * (M.nx - 1) + q.x; };
+    const MfRow<D> r = mf_rowctx<D>(M, p);
     df w1[2][2], w2[2][2], wm[2][2];
 #pragma unroll
     for (int a = 0; a < 2; a++)
 #pragma unroll
         for (int b = 0; b < 2; b++) {
-            const int cc = cell(mv<T2>(mv<T1>(p, a - 1), b - 1));
+            const int cc = r.cell + (a - 1) * M.cs[T1] + (b - 1) * M.cs[T2];
             w1[a][b] = d2f(__ldg(M.w + T1 * nc + cc));
             w2[a][b] = d2f(__ldg(M.w + T2 * nc + cc));
             wm[a][b] = d2f(__ldg(M.w + (3 + D) * nc + cc));
@@ -962,26 +1014,23 @@ __device__ __forceinline__ void mf_row2(const MF &M, Pos p, int k0, const df (&o
     for (int nn = 0; nn < 2; nn++)
 #pragma unroll
         for (int b = 0; b < 2; b++) {
-            Pos q;
             df wa, wb;
             float sg;
             int im, i0, ip;
             if (nn == 0) {
-                q = mv<T2>(p, b - 1);
                 sg = b == 0 ? 1.f : -1.f;
                 wa = w1[0][b];
                 wb = w1[1][b];
-                im = mf_face_n<T1>(M, mv<T1>(q, -1));
-                i0 = mf_face_n<T1>(M, q);
-                ip = mf_face_n<T1>(M, mv<T1>(q, 1));
+                i0 = r.f1 + (b - 1) * M.fs[T1][T2];
+                im = i0 - M.fs[T1][T1];
+                ip = i0 + M.fs[T1][T1];
             } else {
-                q = mv<T1>(p, b - 1);
                 sg = b == 0 ? -1.f : 1.f;
                 wa = w2[b][0];
                 wb = w2[b][1];
-                im = mf_face_n<T2>(M, mv<T2>(q, -1));
-                i0 = mf_face_n<T2>(M, q);
-                ip = mf_face_n<T2>(M, mv<T2>(q, 1));
+                i0 = r.f2 + (b - 1) * M.fs[T2][T1];
+                im = i0 - M.fs[T2][T2];
+                ip = i0 + M.fs[T2][T2];
             }
             const df ca = scale(wa, sg), cb = scale(wb, sg), c0 = scale(add(wa, wb), 2.f * sg);
 #pragma unroll
@@ -1002,9 +1051,8 @@ __device__ __forceinline__ void mf_row2(const MF &M, Pos p, int k0, const df (&o
     for (int a = 0; a < 3; a++)
 #pragma unroll
         for (int b = 0; b < 3; b++) {
-            const Pos q = mv<T2>(mv<T1>(p, a - 1), b - 1);
-            const int e = mf_edge(M, D, q.x, q.y, q.z);
-            if (mf_dirichlet(M, D, q.x, q.y, q.z, e)) continue;
+            if (mf_mass_dir(r, a, b)) continue;
+            const int e = mf_mass_edge(M, r, a, b);
 #pragma unroll
             for (int u = 0; u < 2; u++) {
                 const dfc xe = from4(__ldg(x + e * SP + k0 + u));
@@ -1052,7 +1100,7 @@ k_mf_edges2(int nb, MF M, const float2 *__restrict__ omega, const float4 *__rest
             const long long i = (long long)e * SP + k0;
             const float4 sv[2] = {__ldg(s + i), __ldg(s + i + 1)};
             dfc y[2];
-            if (mf_dirichlet(M, d, p.x, p.y, p.z, e)) {
+            if (mf_dirichlet(M, d, p.x, p.y, p.z)) {
                 y[0] = from4(sv[0]);
                 y[1] = from4(sv[1]);
             } else if (d == 0) {
@@ -1110,7 +1158,7 @@ k_mf_edges(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restr
         const long long i = (long long)e * SP + k;
         const float4 sv4 = __ldg(s + i);
         dfc y;
-        if (mf_dirichlet(M, d, p.x, p.y, p.z, e))
+        if (mf_dirichlet(M, d, p.x, p.y, p.z))
             y = from4(sv4);
         else if (d == 0)
             y = mf_row<SP, 0>(M, p, k, om, s);
@@ -1208,17 +1256,17 @@ __device__ __forceinline__ dfc mf_row_g(const MF &M, Pos p, int k, df om, const 
 {
     constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
     const int nc = (int)M.ncell;
-    auto cell = [&](Pos q) { return (q.z * (M.ny - 1) + q.y) * (M.nx - 1) + q.x; };
+    const MfRow<D> r = mf_rowctx<D>(M, p);
     df wm[2][2];
 #pragma unroll
     for (int a = 0; a < 2; a++)
 #pragma unroll
         for (int b = 0; b < 2; b++)
-            wm[a][b] = d2f(__ldg(M.w + (3 + D) * nc + cell(mv<T2>(mv<T1>(p, a - 1), b - 1))));
-    const dfc g1a = from4(__ldg(M.g + mf_face_n<T1>(M, mv<T2>(p, -1)) * SP + k));
-    const dfc g1b = from4(__ldg(M.g + mf_face_n<T1>(M, p) * SP + k));
-    const dfc g2a = from4(__ldg(M.g + mf_face_n<T2>(M, mv<T1>(p, -1)) * SP + k));
-    const dfc g2b = from4(__ldg(M.g + mf_face_n<T2>(M, p) * SP + k));
+            wm[a][b] = d2f(__ldg(M.w + (3 + D) * nc + r.cell + (a - 1) * M.cs[T1] + (b - 1) * M.cs[T2]));
+    const dfc g1a = from4(__ldg(M.g + (r.f1 - M.fs[T1][T2]) * SP + k));
+    const dfc g1b = from4(__ldg(M.g + r.f1 * SP + k));
+    const dfc g2a = from4(__ldg(M.g + (r.f2 - M.fs[T2][T1]) * SP + k));
+    const dfc g2b = from4(__ldg(M.g + r.f2 * SP + k));
     acc kr, ki;
     kr.add(g1a.re); kr.add(neg(g1b.re)); kr.add(neg(g2a.re)); kr.add(g2b.re);
     ki.add(g1a.im); ki.add(neg(g1b.im)); ki.add(neg(g2a.im)); ki.add(g2b.im);
@@ -1232,8 +1280,8 @@ __device__ __forceinline__ dfc mf_row_g(const MF &M, Pos p, int k, df om, const 
     for (int a = 0; a < 3; a++)
 #pragma unroll
         for (int b = 0; b < 3; b++) {
-            const Pos q = mv<T2>(mv<T1>(p, a - 1), b - 1);
-            const dfc xe = mf_x<SP>(M, x, D, q.x, q.y, q.z, k);
+            dfc xe{df{0.f, 0.f}, df{0.f, 0.f}};
+            if (!mf_mass_dir(r, a, b)) xe = from4(__ldg(x + mf_mass_edge(M, r, a, b) * SP + k));
             mr.mac(cm[a][b], xe.re);
             mi.mac(cm[a][b], xe.im);
         }
@@ -1266,7 +1314,7 @@ k_mf_edges_g(int nb, MF M, const float2 *__restrict__ omega, const float4 *__res
         const long long i = (long long)e * SP + k;
         const float4 sv4 = __ldg(s + i);
         dfc y;
-        if (mf_dirichlet(M, d, p.x, p.y, p.z, e))
+        if (mf_dirichlet(M, d, p.x, p.y, p.z))
             y = from4(sv4);
         else if (d == 0)
             y = mf_row_g<SP, 0>(M, p, k, om, s);
@@ -1785,11 +1833,22 @@ struct Impl {
     static MF mfd(const Survey &V)
     {
         const MatFree &F = V.mf;
-        return MF{F.nx, F.ny, F.nz, F.nfx, F.nfy, F.nfz,
-                  (long long)(F.nx - 1) * (F.ny - 1) * (F.nz - 1),
-                  (F.nx - 1) * F.ny * F.nz, F.nx * (F.ny - 1) * F.nz,
-                  (F.ny - 1) * (3 * F.nx - 1) + (2 * F.nx - 1), 3 * F.nx - 1, 2 * F.nx - 1,
-                  F.lattice ? 1 : 0, F.pos, F.w, F.bedge, F.f, F.g};
+        MF M{};
+        M.nx = F.nx;
+        M.ny = F.ny;
+        M.nz = F.nz;
+        M.nfx = F.nfx;
+        M.nfy = F.nfy;
+        M.nfz = F.nfz;
+        M.ncell = (long long)(F.nx - 1) * (F.ny - 1) * (F.nz - 1);
+        M.nex = (F.nx - 1) * F.ny * F.nz;
+        M.ney = F.nx * (F.ny - 1) * F.nz;
+        mf_strides(M);
+        M.pos = F.pos;
+        M.w = F.w;
+        M.f = F.f;
+        M.g = F.g;
+        return M;
     }
     static void spmv(Survey &V, int mode)
     {
@@ -2151,10 +2210,10 @@ namespace {
 // every node against the lattice (coordinates on the node lines, surface
 // nodes Dirichlet) and every edge against RegularMeshBuilder's numbering
 // (the +d edge of node (i, j, k) at its closed-form number joins n and its
-// +d neighbour), and writes the edge's Dirichlet flag and its row position;
-// k_mfb_cells checks the cells' nodes and materials and writes the weights.
-// bad[0] counts mismatches of the structure, bad[1] Dirichlet flags that
-// differ from the lattice rule.
+// +d neighbour) and writes the edge's row position; k_mfb_cells checks the
+// cells' nodes and materials and writes the weights.  bad[0] counts
+// mismatches of the structure, bad[1] edges whose Dirichlet flag (both
+// nodes Dirichlet) differs from the lattice rule.
 struct MfbLines {
     const double *x, *y, *z;   // node lines
     const double *mu, *sigma;  // per material
@@ -2163,7 +2222,7 @@ struct MfbLines {
 
 __global__ void k_mfb_nodes(MF M, MfbLines L, int nb, const double *__restrict__ xyz,
                             const unsigned char *__restrict__ bnode, const int *__restrict__ edges,
-                            unsigned char *bedge, unsigned *pos, int *bad)
+                            unsigned *pos, int *bad)
 {
     const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int nx = M.nx, ny = M.ny, nz = M.nz;
@@ -2186,7 +2245,6 @@ __global__ void k_mfb_nodes(MF M, MfbLines L, int nb, const double *__restrict__
         const int n2 = (int)n + step[d];
         if (edges[2 * e] != (int)n || edges[2 * e + 1] != n2) nbad++;
         const bool be = bnode[n] && bnode[n2];
-        bedge[e] = be;
         if (be != want[d]) nlat++;
         long long row;
         if (d == 0) row = ((long long)k * ny + j) * (nx - 1) + i;
@@ -2310,7 +2368,7 @@ int matfree_build(Survey &V, const MatFreeMesh &a, const DevMesh &dm, int kuz, i
     double *d_lines = nullptr;
     int *d_bad = nullptr;
     int rc;
-    if ((rc = dev_alloc(&F.pos, (size_t)P.nb)) || (rc = dev_alloc(&F.bedge, (size_t)P.nb)) ||
+    if ((rc = dev_alloc(&F.pos, (size_t)P.nb)) ||
         (rc = dev_alloc(&F.w, (size_t)6 * ncell)) ||
         (rc = dev_alloc(&F.f, (size_t)(F.nfx + F.nfy + F.nfz) * V.SP)) ||
         (rc = dev_alloc(&F.g, (size_t)(F.nfx + F.nfy + F.nfz) * V.SP)) ||
@@ -2337,13 +2395,14 @@ int matfree_build(Survey &V, const MatFreeMesh &a, const DevMesh &dm, int kuz, i
         M.ncell = ncell;
         M.nex = (int)nex;
         M.ney = (int)ney;
-        M.plane = (ny - 1) * (3 * nx - 1) + (2 * nx - 1);
-        M.l3 = 3 * nx - 1;
-        M.l2 = 2 * nx - 1;
+        M.nfx = F.nfx;
+        M.nfy = F.nfy;
+        M.nfz = F.nfz;
+        mf_strides(M);
         const MfbLines L{d_lines, d_lines + nx, d_lines + nx + ny, d_lines + lines.size(),
                          d_lines + lines.size() + nmat, nmat};
         k_mfb_nodes<<<ceil_div(kuz, kB), kB, 0, V.st>>>(M, L, P.nb, dm.xyz, dm.bnode, dm.edges,
-                                                       F.bedge, F.pos, d_bad);
+                                                       F.pos, d_bad);
         k_mfb_cells<<<ceil_div(ncell, kB), kB, 0, V.st>>>(M, L, dm.nver, dm.nver_stride, dm.nvkat, om,
                                                          scale, F.w, d_bad);
         note_launches(2);
@@ -2358,13 +2417,15 @@ int matfree_build(Survey &V, const MatFreeMesh &a, const DevMesh &dm, int kuz, i
         set_last_error(err, "matrix-free tables", __FILE__, __LINE__);
         return MTGPU_ERR_CUDA;
     }
-    if (bad[0] != 0) {
-        F.release();   // not a tensor mesh in the builder's numbering: variant off
+    if (bad[0] != 0 || bad[1] != 0) {
+        // not a tensor mesh in the builder's numbering, or Dirichlet edges
+        // other than the lattice's: variant off
+        F.release();
         return MTGPU_OK;
     }
-    // the tiled variant derives the Dirichlet edges from the lattice: an edge
-    // is Dirichlet iff one of its two transverse node lines is on the surface
-    F.lattice = bad[1] == 0;
+    // the kernels derive the Dirichlet edges from the lattice: an edge is
+    // Dirichlet iff one of its two transverse node lines is on the surface
+    F.lattice = true;
     F.on = true;
     // set-up check against the stored-matrix SpMV on a test vector
     const int ch = V.ch;

@@ -36,11 +36,10 @@ struct MatFree {
     long long nfx = 0, nfy = 0, nfz = 0;
     unsigned *pos = nullptr;         // [nb] rows x-, y-, z-edges: i | j << 10 | k << 20
     float2 *w = nullptr;             // [6][cells] double-float wF/3 (x, y, z), wM/9 (x, y, z)
-    unsigned char *bedge = nullptr;  // [nb] Dirichlet edges
     float4 *f = nullptr;             // face circulations [faces][SP]
     float4 *g = nullptr;             // face mass applied to them, F f [faces][SP] (variant 35)
     double check = -1.0;             // set-up check: max |A_mf s - A s| / max |A s|
-    bool lattice = false;            // Dirichlet edges follow the lattice rule
+    bool lattice = false;            // Dirichlet edges follow the lattice rule (always, when on)
     bool tiled = false;              // variant 34 equals variant 32 bit for bit
     bool tile_checked = false;       // ... and that was checked (on first request)
     bool gface = false;              // the D^T (F f) form agrees with variant 32 (variant 35)
