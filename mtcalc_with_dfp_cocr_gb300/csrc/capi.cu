@@ -169,6 +169,8 @@ int solve_double_float_host(int nb, const int *ig, const int *jg, const int *idi
     if ((rc = validate_mesh(mesh))) return rc;
     cudaStream_t st;
     MTGPU_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    PhaseTrace trace(st, "drop-in");
+    trace.mark("validation");
     SellMatrix A;
     ParamMatrix P;
     Survey V;
@@ -179,9 +181,11 @@ int solve_double_float_host(int nb, const int *ig, const int *jg, const int *idi
         if (!(rc = upload_lower(nb, ig, jg, idi, ijg, di, gg, L, st)))
             rc = sell_from_block2x2_device(nb, L.ig, L.jg, L.idi, L.ijg, L.di, L.gg, ig[nb], A, st);
         note_launches(5);
+        trace.mark("SLAE upload, SELL");
     }
     const double one = 1.0;
     if (!rc) rc = param_from_sell(A, P, st);
+    trace.mark("K, M split");
     if (!rc) {
         A.release();
         // the mesh for the matrix-free SpMV (tensor meshes): mu is taken as
@@ -207,7 +211,9 @@ int solve_double_float_host(int nb, const int *ig, const int *jg, const int *idi
             auto it = g_tuned.find(key);
             if (it != g_tuned.end()) pin = it->second;
         }
+        trace.mark("pattern key");
         rc = survey_setup(P, mesh, 1, &one, V, st, nullptr, xyz ? &mm : nullptr, pin);
+        trace.mark("survey set-up");
         if (!rc && pin < 0) {
             std::lock_guard<std::mutex> lk(g_tune_mu);
             g_tuned[key] = V.ch;
@@ -215,8 +221,10 @@ int solve_double_float_host(int nb, const int *ig, const int *jg, const int *idi
     }
     if (!rc && !(rc = upload(&db, (const double2 *)pr, nb, st)) &&
         !(rc = upload(&dx, (const double2 *)x, nb, st))) {
+        trace.mark("b, x upload");
         const double t1 = now_seconds();
         rc = survey_solve(V, db, dx, eps, maxiter, verify, 16, &ss);
+        trace.mark("solve");
         if (rc > -100) {
             cudaError_t e = cudaMemcpyAsync(x, dx, sizeof(double2) * nb, cudaMemcpyDeviceToHost, st);
             if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -237,11 +245,13 @@ int solve_double_float_host(int nb, const int *ig, const int *jg, const int *idi
         }
     }
     cudaStreamSynchronize(st);
+    trace.mark("x download");
     dev_free(db);
     dev_free(dx);
     V.release();
     P.release();
     A.release();
+    trace.mark("release");
     cudaStreamDestroy(st);
     return rc;
 }

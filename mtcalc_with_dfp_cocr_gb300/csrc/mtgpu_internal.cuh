@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <algorithm>
 #include <vector>
 
@@ -193,4 +194,29 @@ struct mtgpu_cocr_s {
 namespace mtgpu {
 int make_stream(mtgpu_cocr_s *c, void *stream);
 double now_seconds();
+
+// MTGPU_TRACE=1 (environment): the phases of a set-up on stderr, each
+// after a synchronisation of its stream so that device work is charged to
+// the phase that launched it
+struct PhaseTrace {
+    bool on = false;
+    cudaStream_t st;
+    const char *what;
+    double t0 = 0.0, last = 0.0;
+    PhaseTrace(cudaStream_t s, const char *w) : st(s), what(w)
+    {
+        const char *e = getenv("MTGPU_TRACE");
+        on = e && *e == '1';
+        t0 = last = now_seconds();
+    }
+    void mark(const char *phase)
+    {
+        if (!on) return;
+        cudaStreamSynchronize(st);
+        const double now = now_seconds();
+        fprintf(stderr, "[mtgpu] %s %-22s %8.2f ms (total %8.2f)\n", what, phase, 1e3 * (now - last),
+                1e3 * (now - t0));
+        last = now;
+    }
+};
 }  // namespace mtgpu

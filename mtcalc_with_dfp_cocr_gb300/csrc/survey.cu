@@ -324,16 +324,22 @@ k_edge(int n, const int *__restrict__ tp, const int *__restrict__ tj, const floa
     const bool on = sys[k].status == kRun;
     const dfc be = from_d2(sys[k].beta);
     acc awr, awi;
-    const int rpb = kB / SP;
-    for (int e = blockIdx.x * rpb + threadIdx.x / SP; e < n; e += gridDim.x * rpb) {
-        if (!on) continue;
+    const int rpb = kB / SP, stride = gridDim.x * rpb;
+    // the compact G^T row of the next element is loaded one element ahead,
+    // so that this element's h gathers issue with its other loads
+    const int e_first = blockIdx.x * rpb + threadIdx.x / SP;
+    int2 r2n = make_int2(-1, -1);
+    if (tn && on && e_first < n) r2n = __ldg(tn + e_first);
+    for (int e = e_first; e < n; e += stride) {
+        if (!on) break;
         const long long idx = (long long)e * SP + k;
         // G^T row: compact (the rows of the edge's two nodes, -1/2 and +1/2
-        // in that order, one dependent load) or the CSR of T-matrix meshes
+        // in that order) or the CSR of T-matrix meshes
         int j0, j1;
         int2 r2 = make_int2(-1, -1);
         if (tn) {
-            r2 = __ldg(tn + e);
+            r2 = r2n;
+            if (e + stride < n) r2n = __ldg(tn + e + stride);
             j0 = 0;
             j1 = (r2.x >= 0) + (r2.y >= 0);
         } else {
@@ -724,14 +730,13 @@ k_spmv_r2(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restr
 struct MF {
     int nx, ny, nz;
     long long nfx, nfy, nfz, ncell;
-    int nex, ney;              // x- and y-edges: the first two segments of the row order
     int plane, l3, l2;         // edges per node plane below the top one; per node line below / in it
     // strides of the index grids along x, y, z: faces of normal n (fs[n]),
     // cells (cs), and the edges of one direction away from the surface
     // (es = 3, l3, plane: every node before them has its +x, +y, +z edge)
     int fs[3][3], cs[3], es[3];
     int fb[3];                 // first face of each normal
-    const unsigned *pos;       // row (direction-major order) -> i | j << 10 | k << 20
+    const unsigned *pos;       // row -> i | j << 10 | k << 20 | direction << 30 (plane by plane)
     const float2 *w;
     float4 *f;
     float4 *g;                 // F f (variant 35)
@@ -803,6 +808,63 @@ __device__ __forceinline__ dfc mf_x(const MF &M, const float4 *__restrict__ x, i
 {
     if (mf_dirichlet(M, d, i, j, kk)) return dfc{df{0.f, 0.f}, df{0.f, 0.f}};
     return from4(__ldg(x + mf_edge_in(M, d, i, j, kk) * SP + k));
+}
+
+// k_node on a lattice mesh whose G rows are its interior nodes in node
+// order (checked at set-up by k_g_lattice_check): row v is node (i, j, k)
+// = v's position in the (nx-2) x (ny-2) x (nz-2) interior, and its entries
+// are the node's six edges by increasing number, -z, -y, -x (+1/2), +x,
+// +y, +z (-1/2), computed instead of read: the same products in the same
+// order as k_node, without the CSR's dependent loads.
+template <int SP>
+__global__ void __launch_bounds__(kB)
+k_node_lat(MF M, int m, const float4 *__restrict__ ds, const float4 *__restrict__ z,
+           const float4 *__restrict__ a, float4 *__restrict__ h, const SysState *sys, int use_beta)
+{
+    const int k = threadIdx.x % SP;
+    if (sys[k].status != kRun) return;
+    const dfc be = from_d2(sys[k].beta);
+    const int ix = M.nx - 2, iy = M.ny - 2;
+    const int rpb = kB / SP;
+    for (int v = blockIdx.x * rpb + threadIdx.x / SP; v < m; v += gridDim.x * rpb) {
+        const int i = v % ix + 1, t = v / ix, j = t % iy + 1, kk = t / iy + 1;
+        const int e0 = mf_edge_in(M, 0, i, j, kk);
+        const int es[6] = {e0 + 2 - M.plane, e0 + 1 - M.l3, e0 - 3, e0, e0 + 1, e0 + 2};
+        float4 zv[6], av[6];
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+            zv[q] = __ldg(z + (long long)es[q] * SP + k);
+            av[q] = use_beta ? __ldg(a + (long long)es[q] * SP + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        const float4 dsv = __ldg(ds + (long long)v * SP + k);
+        acc hr, hi;
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+            dfc an = from4(zv[q]);
+            if (use_beta) an = caxpy(an, be, from4(av[q]));
+            const float g = q < 3 ? 0.5f : -0.5f;
+            hr.macf(an.re, g);
+            hi.macf(an.im, g);
+        }
+        h[(long long)v * SP + k] = to4(cmul(dfc{hr.get(), hi.get()}, from4(dsv)));
+    }
+}
+
+// counts the G rows that differ from k_node_lat's lattice form
+__global__ void k_g_lattice_check(MF M, int m, const int *__restrict__ gp, const int *__restrict__ gj,
+                                  const float *__restrict__ gv, int *bad)
+{
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= m) return;
+    const int ix = M.nx - 2, iy = M.ny - 2;
+    const int i = v % ix + 1, t = v / ix, j = t % iy + 1, kk = t / iy + 1;
+    const int e0 = mf_edge_in(M, 0, i, j, kk);
+    const int es[6] = {e0 + 2 - M.plane, e0 + 1 - M.l3, e0 - 3, e0, e0 + 1, e0 + 2};
+    int nbad = gp[v + 1] - gp[v] != 6;
+    if (!nbad)
+        for (int q = 0; q < 6; q++)
+            if (gj[gp[v] + q] != es[q] || gv[gp[v] + q] != (q < 3 ? 0.5f : -0.5f)) nbad = 1;
+    if (nbad) atomicAdd(bad, 1);
 }
 
 // f = D s: x(e0) + x(e1) - x(e2) - x(e3) around every face (counterclockwise
@@ -1093,8 +1155,8 @@ k_mf_edges2(int nb, MF M, const float2 *__restrict__ omega, const float4 *__rest
     const int rpb = kB / H;
     if (on[0] || on[1]) {
         for (int row = blockIdx.x * rpb + threadIdx.x / H; row < nb; row += gridDim.x * rpb) {
-            const int d = row < M.nex ? 0 : (row < M.nex + M.ney ? 1 : 2);
             const unsigned c = __ldg(M.pos + row);
+            const int d = (int)(c >> 30);
             const Pos p{(int)(c & 1023u), (int)((c >> 10) & 1023u), (int)((c >> 20) & 1023u)};
             const int e = mf_edge(M, d, p.x, p.y, p.z);
             const long long i = (long long)e * SP + k0;
@@ -1151,8 +1213,8 @@ k_mf_edges(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restr
     const int rpb = kB / SP;
     for (int row = blockIdx.x * rpb + threadIdx.x / SP; row < nb; row += gridDim.x * rpb) {
         if (!on) continue;
-        const int d = row < M.nex ? 0 : (row < M.nex + M.ney ? 1 : 2);
         const unsigned c = __ldg(M.pos + row);
+        const int d = (int)(c >> 30);
         const Pos p{(int)(c & 1023u), (int)((c >> 10) & 1023u), (int)((c >> 20) & 1023u)};
         const int e = mf_edge(M, d, p.x, p.y, p.z);
         const long long i = (long long)e * SP + k;
@@ -1307,8 +1369,8 @@ k_mf_edges_g(int nb, MF M, const float2 *__restrict__ omega, const float4 *__res
     const int rpb = kB / SP;
     for (int row = blockIdx.x * rpb + threadIdx.x / SP; row < nb; row += gridDim.x * rpb) {
         if (!on) continue;
-        const int d = row < M.nex ? 0 : (row < M.nex + M.ney ? 1 : 2);
         const unsigned c = __ldg(M.pos + row);
+        const int d = (int)(c >> 30);
         const Pos p{(int)(c & 1023u), (int)((c >> 10) & 1023u), (int)((c >> 20) & 1023u)};
         const int e = mf_edge(M, d, p.x, p.y, p.z);
         const long long i = (long long)e * SP + k;
@@ -1830,6 +1892,7 @@ struct Impl {
         return TileMat{P.d_wc, P.d_wr, P.d_pc, P.d_pr, V.kc, V.mc, V.kr, V.lc, V.lr,
                        V.uoff, V.ucol, V.tile_T, V.ntiles, P.nslices};
     }
+    static void mfd_into(const Survey &V, MF &M) { M = mfd(V); }
     static MF mfd(const Survey &V)
     {
         const MatFree &F = V.mf;
@@ -1841,14 +1904,22 @@ struct Impl {
         M.nfy = F.nfy;
         M.nfz = F.nfz;
         M.ncell = (long long)(F.nx - 1) * (F.ny - 1) * (F.nz - 1);
-        M.nex = (F.nx - 1) * F.ny * F.nz;
-        M.ney = F.nx * (F.ny - 1) * F.nz;
         mf_strides(M);
         M.pos = F.pos;
         M.w = F.w;
         M.f = F.f;
         M.g = F.g;
         return M;
+    }
+    // h = D_S G (src + beta a): the lattice form where G is the lattice's
+    static void node(Survey &V, const float4 *src, const float4 *a, int use_beta)
+    {
+        if (V.g_lat)
+            k_node_lat<SP><<<V.g_node_lat, kB, 0, V.st>>>(mfd(V), V.G.m, V.ds, src, a, V.h, V.sys,
+                                                          use_beta);
+        else
+            k_node<SP><<<V.g_node, kB, 0, V.st>>>(V.G.m, V.G.d_gp, V.G.d_gj, V.gv32, V.ds, src, a,
+                                                  V.h, V.sys, use_beta);
     }
     static void spmv(Survey &V, int mode)
     {
@@ -1922,8 +1993,7 @@ struct Impl {
             return;
         }
         if (V.G.m > 0)
-            k_node<SP><<<V.g_node, kB, 0, V.st>>>(V.G.m, V.G.d_gp, V.G.d_gj, V.gv32, V.ds, V.z, V.a,
-                                                  V.h, V.sys, 1);
+            node(V, V.z, V.a, 1);
         k_edge<SP><<<V.g_edge, kB, 0, V.st>>>(V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.G.d_tn, V.da, V.h, V.s, V.z,
                                               V.p, V.a, V.w, V.sys, V.partials, 1);
         k_update<SP><<<V.g_update, kB, 0, V.st>>>(V.nb, V.p, V.a, V.w, V.sm, V.x, V.r, V.s, V.sys,
@@ -1940,8 +2010,7 @@ struct Impl {
             return;
         }
         if (V.G.m > 0)
-            k_node<SP><<<V.g_node, kB, 0, V.st>>>(V.G.m, V.G.d_gp, V.G.d_gj, V.gv32, V.ds, V.z, ain,
-                                                  V.h, V.sys, 1);
+            node(V, V.z, ain, 1);
         k_edge<SP><<<V.g_edge, kB, 0, V.st>>>(V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.G.d_tn, V.da, V.h,
                                               V.s, V.z, V.p, ain, V.w, V.sys, V.partials, 1);
     }
@@ -1981,8 +2050,7 @@ struct Impl {
         k_init<SP><<<V.g_init, kB, 0, V.st>>>(V.nb, mat(V), V.omega, V.b, V.x, V.r, V.sm, V.sys,
                                               V.partials);
         if (V.G.m > 0)
-            k_node<SP><<<V.g_node, kB, 0, V.st>>>(V.G.m, V.G.d_gp, V.G.d_gj, V.gv32, V.ds, V.r, V.a,
-                                                  V.h, V.sys, 0);
+            node(V, V.r, V.a, 0);
         k_edge<SP><<<V.g_edge, kB, 0, V.st>>>(V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.G.d_tn, V.da, V.h, V.r, V.z,
                                               V.p, V.a, V.s, V.sys, V.partials, 0);
         cudaMemsetAsync(V.p, 0, sizeof(float4) * (size_t)V.nb * SP, V.st);
@@ -2018,6 +2086,7 @@ struct Impl {
         auto g = [&](const void *f, int work) { return std::max(1, std::min(occ(f) * nsm, work)); };
         V.g_init = g((const void *)k_init<SP>, V.grid_rows);
         V.g_node = g((const void *)k_node<SP>, V.grid_nodes);
+        V.g_node_lat = g((const void *)k_node_lat<SP>, V.grid_nodes);
         V.g_edge = g((const void *)k_edge<SP>, V.grid_rows);
         V.g_update = g((const void *)k_update<SP>, V.grid_rows);
         V.g_true = g((const void *)k_res64<SP>, V.grid_rows);
@@ -2246,11 +2315,16 @@ __global__ void k_mfb_nodes(MF M, MfbLines L, int nb, const double *__restrict__
         if (edges[2 * e] != (int)n || edges[2 * e + 1] != n2) nbad++;
         const bool be = bnode[n] && bnode[n2];
         if (be != want[d]) nlat++;
-        long long row;
-        if (d == 0) row = ((long long)k * ny + j) * (nx - 1) + i;
-        else if (d == 1) row = M.nex + ((long long)k * (ny - 1) + j) * nx + i;
-        else row = (long long)M.nex + M.ney + ((long long)k * ny + j) * nx + i;
-        pos[row] = (unsigned)i | ((unsigned)j << 10) | ((unsigned)k << 20);
+        // rows plane by plane, in a plane its x-, y-, then z-edges (i
+        // fastest): a warp's rows share their direction except at the two
+        // boundaries of a plane, and the three edges of a node, adjacent in
+        // the vectors, are read within one plane's sweep
+        const long long xr = (long long)(nx - 1) * ny, yr = (long long)nx * (ny - 1);
+        long long row = (long long)k * (xr + yr + (long long)nx * ny);
+        if (d == 0) row += (long long)j * (nx - 1) + i;
+        else if (d == 1) row += xr + (long long)j * nx + i;
+        else row += xr + yr + (long long)j * nx + i;
+        pos[row] = (unsigned)i | ((unsigned)j << 10) | ((unsigned)k << 20) | ((unsigned)d << 30);
     }
     if (nbad) atomicAdd(&bad[0], nbad);
     if (nlat) atomicAdd(&bad[1], nlat);
@@ -2393,8 +2467,6 @@ int matfree_build(Survey &V, const MatFreeMesh &a, const DevMesh &dm, int kuz, i
         M.ny = ny;
         M.nz = nz;
         M.ncell = ncell;
-        M.nex = (int)nex;
-        M.ney = (int)ney;
         M.nfx = F.nfx;
         M.nfy = F.nfy;
         M.nfz = F.nfz;
@@ -2671,37 +2743,11 @@ int prec_tile_setup(Survey &V, int nsm)
 
 }  // namespace
 
-namespace {
-// MTGPU_TRACE=1 (environment): the set-up's phases on stderr, each after a
-// synchronisation of the stream so that device work is charged to its phase
-struct PhaseTrace {
-    bool on;
-    cudaStream_t st;
-    std::chrono::steady_clock::time_point t0, last;
-    explicit PhaseTrace(cudaStream_t s) : st(s)
-    {
-        const char *e = getenv("MTGPU_TRACE");
-        on = e && *e == '1';
-        t0 = last = std::chrono::steady_clock::now();
-    }
-    void mark(const char *what)
-    {
-        if (!on) return;
-        cudaStreamSynchronize(st);
-        const auto now = std::chrono::steady_clock::now();
-        fprintf(stderr, "[mtgpu] survey set-up %-22s %8.2f ms (total %8.2f)\n", what,
-                std::chrono::duration<double, std::milli>(now - last).count(),
-                std::chrono::duration<double, std::milli>(now - t0).count());
-        last = now;
-    }
-};
-}  // namespace
-
 int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const double *omega,
                  Survey &V, cudaStream_t st, const mtgpu_assembly_s *a, const MatFreeMesh *mfm,
                  int pin_variant)
 {
-    PhaseTrace trace(st);
+    PhaseTrace trace(st, "survey set-up");
     V.release();
     MTGPU_CHECK_ARG(S >= 1 && S <= 32, "a survey batch holds 1 to 32 systems");
     V.P = &P;
@@ -2807,7 +2853,72 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
     } else if (mfm && (rc = matfree_build(V, *mfm, dmu.view, mesh.n_nodes_c, mesh.kpar, nsm))) {
         return rc;
     }
-    trace.mark("matrix-free tables");
+    // G in the lattice form (k_node_lat): every interior node a row, in
+    // node order, its six edges in order
+    V.g_lat = false;
+    if (V.mf.on && V.G.m > 0 &&
+        (long long)V.G.m == (long long)(V.mf.nx - 2) * (V.mf.ny - 2) * (V.mf.nz - 2)) {
+        int *d_bad = nullptr, bad = 1;
+        if ((rc = dev_alloc(&d_bad, 1))) return rc;
+        cudaError_t e = cudaMemsetAsync(d_bad, 0, sizeof(int), st);
+        if (e == cudaSuccess) {
+            MF M{};
+            MTGPU_SP_DISPATCH(V.SP, mfd_into(V, M));
+            k_g_lattice_check<<<ceil_div(V.G.m, kB), kB, 0, st>>>(M, V.G.m, V.G.d_gp, V.G.d_gj,
+                                                                 V.gv32, d_bad);
+            note_launches(1);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        dev_free(d_bad);
+        if (e != cudaSuccess) {
+            set_last_error(e, "lattice G check", __FILE__, __LINE__);
+            return MTGPU_ERR_CUDA;
+        }
+        V.g_lat = bad == 0;
+    }
+    if (V.g_lat) {
+        // both node kernels on the same pseudo-random z, a and beta: the
+        // lattice form is kept only if its h equals the CSR form's
+        std::vector<SysState> init(32);
+        for (int k = 0; k < 32; k++) {
+            SysState q{};
+            q.status = k < V.S ? kRun : MTGPU_OK;
+            q.beta = make_double2(0.375, -0.25);
+            init[k] = q;
+        }
+        const long long n = (long long)V.nb * V.SP, nh = (long long)V.G.m * V.SP;
+        unsigned long long *d_mx = nullptr;
+        if ((rc = dev_alloc(&d_mx, 2))) return rc;
+        k_pattern<<<4 * nsm, kB, 0, st>>>(n, V.z);
+        k_pattern<<<4 * nsm, kB, 0, st>>>(n, V.p);
+        cudaError_t e = cudaMemcpyAsync(V.sys, init.data(), sizeof(SysState) * 32, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) {
+            MTGPU_SP_DISPATCH(V.SP, node(V, V.z, V.p, 1));   // lattice form -> h
+            e = cudaMemcpyAsync(V.w, V.h, sizeof(float4) * nh, cudaMemcpyDeviceToDevice, st);
+        }
+        if (e == cudaSuccess) {
+            V.g_lat = false;
+            MTGPU_SP_DISPATCH(V.SP, node(V, V.z, V.p, 1));   // CSR form -> h
+            e = cudaMemsetAsync(d_mx, 0, sizeof(unsigned long long) * 2, st);
+        }
+        if (e == cudaSuccess) {
+            k_maxdiff<<<4 * nsm, kB, 0, st>>>(nh, V.h, V.w, d_mx);
+            note_launches(5);
+            e = cudaGetLastError();
+        }
+        unsigned long long mx[2] = {1, 1};
+        if (e == cudaSuccess) e = cudaMemcpyAsync(mx, d_mx, sizeof(mx), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        dev_free(d_mx);
+        if (e != cudaSuccess) {
+            set_last_error(e, "lattice G check", __FILE__, __LINE__);
+            return MTGPU_ERR_CUDA;
+        }
+        V.g_lat = mx[0] == 0;
+    }
+    trace.mark(!V.mf.on ? "no matrix-free tables" : (V.g_lat ? "matrix-free, lattice G" : "matrix-free tables"));
     // the stored matrix's tiles (variants 0, 1) where there is no
     // matrix-free operator; with one they are built only on request
     if (!V.mf.on && (rc = survey_prepare_variant(V, 0))) return rc;
@@ -2827,15 +2938,15 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
         V.ch = pin_variant;
         MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
     } else {
-        // with the matrix-free operator the stored-matrix variants (staged
-        // tiles, 2 or 8 slots in flight, a row per thread) and the tiled
-        // matrix-free one measured slower on every tensor mesh, so only the
-        // 4-slot stored variant stays as a fallback candidate
+        // with the matrix-free operator the stored-matrix variants and the
+        // tiled matrix-free one measured slower on every tensor mesh (whole
+        // iterations on c2 at 2 systems: 0.67 ms and more against 0.57-0.60),
+        // so only the matrix-free forms 32, 33 and 35 are timed
         const int cand[kSpmvVariants] = {0, 1, 2, 4, 8, kRowVariant + 2, kRowVariant + 4, kMatFree,
                                          kMatFree + 1, kMatFree + 2, kMatFree + 3};
         auto tried = [&](int v) {
             if (!V.mf.on) return true;
-            return v == 4 || v == kMatFree || v == kMatFree + 1 || v == kMatFree + 3;
+            return v == kMatFree || v == kMatFree + 1 || v == kMatFree + 3;
         };
         float best = 1e30f;
         int best_ch = 4;

@@ -34,7 +34,7 @@ struct MatFree {
     bool on = false;
     int nx = 0, ny = 0, nz = 0;      // lines per axis
     long long nfx = 0, nfy = 0, nfz = 0;
-    unsigned *pos = nullptr;         // [nb] rows x-, y-, z-edges: i | j << 10 | k << 20
+    unsigned *pos = nullptr;         // [nb] rows plane by plane (x-, y-, z-edges): i | j << 10 | k << 20 | d << 30
     float2 *w = nullptr;             // [6][cells] double-float wF/3 (x, y, z), wM/9 (x, y, z)
     float4 *f = nullptr;             // face circulations [faces][SP]
     float4 *g = nullptr;             // face mass applied to them, F f [faces][SP] (variant 35)
@@ -52,6 +52,8 @@ struct Survey {
     int nb = 0, S = 0, SP = 1;
     int grid_rows = 0, grid_nodes = 0;           // work bounds (blocks that have rows)
     int g_init = 0, g_node = 0, g_edge = 0, g_update = 0, g_spmv = 0, g_true = 0;  // launch grids
+    int g_node_lat = 0;
+    bool g_lat = false;            // G is the lattice's (k_node_lat computes its entries)
     // SpMV variant (autotuned): 0 x and matrix slots staged in shared memory per
     // tile, 1 x staged only, 2/4/8 gathers from global memory with that many slots in flight,
     // kRowVariant + 2/4 (two systems only) one thread per row for both systems

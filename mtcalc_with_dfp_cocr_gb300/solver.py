@@ -34,13 +34,19 @@ def _mesh_args(m: SolveMesh):
 
 def pcocr_2x2_folded(slae: BlockSLAE, mesh: SolveMesh, x0=None, eps=None, maxiter=None,
                      stop_on_true_residual=False, iterations_per_launch=0, write_kit_in=None,
-                     double_float=False):
+                     double_float=False, x=None):
     """Solve A x = pr on the GPU.  Returns (code, x, stats).
 
-    write_kit_in: a directory; when given, the reference entry point
-    (mtgpu_pcocr_2x2_folded) runs there and writes its `kit` file."""
+    x0: initial guess (copied); x: a contiguous float64 array used in place
+    instead, initial guess in and solution out (as the reference's x), e.g.
+    in pinned host memory.  write_kit_in: a directory; when given, the
+    reference entry point (mtgpu_pcocr_2x2_folded) runs there and writes its
+    `kit` file."""
     L = _lib.lib()
-    x = np.zeros(slae.n) if x0 is None else np.array(x0, np.float64)
+    if x is not None:
+        assert x.dtype == np.float64 and x.flags.c_contiguous and x.size == slae.n
+    else:
+        x = np.zeros(slae.n) if x0 is None else np.array(x0, np.float64)
     eps = slae.eps if eps is None else eps
     maxiter = slae.maxiter if maxiter is None else maxiter
     slae_args = (slae.n, i32(slae.ig), i32(slae.jg), i32(slae.idi), i32(slae.ijg),
