@@ -120,6 +120,7 @@ k_mf_tile(MF M, MfTileGrid G, const float2 *__restrict__ omega, const float4 *__
           const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
           SysState *sys, double *partials, int mode)
 {
+    pdl_wait();
     using C = MfTile<SP>;
     constexpr int SB = C::SB, NT = C::NT, NS = C::NS;   // NS: the plane stride of the rings
     // this mesh's tile: TX x TY columns, halo frame NX x (TY + 2)

@@ -48,6 +48,7 @@ k_prec_tile(MF M, PrecGrid G, const float4 *__restrict__ ds, const float4 *__res
             const float4 *__restrict__ a_in, float4 *__restrict__ a_out, float4 *__restrict__ p,
             float4 *__restrict__ w, SysState *sys, double *partials)
 {
+    pdl_wait();
     using C = PrecTile<SP>;
     constexpr int SB = C::SB, TX = C::TX, TY = C::TY, NT = C::NT, NX = C::NX, NS = C::NS;
     extern __shared__ __align__(16) float4 sh[];

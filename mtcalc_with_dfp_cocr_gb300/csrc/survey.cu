@@ -86,15 +86,12 @@ __device__ __forceinline__ long long slot(const long long *p, int row, int k)
 __device__ __forceinline__ df d2f(float2 v) { return df{v.x, v.y}; }
 __device__ __forceinline__ dfc from_d2(double2 v) { return dfc{from_double(v.x), from_double(v.y)}; }
 
-// Per-system FP64 sums of a block: lanes k, k+SP, ... of a warp hold system
-// k.  The block that finishes last adds all block partials in block order
-// and returns true, with the totals in tot[n][k].
-template <int SP, int N, int NT = kB>
-__device__ bool sys_grid_sum(double (&v)[N], double *partials, unsigned int *ticket,
-                             double (*tot)[32])
+// Per-system sums over a block in a fixed order: lanes k, k+SP, ... of a
+// warp hold system k (SP <= 32 divides the warp); a shuffle tree per warp,
+// then thread k < SP adds the warps' sums in warp order into out[n][k].
+template <int SP, int N, int NT>
+__device__ __forceinline__ void sys_block_sum(double (&v)[N], double (*smem)[NT / 32][SP])
 {
-    __shared__ double smem[N][NT / 32][SP];
-    __shared__ bool last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int n = 0; n < N; n++) {
@@ -108,8 +105,29 @@ __device__ bool sys_grid_sum(double (&v)[N], double *partials, unsigned int *tic
         for (int n = 0; n < N; n++) {
             double acc = 0.0;
             for (int q = 0; q < NT / 32; q++) acc += smem[n][q][threadIdx.x];
-            partials[((size_t)n * gridDim.x + blockIdx.x) * SP + threadIdx.x] = acc;
+            v[n] = acc;
         }
+    }
+}
+
+// Per-system FP64 sums over the grid: every block writes its sums, and the
+// block that finishes last adds all block partials and returns true, with
+// the totals in tot[n][k].  The last block spreads that sum over all its
+// threads (thread j*SP + k adds the partials of blocks j, j + NT/SP, ...
+// of system k, then the block tree above): a sum in one thread per system
+// would be a serial chain of gridDim L2 loads at the end of every kernel.
+// The order is fixed, so the totals are run-to-run identical.
+template <int SP, int N, int NT = kB>
+__device__ bool sys_grid_sum(double (&v)[N], double *partials, unsigned int *ticket,
+                             double (*tot)[32])
+{
+    __shared__ double smem[N][NT / 32][SP];
+    __shared__ bool last;
+    sys_block_sum<SP, N, NT>(v, smem);
+    if (threadIdx.x < SP) {
+#pragma unroll
+        for (int n = 0; n < N; n++)
+            partials[((size_t)n * gridDim.x + blockIdx.x) * SP + threadIdx.x] = v[n];
     }
     __threadfence();
     __syncthreads();
@@ -117,18 +135,48 @@ __device__ bool sys_grid_sum(double (&v)[N], double *partials, unsigned int *tic
     __syncthreads();
     if (!last) return false;
     __threadfence();
+    constexpr int G = NT / SP;
+    const int k = threadIdx.x % SP, j = threadIdx.x / SP;
+    double f[N];
+#pragma unroll
+    for (int n = 0; n < N; n++) {
+        double acc = 0.0;
+#pragma unroll 4
+        for (int q = j; q < (int)gridDim.x; q += G)
+            acc += __ldcg(&partials[((size_t)n * gridDim.x + q) * SP + k]);
+        f[n] = acc;
+    }
+    sys_block_sum<SP, N, NT>(f, smem);
     if (threadIdx.x < SP) {
 #pragma unroll
-        for (int n = 0; n < N; n++) {
-            double acc = 0.0;
-            for (int q = 0; q < (int)gridDim.x; q++)
-                acc += __ldcg(&partials[((size_t)n * gridDim.x + q) * SP + threadIdx.x]);
-            tot[n][threadIdx.x] = acc;
-        }
+        for (int n = 0; n < N; n++) tot[n][threadIdx.x] = f[n];
     }
     if (threadIdx.x == 0) *ticket = 0u;
     __syncthreads();
     return true;
+}
+
+// Programmatic dependent launch: the iteration's kernels are launched with
+// the programmatic-serialization attribute, so the next grid is scheduled
+// while the one before it drains; each of them waits here, before its first
+// access to memory, until the grid before it has completed and its writes
+// are visible (a no-op for a kernel launched without the attribute).
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... K, typename... A>
+void pdl(void (*kernel)(K...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, A &&...args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
 }
 
 struct Mat {
@@ -289,6 +337,7 @@ k_node(int m, const int *__restrict__ gp, const int *__restrict__ gj, const floa
        const float4 *__restrict__ ds, const float4 *__restrict__ z, const float4 *__restrict__ a,
        float4 *__restrict__ h, const SysState *sys, int use_beta)
 {
+    pdl_wait();
     const int k = threadIdx.x % SP;
     if (sys[k].status != kRun) return;
     const dfc be = from_d2(sys[k].beta);
@@ -320,6 +369,7 @@ k_edge(int n, const int *__restrict__ tp, const int *__restrict__ tj, const floa
        const float4 *__restrict__ src, const float4 *__restrict__ z, float4 *__restrict__ p,
        float4 *__restrict__ a, float4 *__restrict__ w, SysState *sys, double *partials, int mode)
 {
+    pdl_wait();
     const int k = threadIdx.x % SP;
     const bool on = sys[k].status == kRun;
     const dfc be = from_d2(sys[k].beta);
@@ -430,6 +480,7 @@ k_update(int n, const float4 *__restrict__ p, const float4 *__restrict__ a,
          const float4 *__restrict__ w, const float4 *__restrict__ sm, float4 *__restrict__ x,
          float4 *__restrict__ r, float4 *__restrict__ s, SysState *sys, double *partials)
 {
+    pdl_wait();
     const int k = threadIdx.x % SP;
     const bool on = sys[k].status == kRun;
     const dfc al = from_d2(sys[k].alpha);
@@ -558,6 +609,7 @@ k_spmv(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict
        const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
        SysState *sys, double *partials, int mode)
 {
+    pdl_wait();
     const int k = threadIdx.x % SP;
     const bool on = sys[k].status == kRun;
     const df om = d2f(omega[k]);
@@ -676,6 +728,7 @@ k_spmv_r2(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restr
           const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
           SysState *sys, double *partials, int mode)
 {
+    pdl_wait();
     constexpr int SP = 2;
     bool on[SP];
     df om[SP];
@@ -821,6 +874,7 @@ __global__ void __launch_bounds__(kB)
 k_node_lat(MF M, int m, const float4 *__restrict__ ds, const float4 *__restrict__ z,
            const float4 *__restrict__ a, float4 *__restrict__ h, const SysState *sys, int use_beta)
 {
+    pdl_wait();
     const int k = threadIdx.x % SP;
     if (sys[k].status != kRun) return;
     const dfc be = from_d2(sys[k].beta);
@@ -873,6 +927,7 @@ template <int SP>
 __global__ void __launch_bounds__(kB)
 k_mf_faces(MF M, const float4 *__restrict__ x, const SysState *sys)
 {
+    pdl_wait();
     const int k = threadIdx.x % SP;
     if (sys[k].status != kRun) return;
     const long long nf = M.nfx + M.nfy + M.nfz;
@@ -1140,6 +1195,7 @@ k_mf_edges2(int nb, MF M, const float2 *__restrict__ omega, const float4 *__rest
             const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
             SysState *sys, double *partials, int mode)
 {
+    pdl_wait();
     constexpr int H = SP / 2;
     const int k0 = 2 * (threadIdx.x % H);
     bool on[2];
@@ -1204,6 +1260,7 @@ k_mf_edges(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restr
            const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
            SysState *sys, double *partials, int mode)
 {
+    pdl_wait();
     const int k = threadIdx.x % SP;
     const bool on = sys[k].status == kRun;
     const df om = d2f(omega[k]);
@@ -1246,6 +1303,7 @@ template <int SP>
 __global__ void __launch_bounds__(kB)
 k_mf_gface(MF M, const SysState *sys)
 {
+    pdl_wait();
     const int k = threadIdx.x % SP;
     if (sys[k].status != kRun) return;
     const long long nf = M.nfx + M.nfy + M.nfz;
@@ -1360,6 +1418,7 @@ k_mf_edges_g(int nb, MF M, const float2 *__restrict__ omega, const float4 *__res
              const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
              SysState *sys, double *partials, int mode)
 {
+    pdl_wait();
     const int k = threadIdx.x % SP;
     const bool on = sys[k].status == kRun;
     const df om = d2f(omega[k]);
@@ -1485,6 +1544,7 @@ k_spmv_t(int nb, TileMat A, const float2 *__restrict__ omega, const float4 *__re
          const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
          SysState *sys, double *partials, int mode)
 {
+    pdl_wait();
     extern __shared__ __align__(16) unsigned char smem[];
     const int k = threadIdx.x % SP;
     const bool on = sys[k].status == kRun;
@@ -1738,6 +1798,7 @@ k_res64(int nb, Mat64 A, const double *__restrict__ omega64, const double2 *__re
 template <int SP>
 __global__ void k_fold(long long n, double2 *xacc, float4 *xdf, const int *__restrict__ check)
 {
+    pdl_wait();
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || !check[i % SP]) return;
     const double2 a = xacc[i];
@@ -1915,10 +1976,10 @@ struct Impl {
     static void node(Survey &V, const float4 *src, const float4 *a, int use_beta)
     {
         if (V.g_lat)
-            k_node_lat<SP><<<V.g_node_lat, kB, 0, V.st>>>(mfd(V), V.G.m, V.ds, src, a, V.h, V.sys,
+            pdl(k_node_lat<SP>, V.g_node_lat, kB, 0, V.st, mfd(V), V.G.m, V.ds, src, a, V.h, V.sys,
                                                           use_beta);
         else
-            k_node<SP><<<V.g_node, kB, 0, V.st>>>(V.G.m, V.G.d_gp, V.G.d_gj, V.gv32, V.ds, src, a,
+            pdl(k_node<SP>, V.g_node, kB, 0, V.st, V.G.m, V.G.d_gp, V.G.d_gj, V.gv32, V.ds, src, a,
                                                   V.h, V.sys, use_beta);
     }
     static void spmv(Survey &V, int mode)
@@ -1932,23 +1993,23 @@ struct Impl {
         }
         if (V.ch == kMatFree + 3) {
             const MF M = mfd(V);
-            k_mf_faces<SP><<<V.g_mff, kB, 0, V.st>>>(M, V.s, V.sys);
-            k_mf_gface<SP><<<V.g_mfg, kB, 0, V.st>>>(M, V.sys);
-            k_mf_edges_g<SP><<<V.g_mfe3, kB, 0, V.st>>>(V.nb, M, V.omega, V.s, V.r, V.z, V.sm, V.sys,
+            pdl(k_mf_faces<SP>, V.g_mff, kB, 0, V.st, M, V.s, V.sys);
+            pdl(k_mf_gface<SP>, V.g_mfg, kB, 0, V.st, M, V.sys);
+            pdl(k_mf_edges_g<SP>, V.g_mfe3, kB, 0, V.st, V.nb, M, V.omega, V.s, V.r, V.z, V.sm, V.sys,
                                                        V.partials, mode);
             return;
         }
         if (V.ch == kMatFree || V.ch == kMatFree + 1) {
             const MF M = mfd(V);
-            k_mf_faces<SP><<<V.g_mff, kB, 0, V.st>>>(M, V.s, V.sys);
+            pdl(k_mf_faces<SP>, V.g_mff, kB, 0, V.st, M, V.s, V.sys);
             if constexpr (SP >= 2) {
                 if (V.ch == kMatFree + 1) {
-                    k_mf_edges2<SP><<<V.g_mfe, kB, 0, V.st>>>(V.nb, M, V.omega, V.s, V.r, V.z,
+                    pdl(k_mf_edges2<SP>, V.g_mfe, kB, 0, V.st, V.nb, M, V.omega, V.s, V.r, V.z,
                                                               V.sm, V.sys, V.partials, mode);
                     return;
                 }
             }
-            k_mf_edges<SP><<<V.g_mfe, kB, 0, V.st>>>(V.nb, M, V.omega, V.s, V.r, V.z, V.sm, V.sys,
+            pdl(k_mf_edges<SP>, V.g_mfe, kB, 0, V.st, V.nb, M, V.omega, V.s, V.r, V.z, V.sm, V.sys,
                                                     V.partials, mode);
             return;
         }
@@ -1964,18 +2025,18 @@ struct Impl {
         }
         if constexpr (SP == 2) {
             if (V.ch == kRowVariant + 2) {
-                k_spmv_r2<2><<<V.g_spmv, kB, 0, V.st>>>(V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode);
+                pdl(k_spmv_r2<2>, V.g_spmv, kB, 0, V.st, V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode);
                 return;
             }
             if (V.ch == kRowVariant + 4) {
-                k_spmv_r2<4><<<V.g_spmv, kB, 0, V.st>>>(V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode);
+                pdl(k_spmv_r2<4>, V.g_spmv, kB, 0, V.st, V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode);
                 return;
             }
         }
         switch (V.ch) {
-        case 2: k_spmv<SP, 2><<<V.g_spmv, kB, 0, V.st>>>(V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode); break;
-        case 8: k_spmv<SP, 8><<<V.g_spmv, kB, 0, V.st>>>(V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode); break;
-        default: k_spmv<SP, 4><<<V.g_spmv, kB, 0, V.st>>>(V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode); break;
+        case 2: pdl(k_spmv<SP, 2>, V.g_spmv, kB, 0, V.st, V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode); break;
+        case 8: pdl(k_spmv<SP, 8>, V.g_spmv, kB, 0, V.st, V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode); break;
+        default: pdl(k_spmv<SP, 4>, V.g_spmv, kB, 0, V.st, V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode); break;
         }
     }
     // iteration t of a sequence: the fused preconditioner alternates a's
@@ -1987,16 +2048,16 @@ struct Impl {
             const PrecGrid G{V.pt[0], V.pt[1], V.pt[2], V.pt[3], V.pt[4]};
             k_prec_tile<SP><<<V.g_pt, PrecTile<SP>::NT, PrecTile<SP>::SMEM, V.st>>>(
                 mfd(V), G, V.ds, V.da, V.s, V.z, ain, aout, V.p, V.w, V.sys, V.partials);
-            k_update<SP><<<V.g_update, kB, 0, V.st>>>(V.nb, V.p, aout, V.w, V.sm, V.x, V.r, V.s,
+            pdl(k_update<SP>, V.g_update, kB, 0, V.st, V.nb, V.p, aout, V.w, V.sm, V.x, V.r, V.s,
                                                       V.sys, V.partials);
             spmv(V, 1);
             return;
         }
         if (V.G.m > 0)
             node(V, V.z, V.a, 1);
-        k_edge<SP><<<V.g_edge, kB, 0, V.st>>>(V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.G.d_tn, V.da, V.h, V.s, V.z,
+        pdl(k_edge<SP>, V.g_edge, kB, 0, V.st, V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.G.d_tn, V.da, V.h, V.s, V.z,
                                               V.p, V.a, V.w, V.sys, V.partials, 1);
-        k_update<SP><<<V.g_update, kB, 0, V.st>>>(V.nb, V.p, V.a, V.w, V.sm, V.x, V.r, V.s, V.sys,
+        pdl(k_update<SP>, V.g_update, kB, 0, V.st, V.nb, V.p, V.a, V.w, V.sm, V.x, V.r, V.s, V.sys,
                                                   V.partials);
         spmv(V, 1);
     }
@@ -2011,7 +2072,7 @@ struct Impl {
         }
         if (V.G.m > 0)
             node(V, V.z, ain, 1);
-        k_edge<SP><<<V.g_edge, kB, 0, V.st>>>(V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.G.d_tn, V.da, V.h,
+        pdl(k_edge<SP>, V.g_edge, kB, 0, V.st, V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.G.d_tn, V.da, V.h,
                                               V.s, V.z, V.p, ain, V.w, V.sys, V.partials, 1);
     }
     static void prec_grid(Survey &V, int nsm)
@@ -2069,7 +2130,7 @@ struct Impl {
     static void fold(Survey &V, const int *check)
     {
         const long long n = (long long)V.nb * SP;
-        k_fold<SP><<<(unsigned)((n + kB - 1) / kB), kB, 0, V.st>>>(n, V.xacc, V.x, check);
+        pdl(k_fold<SP>, (unsigned)((n + kB - 1) / kB), kB, 0, V.st, n, V.xacc, V.x, check);
     }
     static void spmv_only(Survey &V) { spmv(V, 0); }
 

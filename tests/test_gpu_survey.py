@@ -139,10 +139,13 @@ def test_spmv_variants_agree(gpu, name, S):
         xyz = w.mesh.xyz()
         e = w.mesh.edges()
         earth = 0.5 * (xyz[e[:, 0], 2] + xyz[e[:, 1], 2]) <= 0.0
-        # the matrix-free operator rounds differently (its own summation
-        # order), so only the 1e-8 FP64 residual ties it to the others: at
-        # 0.01 Hz that leaves the earth edges free at ~1e-7
-        tol = 1e-6 if v >= 32 else 1e-7
+        # every variant rounds its products or dot products in its own order
+        # (the matrix-free operator its own summation, the stored ones their
+        # launch grids' block partials), so the trajectories part at rounding
+        # level and only the 1e-8 FP64 residual ties the solutions together:
+        # that leaves the earth edges free at ~cond x 1e-8, measured up to
+        # ~4e-7
+        tol = 1e-6
         for k in range(S):
             a = x[k].cpu().numpy().view(np.complex128)[earth]
             r = ref[0][k].cpu().numpy().view(np.complex128)[earth]
