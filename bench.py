@@ -291,21 +291,27 @@ def gpu_arm(args):
     # as the iteration launches it: z = A s plus the MRS tail (r read, s_m
     # read and written)
     tail = 3 * 16 * SP * nb
-    if variant in (32, 33):
-        # matrix-free: the faces kernel reads s and the Dirichlet flags and
-        # writes the face circulations; the edges kernel reads them, s, the
-        # flags, 6 double-float weights per cell and the row positions, and
-        # writes z
+    if variant in (32, 33, 35):
+        # matrix-free, per launch as the iteration runs it: the faces kernel
+        # reads s and writes the face circulations f; variants 32/33: the
+        # edges kernel reads f, s, the six double-float weights of every cell
+        # and the row positions and writes z; variant 35: a face kernel reads
+        # f and the cells' face weights and writes g = F f, the edges kernel
+        # reads g, s, the cells' mass weights and the row positions and
+        # writes z.  Each value counted once.
         nx_, ny_, nz_ = m_.nx, m_.ny, m_.nz
         nf = nx_ * (ny_ - 1) * (nz_ - 1) + (nx_ - 1) * ny_ * (nz_ - 1) + (nx_ - 1) * (ny_ - 1) * nz_
-        spmv_bytes = (2 * 16 * SP * nf + 3 * 16 * SP * nb + 2 * nb + 48 * m_.kpar + 4 * nb
-                      + 4 * ny_ * nz_ + tail)
-        edges = "k_mf_edges2" if variant == 33 else "k_mf_edges"
-        spmv_kernel = f"k_mf_faces + {edges} (matrix-free double-float SpMV + MRS tail, S systems)"
-        # the capture is of variant 32 (the autotuning's pick on c2)
-        traffic = SPMV_MF_TRAFFIC_C2 if WORKLOAD == "c2" and variant == 32 else None
-        traffic_src = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_mf_faces<2> + "
-                       "k_mf_edges<2> on c2, profiles/spmv_matfree_c2_s2.md") if traffic else None
+        if variant == 35:
+            spmv_bytes = 16 * SP * (3 * nb + 4 * nf) + 48 * m_.kpar + 4 * nb + tail
+            spmv_kernel = ("k_mf_faces + k_mf_gface + k_mf_edges_g (matrix-free double-float "
+                           "SpMV, face mass applied per face, + MRS tail, S systems)")
+        else:
+            spmv_bytes = 16 * SP * (3 * nb + 2 * nf) + 48 * m_.kpar + 4 * nb + tail
+            edges = "k_mf_edges2" if variant == 33 else "k_mf_edges"
+            spmv_kernel = f"k_mf_faces + {edges} (matrix-free double-float SpMV + MRS tail, S systems)"
+        traffic = SPMV_MF_TRAFFIC_C2.get(variant) if WORKLOAD == "c2" else None
+        traffic_src = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of the variant-{variant} "
+                       f"kernels on c2 (profiles/bench_c2_launch_list.md)") if traffic else None
     else:
         spmv_bytes = nc * (4 + 8 + 8) + nr * (4 + 8) + meta + 2 * S * 16 * nb + tail
         spmv_kernel = (f"k_spmv variant {variant} (batched double-float SELL-32 SpMV + MRS "
