@@ -54,10 +54,10 @@ sys.path.insert(0, ROOT)
 METRIC = "time/solve to rel-res 1e-8: batched mixed vs plain FP64 GPU; SpMV HBM GB/s"
 UNIT = "s/solve"
 WORKLOAD = "c2"
-# DRAM bytes of one launch of the matrix-free SpMV pair on c2 (two lanes,
-# with the MRS tail as the iteration launches it), from the ncu capture
-# summarised in profiles/spmv_matfree_c2_s2.md
-SPMV_MF_TRAFFIC_C2 = 907.7e6
+# DRAM bytes of one matrix-free SpMV on c2 (two lanes, with the MRS tail as
+# the iteration launches it), per variant: the sum of its kernels' ncu
+# dram__bytes_read.sum + dram__bytes_write.sum (profiles/bench_c2_launch_list.md)
+SPMV_MF_TRAFFIC_C2 = {32: 438.2e6, 35: 512.3e6}
 
 
 def load_peaks():
