@@ -47,7 +47,7 @@ struct MfTile {
     static constexpr int OFF_FY = OFF_FX + 2 * SB * NS;            // [2][SB][NS]
     static constexpr int SLOTS = OFF_FY + 2 * SB * NS;
     static constexpr int SMEM = SLOTS * 16;   // the reduction staging reuses it at the end
-    static_assert(NT * 3 * 8 <= SMEM, "staging fits");
+    static_assert(NT * 2 * 8 <= SMEM, "staging fits");
 };
 
 // asynchronous 16-byte copy global -> shared; valid = false writes zeros
@@ -117,7 +117,7 @@ __device__ __forceinline__ dfc mf_mass(acc &kr, acc &ki, const df (&wm)[2][2],
 template <int SP>
 __global__ void __launch_bounds__(MfTile<SP>::NT, 1)
 k_mf_tile(MF M, MfTileGrid G, const float2 *__restrict__ omega, const float4 *__restrict__ s,
-          const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
+          float4 *__restrict__ z,
           SysState *sys, double *partials, int mode)
 {
     pdl_wait();
@@ -165,8 +165,6 @@ k_mf_tile(MF M, MfTileGrid G, const float2 *__restrict__ omega, const float4 *__
     const bool on = sys[kme].status == kRun;
     const df om = d2f(omega[kme]);
     SpmvTail tail;
-    tail.mm = mode ? sys[kme].mrs_mode : 0;
-    tail.wm = from_double(sys[kme].mrs_w);
     const int nc = (int)M.ncell;
 
     // issue the copies of the edges owned by the nodes of plane P (x, y on
@@ -286,7 +284,7 @@ k_mf_tile(MF M, MfTileGrid G, const float2 *__restrict__ omega, const float4 *__
                         for (int B = 0; B < 3; B++) xe[A][B] = exy(k - 1 + B, 0, ii, jj - 1 + A, u_me);
                     y = mf_mass(kr, ki, wm, xe, om);
                 }
-                tail.row(idx, y, sv4, r, z, sm);
+                tail.row(idx, y, sv4, z);
             }
             // y-edge (D = 1, T1 = z, T2 = x)
             if (ey) {
@@ -324,7 +322,7 @@ k_mf_tile(MF M, MfTileGrid G, const float2 *__restrict__ omega, const float4 *__
                         for (int B = 0; B < 3; B++) xe[A][B] = exy(k - 1 + A, 1, ii - 1 + B, jj, u_me);
                     y = mf_mass(kr, ki, wm, xe, om);
                 }
-                tail.row(idx, y, sv4, r, z, sm);
+                tail.row(idx, y, sv4, z);
             }
             // z-edge of layer k (D = 2, T1 = x, T2 = y)
             if (ezp) {
@@ -362,7 +360,7 @@ k_mf_tile(MF M, MfTileGrid G, const float2 *__restrict__ omega, const float4 *__
                         for (int B = 0; B < 3; B++) xe[A][B] = ezs(k, ii - 1 + A, jj - 1 + B, u_me);
                     y = mf_mass(kr, ki, wm, xe, om);
                 }
-                tail.row(idx, y, sv4, r, z, sm);
+                tail.row(idx, y, sv4, z);
             }
         }
         __syncthreads();   // the next plane's copies overwrite ring slots read above
@@ -374,13 +372,12 @@ k_mf_tile(MF M, MfTileGrid G, const float2 *__restrict__ omega, const float4 *__
     double *const red = reinterpret_cast<double *>(sh);
     red[tid] = tail.zsr.to_double();
     red[NT + tid] = tail.zsi.to_double();
-    red[2 * NT + tid] = tail.nn.to_double();
     __syncthreads();
-    double v[3] = {0.0, 0.0, 0.0};
+    double v[2] = {0.0, 0.0};
     if (tid < SP) {
         const int u = tid - sys0;
         if (u >= 0 && u < SB)
-            for (int n = 0; n < 3; n++)
+            for (int n = 0; n < 2; n++)
                 for (int t = u * CPS; t < (u + 1) * CPS; t++) v[n] += red[n * NT + t];
     }
     SpmvTail::finish_v<SP, NT>(v, sys, partials, mode);

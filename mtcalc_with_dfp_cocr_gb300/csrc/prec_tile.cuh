@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(PrecTile<SP>::NT)
 k_prec_tile(MF M, PrecGrid G, const float4 *__restrict__ ds, const float4 *__restrict__ da,
             const float4 *__restrict__ s, const float4 *__restrict__ z,
             const float4 *__restrict__ a_in, float4 *__restrict__ a_out, float4 *__restrict__ p,
-            float4 *__restrict__ w, SysState *sys, double *partials)
+            float4 *__restrict__ w, float4 *__restrict__ x, SysState *sys, double *partials)
 {
     pdl_wait();
     using C = PrecTile<SP>;
@@ -138,6 +138,9 @@ k_prec_tile(MF M, PrecGrid G, const float4 *__restrict__ ds, const float4 *__res
     const int i = i0 + ti, j = j0 + tj;
     const int kme = sys0 + u_me;
     const dfc bme = beta_of(u_me);
+    // the previous iteration's x += alpha p, as in k_edge
+    const bool xpme = sys[kme].xp;
+    const dfc alme = from_d2(sys[kme].alpha);
     const bool col = i < nx && j < ny && sys[kme].status == kRun;
     acc awr, awi;
     for (int k = k0; k < k1; k++) {
@@ -164,6 +167,7 @@ k_prec_tile(MF M, PrecGrid G, const float4 *__restrict__ ds, const float4 *__res
                 const float4 h0 = hh(k, ii, jj, u_me);
                 const float4 h1 = d == 2 ? hh(k + 1, ii, jj, u_me)
                                          : hh(k, ii + (d == 0), jj + (d == 1), u_me);
+                if (xpme) x[idx] = to4(caxpy(from4(x[idx]), alme, from4(pv)));
                 p[idx] = to4(caxpy(from4(srcv), bme, from4(pv)));
                 a_out[idx] = to4(an);
                 const dfc dv = cmul(an, from4(dav));

@@ -367,12 +367,18 @@ __global__ void __launch_bounds__(kB)
 k_edge(int n, const int *__restrict__ tp, const int *__restrict__ tj, const float *__restrict__ tv,
        const int2 *__restrict__ tn, const float4 *__restrict__ da, const float4 *__restrict__ h,
        const float4 *__restrict__ src, const float4 *__restrict__ z, float4 *__restrict__ p,
-       float4 *__restrict__ a, float4 *__restrict__ w, SysState *sys, double *partials, int mode)
+       float4 *__restrict__ a, float4 *__restrict__ w, float4 *__restrict__ x, SysState *sys,
+       double *partials, int mode)
 {
     pdl_wait();
     const int k = threadIdx.x % SP;
     const bool on = sys[k].status == kRun;
     const dfc be = from_d2(sys[k].beta);
+    // the previous iteration's x += alpha p (mode 1), on the p read here
+    // before it is overwritten; alpha is read before the last block
+    // replaces it
+    const bool xp = mode != 0 && sys[k].xp;
+    const dfc alp = from_d2(sys[k].alpha);
     acc awr, awi;
     const int rpb = kB / SP, stride = gridDim.x * rpb;
     // the compact G^T row of the next element is loaded one element ahead,
@@ -397,11 +403,12 @@ k_edge(int n, const int *__restrict__ tp, const int *__restrict__ tj, const floa
             j1 = __ldg(tp + e + 1);
         }
         const float4 srcv = src[idx], dav = __ldg(da + idx);
-        float4 pv = make_float4(0.f, 0.f, 0.f, 0.f), zv = pv, av = pv;
+        float4 pv = make_float4(0.f, 0.f, 0.f, 0.f), zv = pv, av = pv, xv = pv;
         if (mode != 0) {
             pv = p[idx];
             zv = z[idx];
             av = a[idx];
+            if (xp) xv = x[idx];
         }
         float4 hv0 = make_float4(0.f, 0.f, 0.f, 0.f), hv1 = hv0;
         float t0 = 0.f, t1 = 0.f;
@@ -430,6 +437,7 @@ k_edge(int n, const int *__restrict__ tp, const int *__restrict__ tj, const floa
         if (mode == 0) {
             an = from4(srcv);
         } else {
+            if (xp) x[idx] = to4(caxpy(from4(xv), alp, from4(pv)));
             p[idx] = to4(caxpy(from4(srcv), be, from4(pv)));
             an = caxpy(from4(zv), be, from4(av));
             a[idx] = to4(an);
@@ -472,12 +480,18 @@ k_edge(int n, const int *__restrict__ tp, const int *__restrict__ tj, const floa
     }
 }
 
-// x += alpha p, r -= alpha a, s -= alpha w; MRS weight from (s_m, r - s_m).
-// Every input of an element is loaded before anything is stored.
+// r -= alpha a, s -= alpha w, and the MRS smoothing of the residual
+// (MRS.cpp:85-153): first the previous iteration's step of s_m, deferred to
+// here where r and s_m are read anyway (mode 1: s_m = r, 2: s_m += w (r -
+// s_m), on the r of that iteration), then the sums for this iteration's
+// weight w = -(s_m, u) / ||u||^2, u = r - s_m, and for ||s_m|| after this
+// iteration's step: ||s_m + w u||^2 = ||s_m||^2 + 2 w (s_m, u) + w^2 ||u||^2,
+// or ||r||^2 (mode 1).  x += alpha p is left to the next k_edge (which reads
+// p) or the group update.  Every input of an element is loaded before
+// anything is stored.
 template <int SP>
 __global__ void __launch_bounds__(kB)
-k_update(int n, const float4 *__restrict__ p, const float4 *__restrict__ a,
-         const float4 *__restrict__ w, const float4 *__restrict__ sm, float4 *__restrict__ x,
+k_update(int n, const float4 *__restrict__ a, const float4 *__restrict__ w, float4 *__restrict__ sm,
          float4 *__restrict__ r, float4 *__restrict__ s, SysState *sys, double *partials)
 {
     pdl_wait();
@@ -485,106 +499,109 @@ k_update(int n, const float4 *__restrict__ p, const float4 *__restrict__ a,
     const bool on = sys[k].status == kRun;
     const dfc al = from_d2(sys[k].alpha);
     const dfc nal{neg(al.re), neg(al.im)};
-    acc su, uu;
+    const int pm = sys[k].mrs_mode;
+    const df pw = from_double(sys[k].mrs_w);
+    acc su, uu, nn, rr;
     const int rpb = kB / SP;
     const int stride = gridDim.x * rpb;
-    // two elements per pass, all 14 loads issued before any store
+    // two elements per pass, all 10 loads issued before any store
     for (int e = blockIdx.x * rpb + threadIdx.x / SP; e < n; e += 2 * stride) {
-        if (!on) continue;
+        if (!on) break;
         const bool two = e + stride < n;
-        float4 v[2][7];
+        float4 v[2][5];
 #pragma unroll
         for (int u = 0; u < 2; u++) {
             if (u == 1 && !two) break;
             const long long idx = (long long)(e + u * stride) * SP + k;
-            v[u][0] = __ldg(p + idx); v[u][1] = __ldg(a + idx); v[u][2] = __ldg(w + idx);
-            v[u][3] = __ldg(sm + idx); v[u][4] = x[idx]; v[u][5] = r[idx]; v[u][6] = s[idx];
+            v[u][0] = __ldg(a + idx); v[u][1] = __ldg(w + idx);
+            v[u][2] = sm[idx]; v[u][3] = r[idx]; v[u][4] = s[idx];
         }
 #pragma unroll
         for (int u = 0; u < 2; u++) {
             if (u == 1 && !two) break;
             const long long idx = (long long)(e + u * stride) * SP + k;
-            const dfc rn = caxpy(from4(v[u][5]), nal, from4(v[u][1]));
-            x[idx] = to4(caxpy(from4(v[u][4]), al, from4(v[u][0])));
+            const dfc ro = from4(v[u][3]);
+            dfc smv = from4(v[u][2]);
+            if (pm == 1) {
+                smv = ro;
+            } else if (pm == 2) {
+                acc tr, ti;
+                tr.h = smv.re.h; tr.l = smv.re.l;
+                ti.h = smv.im.h; ti.l = smv.im.l;
+                tr.mac(pw, add(ro.re, neg(smv.re)));
+                ti.mac(pw, add(ro.im, neg(smv.im)));
+                smv = dfc{tr.get(), ti.get()};
+            }
+            const dfc rn = caxpy(ro, nal, from4(v[u][0]));
             r[idx] = to4(rn);
-            s[idx] = to4(caxpy(from4(v[u][6]), nal, from4(v[u][2])));
-            const dfc smd = from4(v[u][3]);
-            const df ur = add(rn.re, neg(smd.re)), ui = add(rn.im, neg(smd.im));
-            su.mac(smd.re, ur); su.mac(smd.im, ui);
+            s[idx] = to4(caxpy(from4(v[u][4]), nal, from4(v[u][1])));
+            if (pm != 0) sm[idx] = to4(smv);
+            const df ur = add(rn.re, neg(smv.re)), ui = add(rn.im, neg(smv.im));
+            su.mac(smv.re, ur); su.mac(smv.im, ui);
             uu.mac(ur, ur); uu.mac(ui, ui);
+            nn.mac(smv.re, smv.re); nn.mac(smv.im, smv.im);
+            rr.mac(rn.re, rn.re); rr.mac(rn.im, rn.im);
         }
     }
-    double v[2] = {su.to_double(), uu.to_double()};
-    __shared__ double tot[2][32];
-    if (sys_grid_sum<SP, 2>(v, partials, &sys[0].ticket[2], tot) && threadIdx.x < SP) {
+    double v[4] = {su.to_double(), uu.to_double(), nn.to_double(), rr.to_double()};
+    __shared__ double tot[4][32];
+    if (sys_grid_sum<SP, 4>(v, partials, &sys[0].ticket[2], tot) && threadIdx.x < SP) {
         SysState &q = sys[threadIdx.x];
         if (q.status == kRun) {
             const double s_u = tot[0][threadIdx.x], u_u = tot[1][threadIdx.x];
+            const double n_n = tot[2][threadIdx.x], r_r = tot[3][threadIdx.x];
             const double wm = fabs(u_u) < 1e-100 ? 0.0 : -s_u / u_u;
-            if (wm < 0.0) q.mrs_mode = 0;
-            else if (wm > 1.0) q.mrs_mode = 1;
-            else {
+            if (wm < 0.0) {
+                q.mrs_mode = 0;
+                q.res_next = q.residual;
+            } else if (wm > 1.0) {
+                q.mrs_mode = 1;
+                q.res_next = r_r > 0.0 ? sqrt(r_r) : 0.0;
+            } else {
                 q.mrs_mode = 2;
                 q.mrs_w = wm;
+                const double m2 = n_n + 2.0 * wm * s_u + wm * wm * u_u;
+                q.res_next = m2 > 0.0 ? sqrt(m2) : 0.0;
             }
+            q.xp = 1;
         }
     }
 }
 
-// Per-row tail of the SpMV kernels: store z = A s, accumulate (z, s), update
-// the MRS-smoothed residual s_m and accumulate ||s_m||^2.
+// Per-row tail of the SpMV kernels: store z = A s and accumulate (z, s).
+// (The MRS smoothing of the residual runs in k_update.)
 struct SpmvTail {
-    acc zsr, zsi, nn;
-    int mm;
-    df wm;
-    __device__ __forceinline__ void row(long long i, dfc y, float4 sv4, const float4 *__restrict__ r,
-                                        float4 *__restrict__ z, float4 *__restrict__ sm)
+    acc zsr, zsi;
+    __device__ __forceinline__ void row(long long i, dfc y, float4 sv4, float4 *__restrict__ z)
     {
-        float4 rv4 = make_float4(0.f, 0.f, 0.f, 0.f), smo4 = rv4;
-        if (mm != 0) rv4 = __ldg(r + i);
-        if (mm == 2) smo4 = sm[i];
         z[i] = to4(y);
         const dfc sv = from4(sv4);
         zsr.mac(y.re, sv.re); zsr.mac(neg(y.im), sv.im);
         zsi.mac(y.re, sv.im); zsi.mac(y.im, sv.re);
-        if (mm != 0) {
-            dfc smv = from4(rv4);
-            if (mm == 2) {
-                const dfc old = from4(smo4);
-                acc tr, ti;
-                tr.h = old.re.h; tr.l = old.re.l;
-                ti.h = old.im.h; ti.l = old.im.l;
-                tr.mac(wm, add(smv.re, neg(old.re)));
-                ti.mac(wm, add(smv.im, neg(old.im)));
-                smv = dfc{tr.get(), ti.get()};
-            }
-            sm[i] = to4(smv);
-            nn.mac(smv.re, smv.re);
-            nn.mac(smv.im, smv.im);
-        }
     }
     // grid totals -> stop test and beta (the last block only)
     template <int SP, int NT = kB>
     __device__ __forceinline__ void finish(SysState *sys, double *partials, int mode)
     {
-        double v[3] = {zsr.to_double(), zsi.to_double(), nn.to_double()};
+        double v[2] = {zsr.to_double(), zsi.to_double()};
         finish_v<SP, NT>(v, sys, partials, mode);
     }
-    // the same from this thread's (z, s) re, im and ||s_m||^2 of system
-    // threadIdx.x % SP
+    // the same from this thread's (z, s) re, im of system threadIdx.x % SP.
+    // mode 1: the stop test on ||s_m|| of this iteration (k_update's
+    // res_next), then beta; mode 0 (set-up): (z, s) only
     template <int SP, int NT = kB>
-    static __device__ __forceinline__ void finish_v(double (&v)[3], SysState *sys,
+    static __device__ __forceinline__ void finish_v(double (&v)[2], SysState *sys,
                                                     double *partials, int mode)
     {
-        __shared__ double tot[3][32];
-        if (sys_grid_sum<SP, 3, NT>(v, partials, &sys[0].ticket[3], tot) && threadIdx.x < SP) {
+        __shared__ double tot[2][32];
+        if (sys_grid_sum<SP, 2, NT>(v, partials, &sys[0].ticket[3], tot) && threadIdx.x < SP) {
             SysState &q = sys[threadIdx.x];
             if (q.status == kRun) {
                 const double2 zs_new = make_double2(tot[0][threadIdx.x], tot[1][threadIdx.x]);
                 if (mode == 0) {
                     q.zs = zs_new;
                 } else {
-                    if (q.mrs_mode != 0) q.residual = sqrt(tot[2][threadIdx.x]);
+                    q.residual = q.res_next;
                     q.residual_rel = q.residual / q.r_old;
                     q.beta = cdiv(zs_new, q.zs);
                     q.zs = zs_new;
@@ -600,13 +617,13 @@ struct SpmvTail {
     }
 };
 
-// z = A s, MRS update of s_m, ||s_m||, (z, s) -> stop test and beta.
+// z = A s, (z, s) -> stop test and beta.
 // mode 0 (set-up): z = A s and (z, s) only.  x gathers straight from global
 // memory, CH slots in flight per thread.
 template <int SP, int CH>
 __global__ void __launch_bounds__(kB, 3)
 k_spmv(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict__ s,
-       const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
+       float4 *__restrict__ z,
        SysState *sys, double *partials, int mode)
 {
     pdl_wait();
@@ -614,14 +631,12 @@ k_spmv(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict
     const bool on = sys[k].status == kRun;
     const df om = d2f(omega[k]);
     SpmvTail tail;
-    tail.mm = mode ? sys[k].mrs_mode : 0;
-    tail.wm = from_double(sys[k].mrs_w);
     const int rpb = kB / SP;
     for (int row = blockIdx.x * rpb + threadIdx.x / SP; row < nb; row += gridDim.x * rpb) {
         if (!on) continue;
         const long long i = (long long)row * SP + k;
         const float4 sv4 = __ldg(s + i);
-        tail.row(i, spmv_row<SP, CH>(A, row, k, om, s), sv4, r, z, sm);
+        tail.row(i, spmv_row<SP, CH>(A, row, k, om, s), sv4, z);
     }
     tail.finish<SP>(sys, partials, mode);
 }
@@ -725,7 +740,7 @@ __device__ __forceinline__ void spmv_row_all(const Mat &A, int row, const df (&o
 template <int CH>
 __global__ void __launch_bounds__(kB, 2)
 k_spmv_r2(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restrict__ s,
-          const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
+          float4 *__restrict__ z,
           SysState *sys, double *partials, int mode)
 {
     pdl_wait();
@@ -737,8 +752,6 @@ k_spmv_r2(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restr
     for (int k = 0; k < SP; k++) {
         on[k] = sys[k].status == kRun;
         om[k] = d2f(omega[k]);
-        tail[k].mm = mode ? sys[k].mrs_mode : 0;
-        tail[k].wm = from_double(sys[k].mrs_w);
     }
     if (on[0] || on[1]) {
         for (int row = blockIdx.x * kB + threadIdx.x; row < nb; row += gridDim.x * kB) {
@@ -748,16 +761,16 @@ k_spmv_r2(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restr
             for (int k = 0; k < SP; k++) {
                 if (!on[k]) continue;
                 const long long i = (long long)row * SP + k;
-                tail[k].row(i, y[k], __ldg(s + i), r, z, sm);
+                tail[k].row(i, y[k], __ldg(s + i), z);
             }
         }
     }
     const bool odd = threadIdx.x & 1;
-    double v[3];
-    const double a0[3] = {tail[0].zsr.to_double(), tail[0].zsi.to_double(), tail[0].nn.to_double()};
-    const double a1[3] = {tail[1].zsr.to_double(), tail[1].zsi.to_double(), tail[1].nn.to_double()};
+    double v[2];
+    const double a0[2] = {tail[0].zsr.to_double(), tail[0].zsi.to_double()};
+    const double a1[2] = {tail[1].zsr.to_double(), tail[1].zsi.to_double()};
 #pragma unroll
-    for (int n = 0; n < 3; n++) {
+    for (int n = 0; n < 2; n++) {
         const double mine = odd ? a1[n] : a0[n], give = odd ? a0[n] : a1[n];
         v[n] = mine + __shfl_xor_sync(0xffffffffu, give, 1);
     }
@@ -1200,7 +1213,7 @@ __device__ __forceinline__ void mf_row2(const MF &M, Pos p, int k0, const df (&o
 template <int SP>
 __global__ void __launch_bounds__(kB, 2)
 k_mf_edges2(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restrict__ s,
-            const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
+            float4 *__restrict__ z,
             SysState *sys, double *partials, int mode)
 {
     pdl_wait();
@@ -1213,8 +1226,6 @@ k_mf_edges2(int nb, MF M, const float2 *__restrict__ omega, const float4 *__rest
     for (int u = 0; u < 2; u++) {
         on[u] = sys[k0 + u].status == kRun;
         om[u] = d2f(omega[k0 + u]);
-        tail[u].mm = mode ? sys[k0 + u].mrs_mode : 0;
-        tail[u].wm = from_double(sys[k0 + u].mrs_w);
     }
     const int rpb = kB / H, stride = gridDim.x * rpb;
     if (on[0] || on[1]) {
@@ -1242,25 +1253,24 @@ k_mf_edges2(int nb, MF M, const float2 *__restrict__ omega, const float4 *__rest
             }
 #pragma unroll
             for (int u = 0; u < 2; u++)
-                if (on[u]) tail[u].row(i + u, y[u], sv[u], r, z, sm);
+                if (on[u]) tail[u].row(i + u, y[u], sv[u], z);
         }
     }
     // per-system sums in a fixed order (run-to-run identical): every
     // thread's partials staged, then thread k < SP adds those of system k
     // over the block's threads in thread order
-    __shared__ double stage[3][2][kB];
+    __shared__ double stage[2][2][kB];
 #pragma unroll
     for (int u = 0; u < 2; u++) {
         stage[0][u][threadIdx.x] = tail[u].zsr.to_double();
         stage[1][u][threadIdx.x] = tail[u].zsi.to_double();
-        stage[2][u][threadIdx.x] = tail[u].nn.to_double();
     }
     __syncthreads();
-    double v[3] = {0.0, 0.0, 0.0};
+    double v[2] = {0.0, 0.0};
     if (threadIdx.x < SP) {
         const int kk = threadIdx.x, u = kk & 1, slot = kk >> 1;   // k0 = 2 (t % H) + u
         for (int t = slot; t < kB; t += H)
-            for (int n = 0; n < 3; n++) v[n] += stage[n][u][t];
+            for (int n = 0; n < 2; n++) v[n] += stage[n][u][t];
     }
     SpmvTail::finish_v<SP>(v, sys, partials, mode);
 }
@@ -1269,7 +1279,7 @@ k_mf_edges2(int nb, MF M, const float2 *__restrict__ omega, const float4 *__rest
 template <int SP>
 __global__ void __launch_bounds__(kB, 2)
 k_mf_edges(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restrict__ s,
-           const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
+           float4 *__restrict__ z,
            SysState *sys, double *partials, int mode)
 {
     pdl_wait();
@@ -1277,8 +1287,6 @@ k_mf_edges(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restr
     const bool on = sys[k].status == kRun;
     const df om = d2f(omega[k]);
     SpmvTail tail;
-    tail.mm = mode ? sys[k].mrs_mode : 0;
-    tail.wm = from_double(sys[k].mrs_w);
     const int rpb = kB / SP, stride = gridDim.x * rpb;
     // the next row's position is loaded one row ahead
     const int r0 = blockIdx.x * rpb + threadIdx.x / SP;
@@ -1301,7 +1309,7 @@ k_mf_edges(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restr
             y = mf_row<SP, 1>(M, p, k, om, s);
         else
             y = mf_row<SP, 2>(M, p, k, om, s);
-        tail.row(i, y, sv4, r, z, sm);
+        tail.row(i, y, sv4, z);
     }
     tail.finish<SP>(sys, partials, mode);
 }
@@ -1422,7 +1430,7 @@ __device__ __forceinline__ dfc mf_row_g(const MF &M, Pos p, int k, df om, const 
 template <int SP>
 __global__ void __launch_bounds__(kB)
 k_mf_edges_g(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restrict__ s,
-             const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
+             float4 *__restrict__ z,
              SysState *sys, double *partials, int mode)
 {
     pdl_wait();
@@ -1430,8 +1438,6 @@ k_mf_edges_g(int nb, MF M, const float2 *__restrict__ omega, const float4 *__res
     const bool on = sys[k].status == kRun;
     const df om = d2f(omega[k]);
     SpmvTail tail;
-    tail.mm = mode ? sys[k].mrs_mode : 0;
-    tail.wm = from_double(sys[k].mrs_w);
     const int rpb = kB / SP, stride = gridDim.x * rpb;
     // the next row's position is loaded one row ahead
     const int r0 = blockIdx.x * rpb + threadIdx.x / SP;
@@ -1454,7 +1460,7 @@ k_mf_edges_g(int nb, MF M, const float2 *__restrict__ omega, const float4 *__res
             y = mf_row_g<SP, 1>(M, p, k, om, s);
         else
             y = mf_row_g<SP, 2>(M, p, k, om, s);
-        tail.row(i, y, sv4, r, z, sm);
+        tail.row(i, y, sv4, z);
     }
     tail.finish<SP>(sys, partials, mode);
 }
@@ -1552,7 +1558,7 @@ struct TileCfg {
 template <int SP, bool MAT>
 __global__ void __launch_bounds__(TileCfg<SP>::NT)
 k_spmv_t(int nb, TileMat A, const float2 *__restrict__ omega, const float4 *__restrict__ s,
-         const float4 *__restrict__ r, float4 *__restrict__ z, float4 *__restrict__ sm,
+         float4 *__restrict__ z,
          SysState *sys, double *partials, int mode)
 {
     pdl_wait();
@@ -1561,8 +1567,6 @@ k_spmv_t(int nb, TileMat A, const float2 *__restrict__ omega, const float4 *__re
     const bool on = sys[k].status == kRun;
     const df om = d2f(omega[k]);
     SpmvTail tail;
-    tail.mm = mode ? sys[k].mrs_mode : 0;
-    tail.wm = from_double(sys[k].mrs_w);
     for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
         const int s0 = t * A.T, s1 = min(s0 + A.T, A.nslices);
         const long long c0 = A.pc[s0], nc = A.pc[s1] - c0, q0 = A.pr[s0], nr = A.pr[s1] - q0;
@@ -1633,7 +1637,7 @@ k_spmv_t(int nb, TileMat A, const float2 *__restrict__ omega, const float4 *__re
             kr_.mac(neg(om), mxi);
             ki_.mac(om, mxr);
             const long long i = (long long)row * SP + k;
-            tail.row(i, dfc{kr_.get(), ki_.get()}, __ldg(s + i), r, z, sm);
+            tail.row(i, dfc{kr_.get(), ki_.get()}, __ldg(s + i), z);
         }
     }
     tail.finish<SP, TileCfg<SP>::NT>(sys, partials, mode);
@@ -1805,17 +1809,33 @@ k_res64(int nb, Mat64 A, const double *__restrict__ omega64, const double2 *__re
     }
 }
 
-// xacc += x_df and x_df = 0 for the systems flagged in check (FP64 update)
+// xacc += x_df and x_df = 0 for the systems flagged in check (FP64 update),
+// x_df first completed by the x += alpha p still pending from the last
+// k_update (a system that stopped, or the graph's last iteration); the last
+// block clears the pending flags
 template <int SP>
-__global__ void k_fold(long long n, double2 *xacc, float4 *xdf, const int *__restrict__ check)
+__global__ void k_fold(long long n, double2 *xacc, float4 *xdf, const float4 *__restrict__ p,
+                       const int *__restrict__ check, SysState *sys)
 {
     pdl_wait();
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || !check[i % SP]) return;
-    const double2 a = xacc[i];
-    const float4 d = xdf[i];
-    xacc[i] = make_double2(a.x + ((double)d.x + (double)d.y), a.y + ((double)d.z + (double)d.w));
-    xdf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int k = (int)(i % SP);
+    if (i < n && check[k]) {
+        const double2 a = xacc[i];
+        dfc d = from4(xdf[i]);
+        if (sys[k].xp) d = caxpy(d, from_d2(sys[k].alpha), from4(p[i]));
+        xacc[i] = make_double2(a.x + ((double)d.re.h + (double)d.re.l),
+                               a.y + ((double)d.im.h + (double)d.im.l));
+        xdf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(&sys[0].ticket[4], 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    if (threadIdx.x < SP && check[threadIdx.x]) sys[threadIdx.x].xp = 0;
+    if (threadIdx.x == 0) sys[0].ticket[4] = 0u;
 }
 
 // system-major FP64 [S][nb] <-> row-major FP64 [nb][SP]
@@ -1999,14 +2019,14 @@ struct Impl {
         if (V.ch == kMatFree + 2) {
             const MfTileGrid G{V.mft[0], V.mft[1], V.mft[2], V.mft[3], V.mft[4], V.mft[5], V.mft[6]};
             k_mf_tile<SP><<<V.g_mft, MfTile<SP>::NT, MfTile<SP>::SMEM, V.st>>>(
-                mfd(V), G, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode);
+                mfd(V), G, V.omega, V.s, V.z, V.sys, V.partials, mode);
             return;
         }
         if (V.ch == kMatFree + 3) {
             const MF M = mfd(V);
             pdl(k_mf_faces<SP>, V.g_mff, kB, 0, V.st, M, V.s, V.sys);
             pdl(k_mf_gface<SP>, V.g_mfg, kB, 0, V.st, M, V.sys);
-            pdl(k_mf_edges_g<SP>, V.g_mfe3, kB, 0, V.st, V.nb, M, V.omega, V.s, V.r, V.z, V.sm, V.sys,
+            pdl(k_mf_edges_g<SP>, V.g_mfe3, kB, 0, V.st, V.nb, M, V.omega, V.s, V.z, V.sys,
                                                        V.partials, mode);
             return;
         }
@@ -2015,39 +2035,38 @@ struct Impl {
             pdl(k_mf_faces<SP>, V.g_mff, kB, 0, V.st, M, V.s, V.sys);
             if constexpr (SP >= 2) {
                 if (V.ch == kMatFree + 1) {
-                    pdl(k_mf_edges2<SP>, V.g_mfe, kB, 0, V.st, V.nb, M, V.omega, V.s, V.r, V.z,
-                                                              V.sm, V.sys, V.partials, mode);
+                    pdl(k_mf_edges2<SP>, V.g_mfe, kB, 0, V.st, V.nb, M, V.omega, V.s, V.z, V.sys, V.partials, mode);
                     return;
                 }
             }
-            pdl(k_mf_edges<SP>, V.g_mfe, kB, 0, V.st, V.nb, M, V.omega, V.s, V.r, V.z, V.sm, V.sys,
+            pdl(k_mf_edges<SP>, V.g_mfe, kB, 0, V.st, V.nb, M, V.omega, V.s, V.z, V.sys,
                                                     V.partials, mode);
             return;
         }
         if (V.ch == 0) {
             k_spmv_t<SP, true><<<V.g_spmv_t, TileCfg<SP>::NT, V.tile_smem, V.st>>>(
-                V.nb, tmat(V), V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode);
+                V.nb, tmat(V), V.omega, V.s, V.z, V.sys, V.partials, mode);
             return;
         }
         if (V.ch == 1) {
             k_spmv_t<SP, false><<<V.g_spmv_tx, TileCfg<SP>::NT, V.tile_smem_x, V.st>>>(
-                V.nb, tmat(V), V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode);
+                V.nb, tmat(V), V.omega, V.s, V.z, V.sys, V.partials, mode);
             return;
         }
         if constexpr (SP == 2) {
             if (V.ch == kRowVariant + 2) {
-                pdl(k_spmv_r2<2>, V.g_spmv, kB, 0, V.st, V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode);
+                pdl(k_spmv_r2<2>, V.g_spmv, kB, 0, V.st, V.nb, A, V.omega, V.s, V.z, V.sys, V.partials, mode);
                 return;
             }
             if (V.ch == kRowVariant + 4) {
-                pdl(k_spmv_r2<4>, V.g_spmv, kB, 0, V.st, V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode);
+                pdl(k_spmv_r2<4>, V.g_spmv, kB, 0, V.st, V.nb, A, V.omega, V.s, V.z, V.sys, V.partials, mode);
                 return;
             }
         }
         switch (V.ch) {
-        case 2: pdl(k_spmv<SP, 2>, V.g_spmv, kB, 0, V.st, V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode); break;
-        case 8: pdl(k_spmv<SP, 8>, V.g_spmv, kB, 0, V.st, V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode); break;
-        default: pdl(k_spmv<SP, 4>, V.g_spmv, kB, 0, V.st, V.nb, A, V.omega, V.s, V.r, V.z, V.sm, V.sys, V.partials, mode); break;
+        case 2: pdl(k_spmv<SP, 2>, V.g_spmv, kB, 0, V.st, V.nb, A, V.omega, V.s, V.z, V.sys, V.partials, mode); break;
+        case 8: pdl(k_spmv<SP, 8>, V.g_spmv, kB, 0, V.st, V.nb, A, V.omega, V.s, V.z, V.sys, V.partials, mode); break;
+        default: pdl(k_spmv<SP, 4>, V.g_spmv, kB, 0, V.st, V.nb, A, V.omega, V.s, V.z, V.sys, V.partials, mode); break;
         }
     }
     // iteration t of a sequence: the fused preconditioner alternates a's
@@ -2058,18 +2077,17 @@ struct Impl {
             float4 *ain = (t & 1) ? V.a2 : V.a, *aout = (t & 1) ? V.a : V.a2;
             const PrecGrid G{V.pt[0], V.pt[1], V.pt[2], V.pt[3], V.pt[4]};
             k_prec_tile<SP><<<V.g_pt, PrecTile<SP>::NT, PrecTile<SP>::SMEM, V.st>>>(
-                mfd(V), G, V.ds, V.da, V.s, V.z, ain, aout, V.p, V.w, V.sys, V.partials);
-            pdl(k_update<SP>, V.g_update, kB, 0, V.st, V.nb, V.p, aout, V.w, V.sm, V.x, V.r, V.s,
-                                                      V.sys, V.partials);
+                mfd(V), G, V.ds, V.da, V.s, V.z, ain, aout, V.p, V.w, V.x, V.sys, V.partials);
+            pdl(k_update<SP>, V.g_update, kB, 0, V.st, V.nb, aout, V.w, V.sm, V.r, V.s, V.sys,
+                V.partials);
             spmv(V, 1);
             return;
         }
         if (V.G.m > 0)
             node(V, V.z, V.a, 1);
         pdl(k_edge<SP>, V.g_edge, kB, 0, V.st, V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.G.d_tn, V.da, V.h, V.s, V.z,
-                                              V.p, V.a, V.w, V.sys, V.partials, 1);
-        pdl(k_update<SP>, V.g_update, kB, 0, V.st, V.nb, V.p, V.a, V.w, V.sm, V.x, V.r, V.s, V.sys,
-                                                  V.partials);
+                                              V.p, V.a, V.w, V.x, V.sys, V.partials, 1);
+        pdl(k_update<SP>, V.g_update, kB, 0, V.st, V.nb, V.a, V.w, V.sm, V.r, V.s, V.sys, V.partials);
         spmv(V, 1);
     }
     // one preconditioner step of the iteration (mode 1), unfused or fused
@@ -2078,13 +2096,13 @@ struct Impl {
         if (fused) {
             const PrecGrid G{V.pt[0], V.pt[1], V.pt[2], V.pt[3], V.pt[4]};
             k_prec_tile<SP><<<V.g_pt, PrecTile<SP>::NT, PrecTile<SP>::SMEM, V.st>>>(
-                mfd(V), G, V.ds, V.da, V.s, V.z, ain, aout, V.p, V.w, V.sys, V.partials);
+                mfd(V), G, V.ds, V.da, V.s, V.z, ain, aout, V.p, V.w, V.x, V.sys, V.partials);
             return;
         }
         if (V.G.m > 0)
             node(V, V.z, ain, 1);
         pdl(k_edge<SP>, V.g_edge, kB, 0, V.st, V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.G.d_tn, V.da, V.h,
-                                              V.s, V.z, V.p, ain, V.w, V.sys, V.partials, 1);
+                                              V.s, V.z, V.p, ain, V.w, V.x, V.sys, V.partials, 1);
     }
     static void prec_grid(Survey &V, int nsm)
     {
@@ -2124,7 +2142,7 @@ struct Impl {
         if (V.G.m > 0)
             node(V, V.r, V.a, 0);
         k_edge<SP><<<V.g_edge, kB, 0, V.st>>>(V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.G.d_tn, V.da, V.h, V.r, V.z,
-                                              V.p, V.a, V.s, V.sys, V.partials, 0);
+                                              V.p, V.a, V.s, V.x, V.sys, V.partials, 0);
         cudaMemsetAsync(V.p, 0, sizeof(float4) * (size_t)V.nb * SP, V.st);
         cudaMemsetAsync(V.a, 0, sizeof(float4) * (size_t)V.nb * SP, V.st);
         spmv(V, 0);
@@ -2141,7 +2159,7 @@ struct Impl {
     static void fold(Survey &V, const int *check)
     {
         const long long n = (long long)V.nb * SP;
-        pdl(k_fold<SP>, (unsigned)((n + kB - 1) / kB), kB, 0, V.st, n, V.xacc, V.x, check);
+        pdl(k_fold<SP>, (unsigned)((n + kB - 1) / kB), kB, 0, V.st, n, V.xacc, V.x, V.p, check, V.sys);
     }
     static void spmv_only(Survey &V) { spmv(V, 0); }
 
@@ -2863,7 +2881,7 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
         (rc = dev_alloc(&V.z, nv)) || (rc = dev_alloc(&V.w, nv)) || (rc = dev_alloc(&V.sm, nv)) ||
         (rc = dev_alloc(&V.h, (size_t)mm * V.SP)) || (rc = dev_alloc(&V.b64, nv)) ||
         (rc = dev_alloc(&V.xacc, nv)) || (rc = dev_alloc(&V.all_on, 32)) ||
-        (rc = dev_alloc(&V.partials, (size_t)3 * std::max(gmax, nsm * 32) * V.SP)))
+        (rc = dev_alloc(&V.partials, (size_t)4 * std::max(gmax, nsm * 32) * V.SP)))
         return rc;
     V.pblocks = std::max(gmax, nsm * 32);
     MTGPU_TRY(cudaMallocHost((void **)&V.hsys, sizeof(SysState) * 32));
@@ -3057,10 +3075,10 @@ int survey_set_variant(Survey &V, int variant)
     return MTGPU_OK;
 }
 
-// Times the SpMV as the iteration launches it: mode 1 with the MRS tail
-// (r read, s_m read and written), every system running.  The state set here
-// (no stop threshold, no iteration limit) keeps all systems running across
-// the launches; a solve re-initialises the state and the vectors it touches.
+// Times the SpMV as the iteration launches it: mode 1 (z = A s, (z, s), the
+// stop test and beta), every system running.  The state set here (no stop
+// threshold, no iteration limit) keeps all systems running across the
+// launches; a solve re-initialises the state and the vectors it touches.
 int survey_spmv_timed(Survey &V, int reps, float *ms)
 {
     std::vector<SysState> init(32);
@@ -3077,8 +3095,6 @@ int survey_spmv_timed(Survey &V, int reps, float *ms)
     MTGPU_TRY(cudaMemcpyAsync(V.sys, init.data(), sizeof(SysState) * 32, cudaMemcpyHostToDevice, V.st));
     const size_t nv = sizeof(float4) * (size_t)V.nb * V.SP;
     MTGPU_TRY(cudaMemsetAsync(V.s, 0, nv, V.st));
-    MTGPU_TRY(cudaMemsetAsync(V.r, 0, nv, V.st));
-    MTGPU_TRY(cudaMemsetAsync(V.sm, 0, nv, V.st));
     cudaEvent_t e0, e1;
     MTGPU_TRY(cudaEventCreate(&e0));
     MTGPU_TRY(cudaEventCreate(&e1));

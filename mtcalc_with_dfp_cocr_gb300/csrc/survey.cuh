@@ -15,12 +15,14 @@ struct SysState {
     double eps_k;          // the inner stop threshold on residual_rel
     double bnorm;          // ||b|| of the system (FP64)
     double rnorm;          // ||b - A x|| of the last FP64 residual evaluation
-    int mrs_mode;          // 0 keep s_m, 1 s_m = r, 2 s_m += w (r - s_m)
+    double res_next;       // ||s_m|| after this iteration's MRS step (k_update), for the stop test
+    int mrs_mode;          // 0 keep s_m, 1 s_m = r, 2 s_m += w (r - s_m): the step the next k_update applies
+    int xp;                // x still lacks alpha p of the last k_update (the next k_edge or the fold adds it)
     int status;            // 1 running, else MTGPU_OK / MTGPU_DIV_BY_ZERO / MTGPU_MAXITER / MTGPU_X0_NULL
     int iter;              // the reference's iteration counter
     int checks;            // true-residual verifications
     int maxiter;
-    unsigned int ticket[4];  // block-completion counters (system 0 only)
+    unsigned int ticket[6];  // block-completion counters (system 0 only)
 };
 
 constexpr int kRowVariant = 16;    // + slots in flight: one thread per row, both systems
