@@ -98,6 +98,81 @@ int validate_lower(int nb, const int *ig, const int *jg, const int *idi, const i
     return MTGPU_OK;
 }
 
+// The sizes and offsets a host upload of the lower-triangle SLAE relies
+// on: the rest (every row's offsets, columns and block sizes) is checked on
+// the device after the upload (check_lower_device), not in host loops over
+// the whole matrix.
+int validate_lower_sizes(int nb, const int *ig, const int *jg, const int *idi, const int *ijg)
+{
+    MTGPU_CHECK_ARG(nb > 0, "n must be a positive even number");
+    MTGPU_CHECK_ARG(ig && jg && idi && ijg, "null SLAE pointer");
+    MTGPU_CHECK_ARG(ig[0] == 0 && idi[0] == 0, "ig/idi must be 0-based offsets");
+    const long long nnz = ig[nb];
+    MTGPU_CHECK_ARG(nnz >= 0 && nnz <= (long long)nb * (nb - 1) / 2, "ig is not monotone");
+    MTGPU_CHECK_ARG(idi[nb] >= nb && idi[nb] <= 2LL * nb, "diagonal block size must be 1 or 2");
+    MTGPU_CHECK_ARG(ijg[0] == 0 && ijg[nnz] >= nnz && ijg[nnz] <= 2 * nnz,
+                    "off-diagonal block size must be 1 or 2");
+    return MTGPU_OK;
+}
+
+__global__ void k_check_lower(int nb, int nnz, const int *__restrict__ ig, const int *__restrict__ jg,
+                              const int *__restrict__ idi, const int *__restrict__ ijg, int *bad)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    int b = 0;
+    const int q0 = ig[i], q1 = ig[i + 1];
+    if (q1 < q0 || q0 < 0 || q1 > nnz) b |= 1;
+    const int ds = idi[i + 1] - idi[i];
+    if (ds != 1 && ds != 2) b |= 2;
+    if (!(b & 1))
+        for (int q = q0; q < q1; q++) {
+            const int c = jg[q];
+            if (c < 0 || c >= i) b |= 4;
+            const int sz = ijg[q + 1] - ijg[q];
+            if (sz != 1 && sz != 2) b |= 8;
+        }
+    if (b) atomicOr(bad, b);
+}
+
+// every row of the uploaded lower-triangle SLAE: the checks of
+// validate_lower, with its messages
+int check_lower_device(int nb, int nnz, const LowerDev &L, cudaStream_t st)
+{
+    int *d_bad = nullptr, bad = 0;
+    int rc = dev_alloc(&d_bad, 1);
+    if (rc) return rc;
+    cudaError_t e = cudaMemsetAsync(d_bad, 0, sizeof(int), st);
+    if (e == cudaSuccess) {
+        k_check_lower<<<ceil_div(nb, kThreads), kThreads, 0, st>>>(nb, nnz, L.ig, L.jg, L.idi, L.ijg,
+                                                                  d_bad);
+        note_launches(1);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    dev_free(d_bad);
+    if (e != cudaSuccess) {
+        set_last_error(e, "SLAE check", __FILE__, __LINE__);
+        return MTGPU_ERR_CUDA;
+    }
+    MTGPU_CHECK_ARG(!(bad & 1), "ig is not monotone");
+    MTGPU_CHECK_ARG(!(bad & 2), "diagonal block size must be 1 or 2");
+    MTGPU_CHECK_ARG(!(bad & 4), "jg must hold lower-triangle columns");
+    MTGPU_CHECK_ARG(!(bad & 8), "off-diagonal block size must be 1 or 2");
+    return MTGPU_OK;
+}
+
+// The mesh description's pointers and sizes; its tables' entries are
+// checked on the device when they are uploaded (DevMeshUpload::upload)
+int validate_mesh_sizes(const mtgpu_mesh_desc &m)
+{
+    MTGPU_CHECK_ARG(m.kpar >= 0 && m.n_edges_c > 0 && m.n_nodes_c > 0, "bad mesh sizes");
+    MTGPU_CHECK_ARG(m.nvkat && m.nver14 && m.sigma3d && m.edges2 && m.is_node_bound,
+                    "null mesh pointer");
+    return MTGPU_OK;
+}
+
 int validate_mesh(const mtgpu_mesh_desc &m)
 {
     MTGPU_CHECK_ARG(m.kpar >= 0 && m.n_edges_c > 0 && m.n_nodes_c > 0, "bad mesh sizes");
@@ -162,11 +237,11 @@ int solve_double_float_host(int nb, const int *ig, const int *jg, const int *idi
                      mtgpu_solve_stats *stats)
 {
     const double t0 = now_seconds();
-    int rc = validate_lower(nb, ig, jg, idi, ijg);
+    int rc = validate_lower_sizes(nb, ig, jg, idi, ijg);
     if (rc) return rc;
     mtgpu_mesh_desc mesh{kpar, nb, n_nodes_c, nvkat, nver14, sigma3d, edges2, ig_t, jg_t,
                          gg_t, is_node_bound, 14};
-    if ((rc = validate_mesh(mesh))) return rc;
+    if ((rc = validate_mesh_sizes(mesh))) return rc;
     cudaStream_t st;
     MTGPU_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     PhaseTrace trace(st, "drop-in");
@@ -178,10 +253,11 @@ int solve_double_float_host(int nb, const int *ig, const int *jg, const int *idi
     mtgpu_survey_stats ss{};
     {
         LowerDev L;
-        if (!(rc = upload_lower(nb, ig, jg, idi, ijg, di, gg, L, st)))
+        if (!(rc = upload_lower(nb, ig, jg, idi, ijg, di, gg, L, st)) &&
+            !(rc = check_lower_device(nb, ig[nb], L, st)))
             rc = sell_from_block2x2_device(nb, L.ig, L.jg, L.idi, L.ijg, L.di, L.gg, ig[nb], A, st);
         note_launches(5);
-        trace.mark("SLAE upload, SELL");
+        trace.mark("SLAE upload, check, SELL");
     }
     const double one = 1.0;
     if (!rc) rc = param_from_sell(A, P, st);

@@ -192,6 +192,24 @@ __global__ void k_int_to_flag(int n, const int *__restrict__ in, unsigned char *
     if (i < n) out[i] = in[i] != 0;
 }
 
+// entries of an uploaded mesh description: bad[0] negative edge nodes,
+// bad[1] edge nodes beyond nn (T-matrix nodes), bad[2] negative cell nodes
+__global__ void k_check_mesh(int ne, int nn, const int *__restrict__ edges, int kpar,
+                             const int *__restrict__ nver, int stride, int *bad)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ne) {
+        const int a = edges[2 * i], b = edges[2 * i + 1];
+        if (a < 0 || b < 0) atomicAdd(&bad[0], 1);
+        if (a >= nn || b >= nn) atomicAdd(&bad[1], 1);
+    }
+    if (i < kpar) {
+        int neg = 0;
+        for (int j = 0; j < 8; j++) neg |= nver[(size_t)i * stride + j] < 0;
+        if (neg) atomicAdd(&bad[2], 1);
+    }
+}
+
 }  // namespace
 
 int folded_build_g_device(const DevMesh &dm, Folded &P, cudaStream_t st, bool *conforming)
@@ -291,18 +309,30 @@ int DevMeshUpload::upload(const mtgpu_mesh_desc &m, const double *xyz_host, cuda
     up(sigflag, m.sigma3d, sizeof(double) * (size_t)nmat);
     up(bound_i, m.is_node_bound, sizeof(int) * (size_t)m.n_nodes_c);
     if (xyz_host) up(xyz, xyz_host, sizeof(double) * (size_t)m.n_nodes_c * 3);
+    // the entries the host validation of a mesh description checks
+    int *d_bad = nullptr, bad[3] = {0, 0, 0};
+    if (e == cudaSuccess) e = cudaMalloc((void **)&d_bad, sizeof(int) * 3);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(int) * 3, st);
     if (e == cudaSuccess) {
         k_int_to_flag<<<ceil_div(m.n_nodes_c, kThreads), kThreads, 0, st>>>(m.n_nodes_c, bound_i, bnode);
-        note_launches(1);
+        k_check_mesh<<<ceil_div(std::max(m.n_edges_c, m.kpar), kThreads), kThreads, 0, st>>>(
+            m.n_edges_c, m.n_nodes_c, edges, m.kpar, nver, m.nver_stride, d_bad);
+        note_launches(2);
         e = cudaGetLastError();
     }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(bad, d_bad, sizeof(bad), cudaMemcpyDeviceToHost, st);
     // the host arrays are the caller's: the copies must end before it returns
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     dev_free(bound_i);
+    dev_free(d_bad);
     if (e != cudaSuccess) {
         set_last_error(e, "mesh upload", __FILE__, __LINE__);
         return MTGPU_ERR_CUDA;
     }
+    MTGPU_CHECK_ARG(bad[0] == 0, "negative node in edges");
+    MTGPU_CHECK_ARG(bad[1] == 0 || (m.ig_t && m.jg_t && m.gg_t),
+                    "edge node beyond n_nodes_c without T-matrix");
+    MTGPU_CHECK_ARG(bad[2] == 0, "bad nver");
     view.kpar = m.kpar;
     view.nb = m.n_edges_c;
     view.nn = m.n_nodes_c;

@@ -192,3 +192,39 @@ def test_dropin_double_float(gpu):
     earth = 0.5 * (xyz[e[:, 0], 2] + xyz[e[:, 1], 2]) <= 0.0
     c, c64 = x[0::2] + 1j * x[1::2], x64[0::2] + 1j * x64[1::2]
     assert np.linalg.norm((c - c64)[earth]) <= 1e-7 * np.linalg.norm(c64[earth])
+
+
+def test_dropin_double_float_rejects_bad_input(gpu):
+    """The double-float entry point checks every row of the uploaded SLAE and
+    every entry of the uploaded mesh tables on the device, with the codes and
+    messages of the host validation of the FP64 path: a column outside the
+    lower triangle, an off-diagonal block size of 3, a negative edge node and
+    a negative cell node are each MTGPU_ERR_ARG, and a good input still
+    solves afterwards."""
+    import copy
+    w, s, mesh = _c1_system(1)
+    row = s.nb // 2
+    q = int(s.ig[row])
+    cases = []
+    b = copy.deepcopy(s)
+    b.jg = s.jg.copy()
+    b.jg[q] = row                                 # not below the diagonal
+    cases.append((b, mesh, "lower-triangle"))
+    b = copy.deepcopy(s)
+    b.ijg = s.ijg.copy()
+    b.ijg[q + 1:] += 2                            # block q spans 3 values
+    b.gg = np.concatenate([s.gg, np.zeros(2)])
+    cases.append((b, mesh, "block size"))
+    m = copy.deepcopy(mesh)
+    m.edges = mesh.edges.copy()
+    m.edges[3, 1] = -1
+    cases.append((s, m, "negative node"))
+    m = copy.deepcopy(mesh)
+    m.nver = mesh.nver.copy()
+    m.nver[3, 2] = -5
+    cases.append((s, m, "nver"))
+    for slae, msh, words in cases:
+        with pytest.raises(RuntimeError, match=words):
+            solver.pcocr_2x2_folded(slae, msh, double_float=True, stop_on_true_residual=True)
+    code, x, st = solver.pcocr_2x2_folded(s, mesh, double_float=True, stop_on_true_residual=True)
+    assert code == 0 and st.true_residual_rel < 1e-8
