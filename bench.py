@@ -54,10 +54,15 @@ sys.path.insert(0, ROOT)
 METRIC = "time/solve to rel-res 1e-8: batched mixed vs plain FP64 GPU; SpMV HBM GB/s"
 UNIT = "s/solve"
 WORKLOAD = "c2"
-# DRAM bytes of one matrix-free SpMV on c2 (two lanes, with the MRS tail as
-# the iteration launches it), per variant: the sum of its kernels' ncu
-# dram__bytes_read.sum + dram__bytes_write.sum (profiles/bench_c2_launch_list.md)
-SPMV_MF_TRAFFIC_C2 = {32: 438.2e6, 35: 512.3e6}
+# DRAM bytes of one matrix-free SpMV on c2 (two lanes, as the iteration
+# launches it), per variant: the sum of its kernels' ncu dram__bytes_read.sum
+# + dram__bytes_write.sum (profiles/bench_c2_launch_list.md,
+# profiles/spmv_matfree_c2_s2.md)
+SPMV_MF_TRAFFIC_C2 = {32: 306.3e6, 35: 379.7e6}
+# what bounds the matrix-free SpMV instead of HBM (ncu on c2, two lanes)
+SPMV_MF_BINDING = ("FP32 issue: k_mf_edges<2> 69 % issue-active, 51 % FMA pipe, 42 double-float "
+                   "multiply-adds of 12 FP32 instructions per edge and system "
+                   "(profiles/spmv_matfree_c2_s2.md)")
 
 
 def load_peaks():
@@ -288,9 +293,9 @@ def gpu_arm(args):
     meta = nslices * (8 + 8 + 4 + 4)
     SP = 1 << (S - 1).bit_length()
     m_ = w.mesh
-    # as the iteration launches it: z = A s plus the MRS tail (r read, s_m
-    # read and written)
-    tail = 3 * 16 * SP * nb
+    # as the iteration launches it: z = A s and (z, s) (the MRS smoothing
+    # runs in k_update)
+    tail = 0
     if variant in (32, 33, 35):
         # matrix-free, per launch as the iteration runs it: the faces kernel
         # reads s and writes the face circulations f; variants 32/33: the
@@ -304,18 +309,17 @@ def gpu_arm(args):
         if variant == 35:
             spmv_bytes = 16 * SP * (3 * nb + 4 * nf) + 48 * m_.kpar + 4 * nb + tail
             spmv_kernel = ("k_mf_faces + k_mf_gface + k_mf_edges_g (matrix-free double-float "
-                           "SpMV, face mass applied per face, + MRS tail, S systems)")
+                           "SpMV, face mass applied per face, S systems)")
         else:
             spmv_bytes = 16 * SP * (3 * nb + 2 * nf) + 48 * m_.kpar + 4 * nb + tail
             edges = "k_mf_edges2" if variant == 33 else "k_mf_edges"
-            spmv_kernel = f"k_mf_faces + {edges} (matrix-free double-float SpMV + MRS tail, S systems)"
+            spmv_kernel = f"k_mf_faces + {edges} (matrix-free double-float SpMV, S systems)"
         traffic = SPMV_MF_TRAFFIC_C2.get(variant) if WORKLOAD == "c2" else None
         traffic_src = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of the variant-{variant} "
                        f"kernels on c2 (profiles/bench_c2_launch_list.md)") if traffic else None
     else:
         spmv_bytes = nc * (4 + 8 + 8) + nr * (4 + 8) + meta + 2 * S * 16 * nb + tail
-        spmv_kernel = (f"k_spmv variant {variant} (batched double-float SELL-32 SpMV + MRS "
-                       f"tail, S systems)")
+        spmv_kernel = f"k_spmv variant {variant} (batched double-float SELL-32 SpMV, S systems)"
         traffic = None
         traffic_src = None
     achieved = spmv_bytes / (spmv_ms * 1e-3) / 1e9
@@ -389,7 +393,8 @@ def gpu_arm(args):
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": f"{peak_kind} hbm_gbs",
                      "bytes_per_launch": spmv_bytes, "ms_per_launch": spmv_ms,
-                     "traffic": traffic, "traffic_source": traffic_src},
+                     "traffic": traffic, "traffic_source": traffic_src,
+                     "binding": SPMV_MF_BINDING if variant in (32, 33, 35) else None},
         "roofline_fp64_spmv": {"bound": "fp64 pipe (GB300 FP64 = FP32/64)",
                                "achieved": achieved64, "peak": peak, "unit": "GB/s",
                                "frac": achieved64 / peak, "bytes_per_launch": spmv64_bytes,
