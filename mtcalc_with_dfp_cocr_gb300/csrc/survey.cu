@@ -934,6 +934,32 @@ __global__ void k_g_lattice_check(MF M, int m, const int *__restrict__ gp, const
     if (nbad) atomicAdd(bad, 1);
 }
 
+// face t (faces numbered by normal, then z, y, x) -> normal n and position;
+// 32-bit (the set-up keeps faces x systems below 2^31)
+__device__ __forceinline__ void mf_face_pos(const MF &M, int t, int &n, int &i, int &j, int &kk)
+{
+    const int fx = (int)M.nfx, fy = (int)M.nfy;
+    int q = t, a, b;
+    if (q < fx) {
+        n = 0;
+        a = M.nx;
+        b = M.ny - 1;
+    } else if ((q -= fx) < fy) {
+        n = 1;
+        a = M.nx - 1;
+        b = M.ny;
+    } else {
+        q -= fy;
+        n = 2;
+        a = M.nx - 1;
+        b = M.ny - 1;
+    }
+    const int r = q / a;
+    i = q - r * a;
+    kk = r / b;
+    j = r - kk * b;
+}
+
 // the circulation of system k's x around face (n, i, j, kk)
 template <int SP>
 __device__ __forceinline__ dfc mf_face_f(const MF &M, const float4 *__restrict__ x, int n, int i,
@@ -971,32 +997,11 @@ k_mf_faces(MF M, const float4 *__restrict__ x, const SysState *sys)
     pdl_wait();
     const int k = threadIdx.x % SP;
     if (sys[k].status != kRun) return;
-    const long long nf = M.nfx + M.nfy + M.nfz;
+    const int nf = (int)(M.nfx + M.nfy + M.nfz);
     const int rpb = kB / SP;
-    for (long long t = (long long)blockIdx.x * rpb + threadIdx.x / SP; t < nf;
-         t += (long long)gridDim.x * rpb) {
-        long long q = t;
+    for (int t = blockIdx.x * rpb + threadIdx.x / SP; t < nf; t += gridDim.x * rpb) {
         int n, i, j, kk;
-        if (q < M.nfx) {
-            n = 0;
-            i = (int)(q % M.nx);
-            q /= M.nx;
-            j = (int)(q % (M.ny - 1));
-            kk = (int)(q / (M.ny - 1));
-        } else if ((q -= M.nfx) < M.nfy) {
-            n = 1;
-            i = (int)(q % (M.nx - 1));
-            q /= (M.nx - 1);
-            j = (int)(q % M.ny);
-            kk = (int)(q / M.ny);
-        } else {
-            q -= M.nfy;
-            n = 2;
-            i = (int)(q % (M.nx - 1));
-            q /= (M.nx - 1);
-            j = (int)(q % (M.ny - 1));
-            kk = (int)(q / (M.ny - 1));
-        }
+        mf_face_pos(M, t, n, i, j, kk);
         M.f[t * SP + k] = to4(mf_face_f<SP>(M, x, n, i, j, kk, k));
     }
 }
@@ -1336,30 +1341,9 @@ k_mf_gface(MF M, const SysState *sys)
     const int nc = (int)M.ncell;
     auto cell = [&](int x, int y, int z) { return (z * (M.ny - 1) + y) * (M.nx - 1) + x; };
     const int rpb = kB / SP;
-    for (long long t = (long long)blockIdx.x * rpb + threadIdx.x / SP; t < nf;
-         t += (long long)gridDim.x * rpb) {
-        long long q = t;
+    for (int t = blockIdx.x * rpb + threadIdx.x / SP; t < nf; t += gridDim.x * rpb) {
         int n, i, j, kk;
-        if (q < M.nfx) {
-            n = 0;
-            i = (int)(q % M.nx);
-            q /= M.nx;
-            j = (int)(q % (M.ny - 1));
-            kk = (int)(q / (M.ny - 1));
-        } else if ((q -= M.nfx) < M.nfy) {
-            n = 1;
-            i = (int)(q % (M.nx - 1));
-            q /= (M.nx - 1);
-            j = (int)(q % M.ny);
-            kk = (int)(q / M.ny);
-        } else {
-            q -= M.nfy;
-            n = 2;
-            i = (int)(q % (M.nx - 1));
-            q /= (M.nx - 1);
-            j = (int)(q % (M.ny - 1));
-            kk = (int)(q / (M.ny - 1));
-        }
+        mf_face_pos(M, t, n, i, j, kk);
         const int pos = n == 0 ? i : (n == 1 ? j : kk);
         const int last = (n == 0 ? M.nx : (n == 1 ? M.ny : M.nz)) - 1;
         float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1921,44 +1905,69 @@ __global__ void k_diag_s(int m, int SP, const double *gkg, const double *gmg,
 }
 
 // diag(G K G^T) and diag(G M G^T), FP64, in the reference's summation order
-// (row k of A by increasing column, unfused multiply-add; see folded.cu)
-__global__ void k_gdiag(int m, const int *gp, const int *gj, const double *gv, const int *nc_row,
-                        const int *nr_row, const long long *pc, const long long *pr,
-                        const int *col_c, const double *kc, const double *mc, const int *col_r,
-                        const double *kr, double *gkg, double *gmg)
+// (row k of A by increasing column, unfused multiply-add; see folded.cu),
+// in two passes: one thread per G entry j = (v, k) forms t_j = sum over row
+// k of A of A[k][c] G[v][c]; then one thread per node v adds t_j G[v][k]
+// over its entries in G's order — the sums and their order of the single
+// pass, without its per-node serial chain
+__global__ void k_gdiag_entry(int m, const int *__restrict__ gp, const int *__restrict__ gj,
+                              const double *__restrict__ gv, const int *__restrict__ rowof,
+                              const int *__restrict__ nc_row, const int *__restrict__ nr_row,
+                              const long long *__restrict__ pc, const long long *__restrict__ pr,
+                              const int *__restrict__ col_c, const double *__restrict__ kc,
+                              const double *__restrict__ mc, const int *__restrict__ col_r,
+                              const double *__restrict__ kr, double *tkv, double *tmv)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= gp[m]) return;
+    const int v = rowof[j];
+    const int b0 = gp[v], e0 = gp[v + 1];
+    const int k = gj[j];
+    const int nc = nc_row[k], nr = nr_row[k];
+    double tk = 0.0, tm = 0.0;
+    int qc = 0, qr = 0;
+    while (qc < nc || qr < nr) {
+        const int cc = qc < nc ? col_c[slot(pc, k, qc)] : 0x7fffffff;
+        const int cr = qr < nr ? col_r[slot(pr, k, qr)] : 0x7fffffff;
+        double kv, mv;
+        int c;
+        if (cc < cr) {
+            const long long t = slot(pc, k, qc++);
+            kv = kc[t];
+            mv = mc[t];
+            c = cc;
+        } else {
+            kv = kr[slot(pr, k, qr++)];
+            mv = 0.0;
+            c = cr;
+        }
+        for (int u = b0; u < e0; u++)
+            if (gj[u] == c) {
+                tk = __dadd_rn(tk, __dmul_rn(kv, gv[u]));
+                tm = __dadd_rn(tm, __dmul_rn(mv, gv[u]));
+            }
+    }
+    tkv[j] = tk;
+    tmv[j] = tm;
+}
+
+__global__ void k_gdiag_rows(int m, const int *__restrict__ gp, int *rowof)
 {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= m) return;
-    const int b0 = gp[v], e0 = gp[v + 1];
+    for (int j = gp[v]; j < gp[v + 1]; j++) rowof[j] = v;
+}
+
+__global__ void k_gdiag(int m, const int *__restrict__ gp, const double *__restrict__ gv,
+                        const double *__restrict__ tkv, const double *__restrict__ tmv,
+                        double *gkg, double *gmg)
+{
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= m) return;
     double sk = 0.0, sm = 0.0;
-    for (int j = b0; j < e0; j++) {
-        const int k = gj[j];
-        const int nc = nc_row[k], nr = nr_row[k];
-        double tk = 0.0, tm = 0.0;
-        int qc = 0, qr = 0;
-        while (qc < nc || qr < nr) {
-            const int cc = qc < nc ? col_c[slot(pc, k, qc)] : 0x7fffffff;
-            const int cr = qr < nr ? col_r[slot(pr, k, qr)] : 0x7fffffff;
-            double kv, mv;
-            int c;
-            if (cc < cr) {
-                const long long t = slot(pc, k, qc++);
-                kv = kc[t];
-                mv = mc[t];
-                c = cc;
-            } else {
-                kv = kr[slot(pr, k, qr++)];
-                mv = 0.0;
-                c = cr;
-            }
-            for (int u = b0; u < e0; u++)
-                if (gj[u] == c) {
-                    tk = __dadd_rn(tk, __dmul_rn(kv, gv[u]));
-                    tm = __dadd_rn(tm, __dmul_rn(mv, gv[u]));
-                }
-        }
-        sk = __dadd_rn(sk, __dmul_rn(tk, gv[j]));
-        sm = __dadd_rn(sm, __dmul_rn(tm, gv[j]));
+    for (int j = gp[v]; j < gp[v + 1]; j++) {
+        sk = __dadd_rn(sk, __dmul_rn(tkv[j], gv[j]));
+        sm = __dadd_rn(sm, __dmul_rn(tmv[j], gv[j]));
     }
     gkg[v] = sk;
     gmg[v] = sm;
@@ -2885,6 +2894,7 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
         return rc;
     V.pblocks = std::max(gmax, nsm * 32);
     MTGPU_TRY(cudaMallocHost((void **)&V.hsys, sizeof(SysState) * 32));
+    trace.mark("allocations");
     {
         const std::vector<int> ones(32, 1);
         MTGPU_TRY(cudaMemcpyAsync(V.all_on, ones.data(), sizeof(int) * 32, cudaMemcpyHostToDevice, st));
@@ -2903,6 +2913,7 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
     k_to_df<<<(unsigned)((P.len_r + kB - 1) / kB), kB, 0, st>>>(P.len_r, P.d_kr, V.kr);
     k_diag_a<<<(unsigned)((nv + kB - 1) / kB), kB, 0, st>>>(V.nb, V.SP, P.d_nc, P.d_pc, P.d_col_c,
                                                           P.d_kc, P.d_mc, V.omega64, V.da);
+    trace.mark("double-float K, M, D_A");
     {
         int nnz = 0;
         MTGPU_TRY(cudaMemcpyAsync(&nnz, V.G.d_gp + m, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -2915,9 +2926,29 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
         }
     }
     if (m > 0) {
-        k_gdiag<<<ceil_div(m, 128), 128, 0, st>>>(m, V.G.d_gp, V.G.d_gj, V.G.d_gv, P.d_nc, P.d_nr,
-                                                   P.d_pc, P.d_pr, P.d_col_c, P.d_kc, P.d_mc,
-                                                   P.d_col_r, P.d_kr, V.gkg, V.gmg);
+        int nnz = 0;
+        MTGPU_TRY(cudaMemcpyAsync(&nnz, V.G.d_gp + m, sizeof(int), cudaMemcpyDeviceToHost, st));
+        MTGPU_TRY(cudaStreamSynchronize(st));
+        double *tkv = nullptr, *tmv = nullptr;
+        int *rowof = nullptr;
+        if ((rc = dev_alloc(&tkv, std::max(nnz, 1))) || (rc = dev_alloc(&tmv, std::max(nnz, 1))) ||
+            (rc = dev_alloc(&rowof, std::max(nnz, 1)))) {
+            dev_free(tkv);
+            dev_free(tmv);
+            return rc;
+        }
+        k_gdiag_rows<<<ceil_div(m, kB), kB, 0, st>>>(m, V.G.d_gp, rowof);
+        if (nnz > 0)
+            k_gdiag_entry<<<ceil_div(nnz, 128), 128, 0, st>>>(m, V.G.d_gp, V.G.d_gj, V.G.d_gv, rowof,
+                                                              P.d_nc, P.d_nr, P.d_pc, P.d_pr,
+                                                              P.d_col_c, P.d_kc, P.d_mc, P.d_col_r,
+                                                              P.d_kr, tkv, tmv);
+        k_gdiag<<<ceil_div(m, kB), kB, 0, st>>>(m, V.G.d_gp, V.G.d_gv, tkv, tmv, V.gkg, V.gmg);
+        note_launches(2);
+        cudaStreamSynchronize(st);
+        dev_free(tkv);
+        dev_free(tmv);
+        dev_free(rowof);
         const size_t nm = (size_t)m * V.SP;
         k_diag_s<<<(unsigned)((nm + kB - 1) / kB), kB, 0, st>>>(m, V.SP, V.gkg, V.gmg, V.omega64, V.ds);
     }
