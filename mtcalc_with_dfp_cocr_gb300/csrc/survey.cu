@@ -1261,22 +1261,28 @@ k_mf_edges2(int nb, MF M, const float2 *__restrict__ omega, const float4 *__rest
                 if (on[u]) tail[u].row(i + u, y[u], sv[u], z);
         }
     }
-    // per-system sums in a fixed order (run-to-run identical): every
-    // thread's partials staged, then thread k < SP adds those of system k
-    // over the block's threads in thread order
-    __shared__ double stage[2][2][kB];
+    // per-system sums of the block in a fixed order (run-to-run identical):
+    // the lanes of a warp holding system 2 (t % H) + u are H apart, so a
+    // shuffle tree over offsets 16 ... H leaves the warp's sums in lanes
+    // l < H; then thread k < SP adds the warps' sums of system k in warp
+    // order, and the grid sum takes it from there
+    __shared__ double wsum[2][kB / 32][SP];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int u = 0; u < 2; u++) {
-        stage[0][u][threadIdx.x] = tail[u].zsr.to_double();
-        stage[1][u][threadIdx.x] = tail[u].zsi.to_double();
+        double a[2] = {tail[u].zsr.to_double(), tail[u].zsi.to_double()};
+#pragma unroll
+        for (int n = 0; n < 2; n++) {
+#pragma unroll
+            for (int o = 16; o >= H; o >>= 1) a[n] += __shfl_down_sync(0xffffffffu, a[n], o);
+            if (lane < H) wsum[n][warp][2 * lane + u] = a[n];
+        }
     }
     __syncthreads();
     double v[2] = {0.0, 0.0};
-    if (threadIdx.x < SP) {
-        const int kk = threadIdx.x, u = kk & 1, slot = kk >> 1;   // k0 = 2 (t % H) + u
-        for (int t = slot; t < kB; t += H)
-            for (int n = 0; n < 2; n++) v[n] += stage[n][u][t];
-    }
+    if (threadIdx.x < SP)
+        for (int q = 0; q < kB / 32; q++)
+            for (int n = 0; n < 2; n++) v[n] += wsum[n][q][threadIdx.x];
     SpmvTail::finish_v<SP>(v, sys, partials, mode);
 }
 
