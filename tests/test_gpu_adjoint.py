@@ -78,3 +78,20 @@ def test_autograd_function(case):
     g = pb.gradient(st).cpu().numpy()
     assert float(J.detach()) == pytest.approx(J2, rel=1e-12)
     np.testing.assert_allclose(t.grad.numpy(), g, rtol=1e-9, atol=1e-12 * np.abs(g).max())
+
+
+def test_batched_problem_with_more_than_16_frequencies(gpu):
+    """More than 16 frequencies (over 32 systems: two solver batches in one
+    survey) in the batched problem: the misfit equals the FP64 problem's."""
+    w, m0, m_true, earth_core, rng = _setup()
+    freqs = list(np.logspace(-1, 2, 17))
+    p64 = adjoint.ImpedanceProblem(w.mesh, freqs, w.receivers, solver="fp64", eps=1e-11)
+    resp, _ = p64.forward(m_true)
+    z_obs = adjoint.impedances(resp).cpu().numpy()
+    p64.set_observed(z_obs)
+    pb = adjoint.ImpedanceProblem(w.mesh, freqs, w.receivers, z_obs=z_obs, solver="batched",
+                                  eps=1e-10)
+    J64, _ = p64.misfit(m0)
+    Jb, _ = pb.misfit(m0)
+    assert J64 > 0.0
+    assert abs(Jb - J64) <= 1e-6 * abs(J64)

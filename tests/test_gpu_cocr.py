@@ -228,3 +228,15 @@ def test_dropin_double_float_rejects_bad_input(gpu):
             solver.pcocr_2x2_folded(slae, msh, double_float=True, stop_on_true_residual=True)
     code, x, st = solver.pcocr_2x2_folded(s, mesh, double_float=True, stop_on_true_residual=True)
     assert code == 0 and st.true_residual_rel < 1e-8
+
+
+def test_kit_unwritable_keeps_solution(gpu, tmp_path):
+    """The reference entry point writes its `kit` line after the solve; a kit
+    file that cannot be created is reported and the solver's code returned,
+    with x solved (the reference writes the solution regardless,
+    HarmVect3d.cpp:322-328)."""
+    w, s, mesh = _c1_system(1)
+    (tmp_path / "kit").mkdir()          # fopen("kit", "w") fails on a directory
+    code, x, _ = solver.pcocr_2x2_folded(s, mesh, write_kit_in=str(tmp_path))
+    assert code == 0
+    assert _true_rel_res(s, x) < 1e-7
