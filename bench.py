@@ -323,6 +323,15 @@ def gpu_arm(args):
         traffic = None
         traffic_src = None
     achieved = spmv_bytes / (spmv_ms * 1e-3) / 1e9
+    # the whole iteration against HBM: the algorithmic bytes of its five
+    # kernels (node: z, a gathered, D_S read, h written; edge: s, p, z, a,
+    # D_A, x read, p, a, w, x written, h gathered, the compact G^T row;
+    # update: a, w, s_m, r, s read, r, s, s_m written; the SpMV as above)
+    # over the solve's time per iteration (its set-up and FP64 checks
+    # included); m = the interior nodes, the rows of G on these meshes
+    m_nodes = (m_.nx - 2) * (m_.ny - 2) * (m_.nz - 2)
+    iter_bytes = 16 * SP * (20 * nb + 3 * m_nodes) + 8 * nb + spmv_bytes
+    iter_ms = 1e3 * batched["seconds"] / max(batched["iterations"])
     # the FP64 SpMV of the plain path (bound by the FP64 pipe on GB300)
     ctx = A.cocr(nus[0], stream)
     xs = torch.randn(2 * nb, dtype=torch.float64, device="cuda")
@@ -395,6 +404,10 @@ def gpu_arm(args):
                      "bytes_per_launch": spmv_bytes, "ms_per_launch": spmv_ms,
                      "traffic": traffic, "traffic_source": traffic_src,
                      "binding": SPMV_MF_BINDING if variant in (32, 33, 35) else None},
+        "roofline_iteration": {"bound": "hbm", "achieved": iter_bytes / (iter_ms * 1e-3) / 1e9,
+                               "peak": peak, "unit": "GB/s",
+                               "frac": iter_bytes / (iter_ms * 1e-3) / 1e9 / peak,
+                               "bytes_per_iteration": iter_bytes, "ms_per_iteration": iter_ms},
         "roofline_fp64_spmv": {"bound": "fp64 pipe (GB300 FP64 = FP32/64)",
                                "achieved": achieved64, "peak": peak, "unit": "GB/s",
                                "frac": achieved64 / peak, "bytes_per_launch": spmv64_bytes,

@@ -384,7 +384,7 @@ int mtgpu_cocr_create(int nb, int nnz_lower, const int *ig, const int *jg, const
         note_launches(5);
         if (rc) goto fail;
     }
-    if ((rc = folded_build_g(mesh, S.P, S.st))) goto fail;
+    if ((rc = folded_build_g_auto(mesh, nullptr, S.P, S.st))) goto fail;
     if ((rc = folded_build_diag(S.A, S.P, S.st))) goto fail;
     note_launches(2);
     if ((rc = cocr_alloc(S))) goto fail;

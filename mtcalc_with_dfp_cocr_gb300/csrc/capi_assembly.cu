@@ -247,7 +247,13 @@ int mtgpu_cocr_create_from_assembly(mtgpu_assembly *a, double nu, void *stream, 
     mtgpu_mesh_desc mesh{a->P.kpar, a->P.nb, a->P.kuzlov, a->nvkat.data(), a->nver.data(),
                          a->sigflag.data(), a->edges.data(), a->ig_t.data(), a->ig_t.data(),
                          nullptr, a->bound.data(), a->nver_stride};
-    if (!(rc = param_to_sell(a->P, kTwoPi * nu, S.A, S.st)) && !(rc = folded_build_g(mesh, S.P, S.st)) &&
+    DevMeshUpload dmu;
+    const ParamMatrix &P = a->P;
+    if (!(rc = param_to_sell(a->P, kTwoPi * nu, S.A, S.st)) &&
+        !(rc = dmu.over_device(P.kpar, P.nb, P.kuzlov, P.nver_stride, P.d_xyz, P.d_nver, P.d_nvkat,
+                               P.d_edges, P.d_bnode, a->sigflag.data(), (int)a->sigflag.size(),
+                               S.st)) &&
+        !(rc = folded_build_g_auto(mesh, &dmu.view, S.P, S.st)) &&
         !(rc = folded_build_diag(S.A, S.P, S.st)) && !(rc = cocr_alloc(S))) {
         note_launches(2);
         cudaError_t e = cudaStreamSynchronize(S.st);

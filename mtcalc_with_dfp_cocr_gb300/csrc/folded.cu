@@ -276,6 +276,19 @@ int folded_build_g_device(const DevMesh &dm, Folded &P, cudaStream_t st, bool *c
     return done(MTGPU_OK);
 }
 
+int folded_build_g_auto(const mtgpu_mesh_desc &mesh, const DevMesh *dm, Folded &P, cudaStream_t st)
+{
+    DevMeshUpload dmu;
+    int rc;
+    if (!dm) {
+        if ((rc = dmu.upload(mesh, nullptr, st))) return rc;
+        dm = &dmu.view;
+    }
+    bool conforming = false;
+    if ((rc = folded_build_g_device(*dm, P, st, &conforming))) return rc;
+    return conforming ? MTGPU_OK : folded_build_g(mesh, P, st);
+}
+
 void DevMeshUpload::release()
 {
     dev_free(nver); dev_free(nvkat); dev_free(edges); dev_free(xyz); dev_free(sigflag);

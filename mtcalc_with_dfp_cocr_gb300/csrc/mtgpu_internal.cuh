@@ -119,6 +119,10 @@ struct DevMeshUpload {
 // folded_build_g); *conforming = false, and nothing built, when an edge
 // has a node beyond nn (T-matrix meshes: folded_build_g handles them)
 int folded_build_g_device(const DevMesh &dm, Folded &P, cudaStream_t st, bool *conforming);
+// G and G^T for a solver set-up: on the device from dm (or from an upload of
+// the host mesh description when dm is null) where the mesh is conforming,
+// else by the host construction
+int folded_build_g_auto(const mtgpu_mesh_desc &mesh, const DevMesh *dm, Folded &P, cudaStream_t st);
 // exclusive prefix sum: out[0..n] (out[n] = total), *total on the host
 int dev_exclusive_scan(const int *d_in, long long n, int *d_out, long long *total, cudaStream_t st);
 // D_A and D_S from the device matrix.
