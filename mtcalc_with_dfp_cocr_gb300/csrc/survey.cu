@@ -163,6 +163,13 @@ __device__ bool sys_grid_sum(double (&v)[N], double *partials, unsigned int *tic
 // are visible (a no-op for a kernel launched without the attribute).
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
+// Element i of a grid-stride sweep over n elements, forwards or backwards.
+// Consecutive kernels of the iteration sweep in opposite directions, so
+// that each starts on the end of what the previous one streamed, which is
+// still in L2 (a 58 MB vector of two systems against ~126 MB of L2); only
+// the order of the partial sums changes, and it is fixed.
+__device__ __forceinline__ int sweep(int i, int n, int rev) { return rev ? n - 1 - i : i; }
+
 template <typename... K, typename... A>
 void pdl(void (*kernel)(K...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, A &&...args)
 {
@@ -335,14 +342,15 @@ template <int SP>
 __global__ void __launch_bounds__(kB)
 k_node(int m, const int *__restrict__ gp, const int *__restrict__ gj, const float *__restrict__ gv,
        const float4 *__restrict__ ds, const float4 *__restrict__ z, const float4 *__restrict__ a,
-       float4 *__restrict__ h, const SysState *sys, int use_beta)
+       float4 *__restrict__ h, const SysState *sys, int use_beta, int rev)
 {
     pdl_wait();
     const int k = threadIdx.x % SP;
     if (sys[k].status != kRun) return;
     const dfc be = from_d2(sys[k].beta);
     const int rpb = kB / SP;
-    for (int v = blockIdx.x * rpb + threadIdx.x / SP; v < m; v += gridDim.x * rpb) {
+    for (int vi = blockIdx.x * rpb + threadIdx.x / SP; vi < m; vi += gridDim.x * rpb) {
+        const int v = sweep(vi, m, rev);
         const int j0 = __ldg(gp + v), j1 = __ldg(gp + v + 1);
         const float4 dsv = __ldg(ds + (long long)v * SP + k);
         acc hr, hi;
@@ -368,7 +376,7 @@ k_edge(int n, const int *__restrict__ tp, const int *__restrict__ tj, const floa
        const int2 *__restrict__ tn, const float4 *__restrict__ da, const float4 *__restrict__ h,
        const float4 *__restrict__ src, const float4 *__restrict__ z, float4 *__restrict__ p,
        float4 *__restrict__ a, float4 *__restrict__ w, float4 *__restrict__ x, SysState *sys,
-       double *partials, int mode)
+       double *partials, int mode, int rev)
 {
     pdl_wait();
     const int k = threadIdx.x % SP;
@@ -385,9 +393,10 @@ k_edge(int n, const int *__restrict__ tp, const int *__restrict__ tj, const floa
     // so that this element's h gathers issue with its other loads
     const int e_first = blockIdx.x * rpb + threadIdx.x / SP;
     int2 r2n = make_int2(-1, -1);
-    if (tn && on && e_first < n) r2n = __ldg(tn + e_first);
-    for (int e = e_first; e < n; e += stride) {
+    if (tn && on && e_first < n) r2n = __ldg(tn + sweep(e_first, n, rev));
+    for (int ei = e_first; ei < n; ei += stride) {
         if (!on) break;
+        const int e = sweep(ei, n, rev);
         const long long idx = (long long)e * SP + k;
         // G^T row: compact (the rows of the edge's two nodes, -1/2 and +1/2
         // in that order) or the CSR of T-matrix meshes
@@ -395,7 +404,7 @@ k_edge(int n, const int *__restrict__ tp, const int *__restrict__ tj, const floa
         int2 r2 = make_int2(-1, -1);
         if (tn) {
             r2 = r2n;
-            if (e + stride < n) r2n = __ldg(tn + e + stride);
+            if (ei + stride < n) r2n = __ldg(tn + sweep(ei + stride, n, rev));
             j0 = 0;
             j1 = (r2.x >= 0) + (r2.y >= 0);
         } else {
@@ -492,7 +501,7 @@ k_edge(int n, const int *__restrict__ tp, const int *__restrict__ tj, const floa
 template <int SP>
 __global__ void __launch_bounds__(kB)
 k_update(int n, const float4 *__restrict__ a, const float4 *__restrict__ w, float4 *__restrict__ sm,
-         float4 *__restrict__ r, float4 *__restrict__ s, SysState *sys, double *partials)
+         float4 *__restrict__ r, float4 *__restrict__ s, SysState *sys, double *partials, int rev)
 {
     pdl_wait();
     const int k = threadIdx.x % SP;
@@ -512,14 +521,14 @@ k_update(int n, const float4 *__restrict__ a, const float4 *__restrict__ w, floa
 #pragma unroll
         for (int u = 0; u < 2; u++) {
             if (u == 1 && !two) break;
-            const long long idx = (long long)(e + u * stride) * SP + k;
+            const long long idx = (long long)sweep(e + u * stride, n, rev) * SP + k;
             v[u][0] = __ldg(a + idx); v[u][1] = __ldg(w + idx);
             v[u][2] = sm[idx]; v[u][3] = r[idx]; v[u][4] = s[idx];
         }
 #pragma unroll
         for (int u = 0; u < 2; u++) {
             if (u == 1 && !two) break;
-            const long long idx = (long long)(e + u * stride) * SP + k;
+            const long long idx = (long long)sweep(e + u * stride, n, rev) * SP + k;
             const dfc ro = from4(v[u][3]);
             dfc smv = from4(v[u][2]);
             if (pm == 1) {
@@ -885,7 +894,8 @@ __device__ __forceinline__ dfc mf_x(const MF &M, const float4 *__restrict__ x, i
 template <int SP>
 __global__ void __launch_bounds__(kB)
 k_node_lat(MF M, int m, const float4 *__restrict__ ds, const float4 *__restrict__ z,
-           const float4 *__restrict__ a, float4 *__restrict__ h, const SysState *sys, int use_beta)
+           const float4 *__restrict__ a, float4 *__restrict__ h, const SysState *sys, int use_beta,
+           int rev)
 {
     pdl_wait();
     const int k = threadIdx.x % SP;
@@ -893,7 +903,8 @@ k_node_lat(MF M, int m, const float4 *__restrict__ ds, const float4 *__restrict_
     const dfc be = from_d2(sys[k].beta);
     const int ix = M.nx - 2, iy = M.ny - 2;
     const int rpb = kB / SP;
-    for (int v = blockIdx.x * rpb + threadIdx.x / SP; v < m; v += gridDim.x * rpb) {
+    for (int vi = blockIdx.x * rpb + threadIdx.x / SP; vi < m; vi += gridDim.x * rpb) {
+        const int v = sweep(vi, m, rev);
         const int i = v % ix + 1, t = v / ix, j = t % iy + 1, kk = t / iy + 1;
         const int e0 = mf_edge_in(M, 0, i, j, kk);
         const int es[6] = {e0 + 2 - M.plane, e0 + 1 - M.l3, e0 - 3, e0, e0 + 1, e0 + 2};
@@ -992,14 +1003,15 @@ __device__ __forceinline__ dfc mf_face_f(const MF &M, const float4 *__restrict__
 // seen from +n: y then z for n = x, z then x for n = y, x then y for n = z)
 template <int SP>
 __global__ void __launch_bounds__(kB)
-k_mf_faces(MF M, const float4 *__restrict__ x, const SysState *sys)
+k_mf_faces(MF M, const float4 *__restrict__ x, const SysState *sys, int rev)
 {
     pdl_wait();
     const int k = threadIdx.x % SP;
     if (sys[k].status != kRun) return;
     const int nf = (int)(M.nfx + M.nfy + M.nfz);
     const int rpb = kB / SP;
-    for (int t = blockIdx.x * rpb + threadIdx.x / SP; t < nf; t += gridDim.x * rpb) {
+    for (int ti = blockIdx.x * rpb + threadIdx.x / SP; ti < nf; ti += gridDim.x * rpb) {
+        const int t = sweep(ti, nf, rev);
         int n, i, j, kk;
         mf_face_pos(M, t, n, i, j, kk);
         M.f[t * SP + k] = to4(mf_face_f<SP>(M, x, n, i, j, kk, k));
@@ -1219,7 +1231,7 @@ template <int SP>
 __global__ void __launch_bounds__(kB, 2)
 k_mf_edges2(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restrict__ s,
             float4 *__restrict__ z,
-            SysState *sys, double *partials, int mode)
+            SysState *sys, double *partials, int mode, int rev)
 {
     pdl_wait();
     constexpr int H = SP / 2;
@@ -1236,10 +1248,10 @@ k_mf_edges2(int nb, MF M, const float2 *__restrict__ omega, const float4 *__rest
     if (on[0] || on[1]) {
         // the next row's position is loaded one row ahead
         const int r0 = blockIdx.x * rpb + threadIdx.x / H;
-        unsigned cn = r0 < nb ? __ldg(M.pos + r0) : 0u;
-        for (int row = r0; row < nb; row += stride) {
+        unsigned cn = r0 < nb ? __ldg(M.pos + sweep(r0, nb, rev)) : 0u;
+        for (int ri = r0; ri < nb; ri += stride) {
             const unsigned c = cn;
-            if (row + stride < nb) cn = __ldg(M.pos + row + stride);
+            if (ri + stride < nb) cn = __ldg(M.pos + sweep(ri + stride, nb, rev));
             const int d = (int)(c >> 30);
             const Pos p{(int)(c & 1023u), (int)((c >> 10) & 1023u), (int)((c >> 20) & 1023u)};
             const int e = mf_edge(M, d, p.x, p.y, p.z);
@@ -1291,7 +1303,7 @@ template <int SP>
 __global__ void __launch_bounds__(kB, 2)
 k_mf_edges(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restrict__ s,
            float4 *__restrict__ z,
-           SysState *sys, double *partials, int mode)
+           SysState *sys, double *partials, int mode, int rev)
 {
     pdl_wait();
     const int k = threadIdx.x % SP;
@@ -1301,11 +1313,11 @@ k_mf_edges(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restr
     const int rpb = kB / SP, stride = gridDim.x * rpb;
     // the next row's position is loaded one row ahead
     const int r0 = blockIdx.x * rpb + threadIdx.x / SP;
-    unsigned cn = on && r0 < nb ? __ldg(M.pos + r0) : 0u;
-    for (int row = r0; row < nb; row += stride) {
+    unsigned cn = on && r0 < nb ? __ldg(M.pos + sweep(r0, nb, rev)) : 0u;
+    for (int ri = r0; ri < nb; ri += stride) {
         if (!on) break;
         const unsigned c = cn;
-        if (row + stride < nb) cn = __ldg(M.pos + row + stride);
+        if (ri + stride < nb) cn = __ldg(M.pos + sweep(ri + stride, nb, rev));
         const int d = (int)(c >> 30);
         const Pos p{(int)(c & 1023u), (int)((c >> 10) & 1023u), (int)((c >> 20) & 1023u)};
         const int e = mf_edge(M, d, p.x, p.y, p.z);
@@ -1338,7 +1350,7 @@ k_mf_edges(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restr
 // against 1.98 s for the 32-system c3 solve.)
 template <int SP>
 __global__ void __launch_bounds__(kB)
-k_mf_gface(MF M, const SysState *sys)
+k_mf_gface(MF M, const SysState *sys, int rev)
 {
     pdl_wait();
     const int k = threadIdx.x % SP;
@@ -1347,7 +1359,8 @@ k_mf_gface(MF M, const SysState *sys)
     const int nc = (int)M.ncell;
     auto cell = [&](int x, int y, int z) { return (z * (M.ny - 1) + y) * (M.nx - 1) + x; };
     const int rpb = kB / SP;
-    for (int t = blockIdx.x * rpb + threadIdx.x / SP; t < nf; t += gridDim.x * rpb) {
+    for (int ti = blockIdx.x * rpb + threadIdx.x / SP; ti < nf; ti += gridDim.x * rpb) {
+        const int t = sweep(ti, nf, rev);
         int n, i, j, kk;
         mf_face_pos(M, t, n, i, j, kk);
         const int pos = n == 0 ? i : (n == 1 ? j : kk);
@@ -1421,7 +1434,7 @@ template <int SP>
 __global__ void __launch_bounds__(kB)
 k_mf_edges_g(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restrict__ s,
              float4 *__restrict__ z,
-             SysState *sys, double *partials, int mode)
+             SysState *sys, double *partials, int mode, int rev)
 {
     pdl_wait();
     const int k = threadIdx.x % SP;
@@ -1431,11 +1444,11 @@ k_mf_edges_g(int nb, MF M, const float2 *__restrict__ omega, const float4 *__res
     const int rpb = kB / SP, stride = gridDim.x * rpb;
     // the next row's position is loaded one row ahead
     const int r0 = blockIdx.x * rpb + threadIdx.x / SP;
-    unsigned cn = on && r0 < nb ? __ldg(M.pos + r0) : 0u;
-    for (int row = r0; row < nb; row += stride) {
+    unsigned cn = on && r0 < nb ? __ldg(M.pos + sweep(r0, nb, rev)) : 0u;
+    for (int ri = r0; ri < nb; ri += stride) {
         if (!on) break;
         const unsigned c = cn;
-        if (row + stride < nb) cn = __ldg(M.pos + row + stride);
+        if (ri + stride < nb) cn = __ldg(M.pos + sweep(ri + stride, nb, rev));
         const int d = (int)(c >> 30);
         const Pos p{(int)(c & 1023u), (int)((c >> 10) & 1023u), (int)((c >> 20) & 1023u)};
         const int e = mf_edge(M, d, p.x, p.y, p.z);
@@ -2019,14 +2032,17 @@ struct Impl {
         return M;
     }
     // h = D_S G (src + beta a): the lattice form where G is the lattice's
+    // the sweep direction of the next launch: opposite to the previous one's
+    static int flip(Survey &V) { return V.dir ^= 1; }
     static void node(Survey &V, const float4 *src, const float4 *a, int use_beta)
     {
+        const int rv = flip(V);
         if (V.g_lat)
             pdl(k_node_lat<SP>, V.g_node_lat, kB, 0, V.st, mfd(V), V.G.m, V.ds, src, a, V.h, V.sys,
-                                                          use_beta);
+                use_beta, rv);
         else
             pdl(k_node<SP>, V.g_node, kB, 0, V.st, V.G.m, V.G.d_gp, V.G.d_gj, V.gv32, V.ds, src, a,
-                                                  V.h, V.sys, use_beta);
+                V.h, V.sys, use_beta, rv);
     }
     static void spmv(Survey &V, int mode)
     {
@@ -2039,23 +2055,23 @@ struct Impl {
         }
         if (V.ch == kMatFree + 3) {
             const MF M = mfd(V);
-            pdl(k_mf_faces<SP>, V.g_mff, kB, 0, V.st, M, V.s, V.sys);
-            pdl(k_mf_gface<SP>, V.g_mfg, kB, 0, V.st, M, V.sys);
+            pdl(k_mf_faces<SP>, V.g_mff, kB, 0, V.st, M, V.s, V.sys, flip(V));
+            pdl(k_mf_gface<SP>, V.g_mfg, kB, 0, V.st, M, V.sys, flip(V));
             pdl(k_mf_edges_g<SP>, V.g_mfe3, kB, 0, V.st, V.nb, M, V.omega, V.s, V.z, V.sys,
-                                                       V.partials, mode);
+                                                       V.partials, mode, flip(V));
             return;
         }
         if (V.ch == kMatFree || V.ch == kMatFree + 1) {
             const MF M = mfd(V);
-            pdl(k_mf_faces<SP>, V.g_mff, kB, 0, V.st, M, V.s, V.sys);
+            pdl(k_mf_faces<SP>, V.g_mff, kB, 0, V.st, M, V.s, V.sys, flip(V));
             if constexpr (SP >= 2) {
                 if (V.ch == kMatFree + 1) {
-                    pdl(k_mf_edges2<SP>, V.g_mfe, kB, 0, V.st, V.nb, M, V.omega, V.s, V.z, V.sys, V.partials, mode);
+                    pdl(k_mf_edges2<SP>, V.g_mfe, kB, 0, V.st, V.nb, M, V.omega, V.s, V.z, V.sys, V.partials, mode, flip(V));
                     return;
                 }
             }
             pdl(k_mf_edges<SP>, V.g_mfe, kB, 0, V.st, V.nb, M, V.omega, V.s, V.z, V.sys,
-                                                    V.partials, mode);
+                                                    V.partials, mode, flip(V));
             return;
         }
         if (V.ch == 0) {
@@ -2094,15 +2110,15 @@ struct Impl {
             k_prec_tile<SP><<<V.g_pt, PrecTile<SP>::NT, PrecTile<SP>::SMEM, V.st>>>(
                 mfd(V), G, V.ds, V.da, V.s, V.z, ain, aout, V.p, V.w, V.x, V.sys, V.partials);
             pdl(k_update<SP>, V.g_update, kB, 0, V.st, V.nb, aout, V.w, V.sm, V.r, V.s, V.sys,
-                V.partials);
+                V.partials, flip(V));
             spmv(V, 1);
             return;
         }
         if (V.G.m > 0)
             node(V, V.z, V.a, 1);
         pdl(k_edge<SP>, V.g_edge, kB, 0, V.st, V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.G.d_tn, V.da, V.h, V.s, V.z,
-                                              V.p, V.a, V.w, V.x, V.sys, V.partials, 1);
-        pdl(k_update<SP>, V.g_update, kB, 0, V.st, V.nb, V.a, V.w, V.sm, V.r, V.s, V.sys, V.partials);
+                                              V.p, V.a, V.w, V.x, V.sys, V.partials, 1, flip(V));
+        pdl(k_update<SP>, V.g_update, kB, 0, V.st, V.nb, V.a, V.w, V.sm, V.r, V.s, V.sys, V.partials, flip(V));
         spmv(V, 1);
     }
     // one preconditioner step of the iteration (mode 1), unfused or fused
@@ -2117,7 +2133,7 @@ struct Impl {
         if (V.G.m > 0)
             node(V, V.z, ain, 1);
         pdl(k_edge<SP>, V.g_edge, kB, 0, V.st, V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.G.d_tn, V.da, V.h,
-                                              V.s, V.z, V.p, ain, V.w, V.x, V.sys, V.partials, 1);
+                                              V.s, V.z, V.p, ain, V.w, V.x, V.sys, V.partials, 1, flip(V));
     }
     static void prec_grid(Survey &V, int nsm)
     {
@@ -2157,7 +2173,7 @@ struct Impl {
         if (V.G.m > 0)
             node(V, V.r, V.a, 0);
         k_edge<SP><<<V.g_edge, kB, 0, V.st>>>(V.nb, V.G.d_tp, V.G.d_tj, V.tv32, V.G.d_tn, V.da, V.h, V.r, V.z,
-                                              V.p, V.a, V.s, V.x, V.sys, V.partials, 0);
+                                              V.p, V.a, V.s, V.x, V.sys, V.partials, 0, flip(V));
         cudaMemsetAsync(V.p, 0, sizeof(float4) * (size_t)V.nb * SP, V.st);
         cudaMemsetAsync(V.a, 0, sizeof(float4) * (size_t)V.nb * SP, V.st);
         spmv(V, 0);

@@ -56,6 +56,7 @@ struct Survey {
     int g_init = 0, g_node = 0, g_edge = 0, g_update = 0, g_spmv = 0, g_true = 0;  // launch grids
     int g_node_lat = 0;
     bool g_lat = false;            // G is the lattice's (k_node_lat computes its entries)
+    int dir = 0;                   // sweep direction of the last launch (kernels alternate)
     // SpMV variant (autotuned): 0 x and matrix slots staged in shared memory per
     // tile, 1 x staged only, 2/4/8 gathers from global memory with that many slots in flight,
     // kRowVariant + 2/4 (two systems only) one thread per row for both systems
