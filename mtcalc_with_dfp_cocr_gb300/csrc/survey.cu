@@ -1345,44 +1345,110 @@ k_mf_edges(int nb, MF M, const float2 *__restrict__ omega, const float4 *__restr
 // edge's curl-curl row is then the signed sum of g over its 4 faces, 8 adds
 // instead of the 24 multiply-adds of mf_row.  g is needed only on faces
 // whose position along the normal is interior (the faces of non-Dirichlet
-// edges); the others get 0.  (Computing the three circulations from x in
-// this kernel instead of reading the face array measured slower: 2.04 s
-// against 1.98 s for the 32-system c3 solve.)
+// edges); the others get 0.
+
+// g = F f straight from x, each circulation formed once (variant 35):
+// y- and z-normal faces by columns along the normal — a thread owns a
+// column (its transverse position; neighbouring threads, neighbouring
+// columns) and a chunk of kMarch positions, computes the circulations of
+// the chunk and of its two neighbours and keeps the last two in registers
+// while it marches; x-normal faces, whose neighbours along the normal are
+// the adjacent faces of the same row, one per thread with the two
+// neighbours' circulations formed from the same cached loads.  Every
+// circulation is k_mf_faces' sum and every g the same three multiply-adds
+// in the same order whichever thread forms it, so g does not depend on the
+// decomposition; no face array is written.
+constexpr int kMarch = 16;
+
+struct GMarch {
+    int xitems, yitems;    // x-normal faces; y-normal column chunks (z-normal after)
+    int ycols, zcols;      // columns per chunk row: (nx-1) for both
+    int ych, zch;          // chunks per column
+};
+
+template <int SP>
+__device__ __forceinline__ dfc mf_g(const MF &M, int n, int cb, int ca, dfc fm, dfc f0, dfc fp)
+{
+    const int nc = (int)M.ncell;
+    const df wa = d2f(__ldg(M.w + n * nc + cb)), wb = d2f(__ldg(M.w + n * nc + ca));
+    const df c0 = scale(add(wa, wb), 2.f);
+    acc gr, gi;
+    gr.mac(wa, fm.re); gr.mac(c0, f0.re); gr.mac(wb, fp.re);
+    gi.mac(wa, fm.im); gi.mac(c0, f0.im); gi.mac(wb, fp.im);
+    return dfc{gr.get(), gi.get()};
+}
+
 template <int SP>
 __global__ void __launch_bounds__(kB)
-k_mf_gface(MF M, const SysState *sys, int rev)
+k_mf_gmarch(MF M, GMarch G, const float4 *__restrict__ x, const SysState *sys, int rev)
 {
     pdl_wait();
     const int k = threadIdx.x % SP;
     if (sys[k].status != kRun) return;
-    const long long nf = M.nfx + M.nfy + M.nfz;
-    const int nc = (int)M.ncell;
-    auto cell = [&](int x, int y, int z) { return (z * (M.ny - 1) + y) * (M.nx - 1) + x; };
+    const dfc zero{df{0.f, 0.f}, df{0.f, 0.f}};
+    const int nx = M.nx, ny = M.ny, nz = M.nz;
+    auto cell = [&](int a, int b, int c) { return (c * (ny - 1) + b) * (nx - 1) + a; };
+    const int zitems = G.zcols * (ny - 1) * G.zch;
+    const int nitems = G.xitems + G.yitems + zitems;
     const int rpb = kB / SP;
-    for (int ti = blockIdx.x * rpb + threadIdx.x / SP; ti < nf; ti += gridDim.x * rpb) {
-        const int t = sweep(ti, nf, rev);
-        int n, i, j, kk;
-        mf_face_pos(M, t, n, i, j, kk);
-        const int pos = n == 0 ? i : (n == 1 ? j : kk);
-        const int last = (n == 0 ? M.nx : (n == 1 ? M.ny : M.nz)) - 1;
-        float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (pos >= 1 && pos < last) {
-            // the neighbouring faces along the normal (dm faces apart in the
-            // face numbering) and the cells between them
-            const int di = n == 0, dj = n == 1, dk = n == 2;
-            const long long dm = n == 0 ? 1 : (n == 1 ? M.nx - 1 : (long long)(M.nx - 1) * (M.ny - 1));
-            const int cb = cell(i - di, j - dj, kk - dk), ca = cell(i, j, kk);
-            const df wa = d2f(__ldg(M.w + n * nc + cb)), wb = d2f(__ldg(M.w + n * nc + ca));
-            const dfc fm = from4(__ldg(M.f + (t - dm) * SP + k));
-            const dfc f0 = from4(__ldg(M.f + t * SP + k));
-            const dfc fp = from4(__ldg(M.f + (t + dm) * SP + k));
-            const df c0 = scale(add(wa, wb), 2.f);
-            acc gr, gi;
-            gr.mac(wa, fm.re); gr.mac(c0, f0.re); gr.mac(wb, fp.re);
-            gi.mac(wa, fm.im); gi.mac(c0, f0.im); gi.mac(wb, fp.im);
-            out = to4(dfc{gr.get(), gi.get()});
+    for (int qi = blockIdx.x * rpb + threadIdx.x / SP; qi < nitems; qi += gridDim.x * rpb) {
+        const int q = sweep(qi, nitems, rev);
+        if (q < G.xitems) {
+            // x-normal face t = (kk (ny-1) + j) nx + i: neighbours i -+ 1
+            int n, i, j, kk;
+            mf_face_pos(M, q, n, i, j, kk);
+            dfc out = zero;
+            if (i >= 1 && i < nx - 1) {
+                const dfc fm = mf_face_f<SP>(M, x, 0, i - 1, j, kk, k);
+                const dfc f0 = mf_face_f<SP>(M, x, 0, i, j, kk, k);
+                const dfc fp = mf_face_f<SP>(M, x, 0, i + 1, j, kk, k);
+                out = mf_g<SP>(M, 0, cell(i - 1, j, kk), cell(i, j, kk), fm, f0, fp);
+            }
+            M.g[(long long)q * SP + k] = to4(out);
+            continue;
         }
-        M.g[t * SP + k] = out;
+        // a column chunk: y-normal (column (i, kk), positions j) or z-normal
+        // (column (i, j), positions kk)
+        int n, i, c2, p0, L;
+        if (q < G.xitems + G.yitems) {
+            const int r = q - G.xitems;
+            n = 1;
+            i = r % G.ycols;
+            const int t = r / G.ycols;
+            c2 = t % (nz - 1);              // kk
+            p0 = (t / (nz - 1)) * kMarch;   // j
+            L = ny - 1;
+        } else {
+            const int r = q - G.xitems - G.yitems;
+            n = 2;
+            i = r % G.zcols;
+            const int t = r / G.zcols;
+            c2 = t % (ny - 1);              // j
+            p0 = (t / (ny - 1)) * kMarch;   // kk
+            L = nz - 1;
+        }
+        const int p1 = min(p0 + kMarch, L + 1);
+        auto fat = [&](int p) {
+            return n == 1 ? mf_face_f<SP>(M, x, 1, i, p, c2, k) : mf_face_f<SP>(M, x, 2, i, c2, p, k);
+        };
+        auto face = [&](int p) -> long long {
+            return n == 1 ? M.nfx + ((long long)c2 * ny + p) * (nx - 1) + i
+                          : M.nfx + M.nfy + ((long long)p * (ny - 1) + c2) * (nx - 1) + i;
+        };
+        dfc fm = p0 >= 1 ? fat(p0 - 1) : zero;
+        dfc f0 = fat(p0);
+        for (int p = p0; p < p1; p++) {
+            const dfc fp = p + 1 <= L ? fat(p + 1) : zero;
+            dfc out = zero;
+            if (p >= 1 && p < L) {
+                const int cb = n == 1 ? cell(i, p - 1, c2) : cell(i, c2, p - 1);
+                const int ca = n == 1 ? cell(i, p, c2) : cell(i, c2, p);
+                out = mf_g<SP>(M, n, cb, ca, fm, f0, fp);
+            }
+            M.g[face(p) * SP + k] = to4(out);
+            fm = f0;
+            f0 = fp;
+        }
     }
 }
 
@@ -2013,6 +2079,18 @@ struct Impl {
                        V.uoff, V.ucol, V.tile_T, V.ntiles, P.nslices};
     }
     static void mfd_into(const Survey &V, MF &M) { M = mfd(V); }
+    // the work items of k_mf_gmarch
+    static GMarch gmarch(const Survey &V)
+    {
+        const MatFree &F = V.mf;
+        GMarch G;
+        G.ycols = G.zcols = F.nx - 1;
+        G.ych = ceil_div(F.ny, kMarch);
+        G.zch = ceil_div(F.nz, kMarch);
+        G.xitems = (int)F.nfx;
+        G.yitems = G.ycols * (F.nz - 1) * G.ych;
+        return G;
+    }
     static MF mfd(const Survey &V)
     {
         const MatFree &F = V.mf;
@@ -2055,8 +2133,7 @@ struct Impl {
         }
         if (V.ch == kMatFree + 3) {
             const MF M = mfd(V);
-            pdl(k_mf_faces<SP>, V.g_mff, kB, 0, V.st, M, V.s, V.sys, flip(V));
-            pdl(k_mf_gface<SP>, V.g_mfg, kB, 0, V.st, M, V.sys, flip(V));
+            pdl(k_mf_gmarch<SP>, V.g_mfg, kB, 0, V.st, M, gmarch(V), V.s, V.sys, flip(V));
             pdl(k_mf_edges_g<SP>, V.g_mfe3, kB, 0, V.st, V.nb, M, V.omega, V.s, V.z, V.sys,
                                                        V.partials, mode, flip(V));
             return;
@@ -2219,8 +2296,13 @@ struct Impl {
             V.g_mff = g((const void *)k_mf_faces<SP>, (int)std::min<long long>(
                                                           (nf + kB / SP - 1) / (kB / SP), INT_MAX));
             V.g_mfe = g((const void *)k_mf_edges<SP>, V.grid_rows);
-            V.g_mfg = g((const void *)k_mf_gface<SP>, (int)std::min<long long>(
-                                                          (nf + kB / SP - 1) / (kB / SP), INT_MAX));
+            {
+                const GMarch G = gmarch(V);
+                const long long items = (long long)G.xitems + G.yitems +
+                                        (long long)G.zcols * (V.mf.ny - 1) * G.zch;
+                V.g_mfg = g((const void *)k_mf_gmarch<SP>, (int)std::min<long long>(
+                                                               (items + kB / SP - 1) / (kB / SP), INT_MAX));
+            }
             V.g_mfe3 = g((const void *)k_mf_edges_g<SP>, V.grid_rows);
             if constexpr (SP >= 2) {
                 if (V.ch == kMatFree + 1)

@@ -118,7 +118,7 @@ inline bool spmv_variant_available(const Survey &V, int v)
 // the matrix-free forms
 inline int spmv_extra_launches(int v)
 {
-    return v == kMatFree || v == kMatFree + 1 ? 1 : (v == kMatFree + 3 ? 2 : 0);
+    return v == kMatFree || v == kMatFree + 1 || v == kMatFree + 3 ? 1 : 0;
 }
 
 // The host side of the matrix-free set-up (the tables themselves are
