@@ -4,6 +4,7 @@
 #pragma once
 #include "mtgpu_internal.cuh"
 
+#include <map>
 #include <vector>
 
 namespace mtgpu {
@@ -69,4 +70,8 @@ struct mtgpu_assembly_s {
     std::vector<double> sigflag;
     std::vector<int> ig_t;
     int nver_stride = 14;
+    // the SpMV variant the first survey set-up on this mesh chose, per batch
+    // width (lanes): the choice depends on the mesh and the width only, so
+    // later surveys on the assembly skip the autotuning
+    std::map<int, int> tuned;
 };

@@ -347,7 +347,12 @@ int mtgpu_survey_create_multi(int nmesh, mtgpu_assembly *const *a, const int *S,
             s->g_first.push_back(k0 + f);
             std::vector<double> om(n);
             for (int k = 0; k < n; k++) om[k] = kTwoPi * nu[k0 + f + k];
-            int rc = survey_setup(am->P, mesh, n, om.data(), *s->groups.back(), st, am);
+            int sp = 1;
+            while (sp < n) sp <<= 1;
+            const auto tu = am->tuned.find(sp);
+            int rc = survey_setup(am->P, mesh, n, om.data(), *s->groups.back(), st, am,
+                                  nullptr, tu != am->tuned.end() ? tu->second : -1);
+            if (!rc && s->groups.back()->autotuned) am->tuned[sp] = s->groups.back()->ch;
             if (rc) {
                 mtgpu_survey_destroy(s);
                 return rc;

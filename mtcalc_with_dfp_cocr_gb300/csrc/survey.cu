@@ -2952,6 +2952,7 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
 {
     PhaseTrace trace(st, "survey set-up");
     V.release();
+    V.autotuned = false;
     MTGPU_CHECK_ARG(S >= 1 && S <= 32, "a survey batch holds 1 to 32 systems");
     V.P = &P;
     V.st = st;
@@ -3189,6 +3190,7 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
             }
         }
         V.ch = best_ch;
+        V.autotuned = true;
         MTGPU_SP_DISPATCH(V.SP, grids(V, nsm));
     }
     trace.mark("SpMV autotuning");

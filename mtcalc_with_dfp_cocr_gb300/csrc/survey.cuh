@@ -67,6 +67,7 @@ struct Survey {
     int *uoff = nullptr, *ucol = nullptr;
     unsigned short *lc = nullptr, *lr = nullptr;
     float tune_ms[kSpmvVariants] = {};   // SpMV times of the variants 0, 1, 2, 4, 8, 18, 20, 32, 33, 34, 35
+    bool autotuned = false;              // the variant was chosen by this set-up's timing
     MatFree mf;
     int g_mff = 0, g_mfe = 0;                    // matrix-free launch grids (faces, edges)
     int g_mft = 0;                               // tiled matrix-free launch grid (variant 34)
