@@ -362,6 +362,11 @@ def gpu_arm(args):
     h2d = d2h = 0
     e2e_steps = max(1, min(args.steps, 3))
     e2e_setup = e2e_solve = 0.0
+    # one untimed call first, as the batched arm has its warm-up steps: the
+    # process's first one-system solve loads that width's kernels
+    xpin[0][:] = 0.0
+    solver.pcocr_2x2_folded(host[0], mesh_h, double_float=True, stop_on_true_residual=True,
+                            x=xpin[0])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
