@@ -21,10 +21,12 @@
 // (MRS.cpp:85-153, rci.cpp:66-75), per system; when a system stops, its true
 // residual ||b - A x|| / ||b|| is computed in FP64 and, if `verify` is set and
 // it is not below eps, the system keeps iterating or restarts on its FP64
-// residual (iterative refinement, FP64 solution).  One iteration is four kernels
-// (node gather, edge gather + (a,w), updates + MRS weight, SpMV + MRS +
-// (z,s)), captured in a CUDA graph several iterations at a time; all
-// per-system decisions are taken on the device.
+// residual (iterative refinement, FP64 solution).  One iteration is the node
+// gather, the edge gather + (a, w) (with the previous iteration's x += alpha
+// p), the updates + the MRS smoothing, and the SpMV + (z, s) (one kernel for
+// a stored matrix, two for the matrix-free forms), captured in a CUDA graph
+// several iterations at a time; all per-system decisions are taken on the
+// device by the block of each kernel that finishes last.
 #include "survey.cuh"
 #include "dfloat.cuh"
 
