@@ -362,6 +362,7 @@ def gpu_arm(args):
     h2d = d2h = 0
     e2e_steps = max(1, min(args.steps, 3))
     e2e_setup = e2e_solve = 0.0
+    e2e_calls = []
     # one untimed call first, as the batched arm has its warm-up steps: the
     # process's first one-system solve loads that width's kernels
     xpin[0][:] = 0.0
@@ -379,6 +380,7 @@ def gpu_arm(args):
                 raise RuntimeError(f"e2e solve failed with code {code}")
             e2e_setup += st.setup_seconds
             e2e_solve += st.solve_seconds
+            e2e_calls.append(round(st.setup_seconds * 1e3, 2))
             h2d += (s.ig.nbytes + s.jg.nbytes + s.idi.nbytes + s.ijg.nbytes + s.di.nbytes +
                     s.gg.nbytes + s.pr.nbytes + xh.nbytes)
             d2h += xh.nbytes
@@ -421,6 +423,7 @@ def gpu_arm(args):
                 "d2h_bytes_per_step": d2h // e2e_steps,
                 "setup_seconds_per_solve": e2e_setup / (e2e_steps * S),
                 "solve_seconds_per_solve": e2e_solve / (e2e_steps * S),
+                "setup_ms_per_call": e2e_calls,
                 "path": "mtgpu_pcocr_2x2_folded_ex(double_float=1, stop_on_true_residual=1), pinned host SLAE and x buffers"},
         "oracle_parity": oracle_err,
         "gpu_launches": int(launches),

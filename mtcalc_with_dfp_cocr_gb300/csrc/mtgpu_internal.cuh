@@ -201,22 +201,24 @@ double now_seconds();
 
 // MTGPU_TRACE=1 (environment): the phases of a set-up on stderr, each
 // after a synchronisation of its stream so that device work is charged to
-// the phase that launched it
+// the phase that launched it; MTGPU_TRACE=2: host time only, no
+// synchronisation (where the host itself waits)
 struct PhaseTrace {
-    bool on = false;
+    bool on = false, sync = true;
     cudaStream_t st;
     const char *what;
     double t0 = 0.0, last = 0.0;
     PhaseTrace(cudaStream_t s, const char *w) : st(s), what(w)
     {
         const char *e = getenv("MTGPU_TRACE");
-        on = e && *e == '1';
+        on = e && (*e == '1' || *e == '2');
+        sync = !(e && *e == '2');
         t0 = last = now_seconds();
     }
     void mark(const char *phase)
     {
         if (!on) return;
-        cudaStreamSynchronize(st);
+        if (sync) cudaStreamSynchronize(st);
         const double now = now_seconds();
         fprintf(stderr, "[mtgpu] %s %-22s %8.2f ms (total %8.2f)\n", what, phase, 1e3 * (now - last),
                 1e3 * (now - t0));

@@ -2038,6 +2038,81 @@ __global__ void k_gdiag_entry(int m, const int *__restrict__ gp, const int *__re
     tmv[j] = tm;
 }
 
+// The first pass on meshes with the compact G^T, one thread per edge k: row
+// k of A is read slot by slot (a warp's 32 rows side by side in the slice),
+// and both of column k's G entries (v_a, k) and (v_b, k) are formed, v_a and
+// v_b the G rows of k's first and second node.  G[v][c] is -1/2 where v is
+// the row of c's first node and +1/2 where it is its second's, so every
+// term and its place in the sum are those of k_gdiag_entry.  t[k] holds
+// (t of v_a, t of v_b).
+__global__ void k_gdiag_edge(int nb, const int2 *__restrict__ tn, const int *__restrict__ nc_row,
+                             const int *__restrict__ nr_row, const long long *__restrict__ pc,
+                             const long long *__restrict__ pr, const int *__restrict__ col_c,
+                             const double *__restrict__ kc, const double *__restrict__ mc,
+                             const int *__restrict__ col_r, const double *__restrict__ kr,
+                             double2 *tk, double2 *tm)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nb) return;
+    const int2 me = tn[k];
+    if (me.x < 0 && me.y < 0) return;
+    const int nc = nc_row[k], nr = nr_row[k];
+    double ak = 0.0, am = 0.0, bk = 0.0, bm = 0.0;
+    int qc = 0, qr = 0;
+    int cc = nc > 0 ? col_c[slot(pc, k, 0)] : 0x7fffffff;
+    int cr = nr > 0 ? col_r[slot(pr, k, 0)] : 0x7fffffff;
+    while (qc < nc || qr < nr) {
+        double kv, mv;
+        int c;
+        if (cc < cr) {
+            const long long t = slot(pc, k, qc++);
+            kv = kc[t];
+            mv = mc[t];
+            c = cc;
+            cc = qc < nc ? col_c[slot(pc, k, qc)] : 0x7fffffff;
+        } else {
+            kv = kr[slot(pr, k, qr++)];
+            mv = 0.0;
+            c = cr;
+            cr = qr < nr ? col_r[slot(pr, k, qr)] : 0x7fffffff;
+        }
+        const int2 o = __ldg(tn + c);
+        const double ga = me.x < 0 ? 0.0 : (o.x == me.x ? -0.5 : (o.y == me.x ? 0.5 : 0.0));
+        const double gb = me.y < 0 ? 0.0 : (o.x == me.y ? -0.5 : (o.y == me.y ? 0.5 : 0.0));
+        if (ga != 0.0) {
+            ak = __dadd_rn(ak, __dmul_rn(kv, ga));
+            am = __dadd_rn(am, __dmul_rn(mv, ga));
+        }
+        if (gb != 0.0) {
+            bk = __dadd_rn(bk, __dmul_rn(kv, gb));
+            bm = __dadd_rn(bm, __dmul_rn(mv, gb));
+        }
+    }
+    tk[k] = make_double2(ak, bk);
+    tm[k] = make_double2(am, bm);
+}
+
+// the second pass over k_gdiag_edge's per-edge values: node v's entries in
+// G's order, each t taken from the side of its edge that v is
+__global__ void k_gdiag_nodes(int m, const int *__restrict__ gp, const int *__restrict__ gj,
+                              const double *__restrict__ gv, const int2 *__restrict__ tn,
+                              const double2 *__restrict__ tk, const double2 *__restrict__ tm,
+                              double *gkg, double *gmg)
+{
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= m) return;
+    double sk = 0.0, sm = 0.0;
+    for (int j = gp[v]; j < gp[v + 1]; j++) {
+        const int e = gj[j];
+        const bool first = tn[e].x == v;
+        const double2 a = tk[e], b = tm[e];
+        sk = __dadd_rn(sk, __dmul_rn(first ? a.x : a.y, gv[j]));
+        sm = __dadd_rn(sm, __dmul_rn(first ? b.x : b.y, gv[j]));
+    }
+    gkg[v] = sk;
+    gmg[v] = sm;
+}
+
 __global__ void k_gdiag_rows(int m, const int *__restrict__ gp, int *rowof)
 {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
@@ -3032,7 +3107,27 @@ int survey_setup(const ParamMatrix &P, const mtgpu_mesh_desc &mesh, int S, const
             k_f64_to_f32<<<(nnz + kB - 1) / kB, kB, 0, st>>>(nnz, V.G.d_tv, V.tv32);
         }
     }
-    if (m > 0) {
+    // MTGPU_GDIAG_ENTRIES=1 (environment): the per-entry passes on every mesh
+    const char *ge = getenv("MTGPU_GDIAG_ENTRIES");
+    const bool per_edge = V.G.d_tn && !(ge && *ge == '1');
+    if (m > 0 && per_edge) {
+        double2 *tk = nullptr, *tm = nullptr;
+        if ((rc = dev_alloc(&tk, V.nb)) || (rc = dev_alloc(&tm, V.nb))) {
+            dev_free(tk);
+            return rc;
+        }
+        k_gdiag_edge<<<ceil_div(V.nb, kB), kB, 0, st>>>(V.nb, V.G.d_tn, P.d_nc, P.d_nr, P.d_pc,
+                                                        P.d_pr, P.d_col_c, P.d_kc, P.d_mc,
+                                                        P.d_col_r, P.d_kr, tk, tm);
+        k_gdiag_nodes<<<ceil_div(m, kB), kB, 0, st>>>(m, V.G.d_gp, V.G.d_gj, V.G.d_gv, V.G.d_tn,
+                                                      tk, tm, V.gkg, V.gmg);
+        note_launches(2);
+        cudaStreamSynchronize(st);
+        dev_free(tk);
+        dev_free(tm);
+        const size_t nm = (size_t)m * V.SP;
+        k_diag_s<<<(unsigned)((nm + kB - 1) / kB), kB, 0, st>>>(m, V.SP, V.gkg, V.gmg, V.omega64, V.ds);
+    } else if (m > 0) {
         int nnz = 0;
         MTGPU_TRY(cudaMemcpyAsync(&nnz, V.G.d_gp + m, sizeof(int), cudaMemcpyDeviceToHost, st));
         MTGPU_TRY(cudaStreamSynchronize(st));

@@ -390,3 +390,25 @@ def test_fused_preconditioner(gpu, monkeypatch, name, systems):
         a = res["1"][1][k].view(np.complex128)[earth]
         r = res["0"][1][k].view(np.complex128)[earth]
         assert np.linalg.norm(a - r) <= 1e-7 * np.linalg.norm(r)
+
+
+@pytest.mark.parametrize("name,systems", [("small", [(0.1, 1), (0.1, 0), (10.0, 1)]),
+                                          ("c1", [(1.0, 1), (1.0, 0)])])
+def test_preconditioner_diagonal_passes_agree(gpu, monkeypatch, name, systems):
+    """diag(G K G^T) and diag(G M G^T) from the per-edge passes (meshes with
+    the compact G^T: row k of A read once for both nodes of edge k) have the
+    terms and the summation order of the per-entry passes
+    (MTGPU_GDIAG_ENTRIES=1): with one SpMV variant pinned, the two set-ups
+    give the same solves bit for bit."""
+    torch = gpu
+    monkeypatch.setenv("MTGPU_SPMV_VARIANT", "4")
+    monkeypatch.setenv("MTGPU_PREC_TILE", "0")
+    out = {}
+    for entries in ("0", "1"):
+        monkeypatch.setenv("MTGPU_GDIAG_ENTRIES", entries)
+        w, A, tabs, b, x, code, st = _run(torch, name, systems)
+        assert code == 0 and max(st["true_residual_rel"]) < 1e-8
+        out[entries] = (st["iterations"], x.clone())
+        A.close()
+    assert out["0"][0] == out["1"][0]
+    assert torch.equal(out["0"][1], out["1"][1])
