@@ -17,8 +17,9 @@
 // a is read (a_in) and written (a_out) in different buffers: the halo of a
 // tile reads a neighbour tile's edges.  The sums run in the order of k_node
 // (a node's edges by increasing number: -z, -y, -x, +x, +y, +z) and k_edge
-// (D_A a, then the first node's -1/2 h, then the second's +1/2 h), so p, a,
-// w and (a, w) equal the two-kernel form's to the last bit.
+// (D_A a, then the first node's -1/2 h, then the second's +1/2 h), so p, a
+// and w equal the two-kernel form's to the last bit; the grid sum (a, w)
+// groups its terms by tile and so rounds differently.
 
 template <int SP>
 struct PrecTile {

@@ -799,11 +799,14 @@ k_spmv_r2(int nb, Mat A, const float2 *__restrict__ omega, const float4 *__restr
 // them).  So A s = D^T F_g D s + i omega M s with F_g, M regenerated from
 // six weights per cell (wF / 3 and sigma wM / 9, double-float; the 1/3 and
 // 1/9 make the remaining multipliers 1, 2, 4, exact) instead of 33 stored
-// slots per row.  Two passes: the circulation of every face
-// (k_mf_faces), then per edge the 4 faces through it, their neighbours
-// along the normal and the 3 x 3 parallel edges of the 4 cells around it
-// (k_mf_edges, with the SpMV tail).  Dirichlet edges (both nodes on the
-// boundary) read as 0 and map to themselves, as in the assembled matrix.
+// slots per row.  Variants 32 and 33 make two passes: the circulation of
+// every face (k_mf_faces), then per edge the 4 faces through it, their
+// neighbours along the normal and the 3 x 3 parallel edges of the 4 cells
+// around it (k_mf_edges / k_mf_edges2: z and (z, s)).  Variant 35 forms
+// g = F f per face straight from s (k_mf_gmarch) and sums the 4 g of each
+// edge (k_mf_edges_g); variant 34 is one tiled kernel (mf_tile.cuh).
+// Dirichlet edges (both nodes on the boundary) read as 0 and map to
+// themselves, as in the assembled matrix.
 struct MF {
     int nx, ny, nz;
     long long nfx, nfy, nfz, ncell;
