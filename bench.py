@@ -58,7 +58,7 @@ WORKLOAD = "c2"
 # launches it), per variant: the sum of its kernels' ncu dram__bytes_read.sum
 # + dram__bytes_write.sum (profiles/bench_c2_launch_list.md,
 # profiles/spmv_matfree_c2_s2.md)
-SPMV_MF_TRAFFIC_C2 = {32: 306.3e6, 35: 379.7e6}
+SPMV_MF_TRAFFIC_C2 = {32: 306.3e6}
 # what bounds the matrix-free SpMV instead of HBM (ncu on c2, two lanes)
 SPMV_MF_BINDING = ("FP32 issue: k_mf_edges<2> 69 % issue-active, 51 % FMA pipe, 42 double-float "
                    "multiply-adds of 12 FP32 instructions per edge and system "
@@ -297,21 +297,20 @@ def gpu_arm(args):
     # runs in k_update)
     tail = 0
     if variant in (32, 33, 35):
-        # matrix-free, per launch as the iteration runs it: the faces kernel
-        # reads s and writes the face circulations f; variants 32/33: the
+        # matrix-free, per launch as the iteration runs it.  Variants 32/33:
+        # the faces kernel reads s and writes the face circulations f, the
         # edges kernel reads f, s, the six double-float weights of every cell
-        # and the row positions and writes z; variant 35: a face kernel reads
-        # f and the cells' face weights and writes g = F f, the edges kernel
-        # reads g, s, the cells' mass weights and the row positions and
-        # writes z.  Each value counted once.
+        # and the row positions and writes z.  Variant 35: k_mf_gmarch reads
+        # s and the cells' face weights and writes g = F f per face, the
+        # edges kernel reads g, s, the cells' mass weights and the row
+        # positions and writes z.  Each value counted once: the same bytes.
         nx_, ny_, nz_ = m_.nx, m_.ny, m_.nz
         nf = nx_ * (ny_ - 1) * (nz_ - 1) + (nx_ - 1) * ny_ * (nz_ - 1) + (nx_ - 1) * (ny_ - 1) * nz_
+        spmv_bytes = 16 * SP * (3 * nb + 2 * nf) + 48 * m_.kpar + 4 * nb + tail
         if variant == 35:
-            spmv_bytes = 16 * SP * (3 * nb + 4 * nf) + 48 * m_.kpar + 4 * nb + tail
-            spmv_kernel = ("k_mf_faces + k_mf_gface + k_mf_edges_g (matrix-free double-float "
-                           "SpMV, face mass applied per face, S systems)")
+            spmv_kernel = ("k_mf_gmarch + k_mf_edges_g (matrix-free double-float SpMV, g = F f "
+                           "formed per face from s, S systems)")
         else:
-            spmv_bytes = 16 * SP * (3 * nb + 2 * nf) + 48 * m_.kpar + 4 * nb + tail
             edges = "k_mf_edges2" if variant == 33 else "k_mf_edges"
             spmv_kernel = f"k_mf_faces + {edges} (matrix-free double-float SpMV, S systems)"
         traffic = SPMV_MF_TRAFFIC_C2.get(variant) if WORKLOAD == "c2" else None
