@@ -351,6 +351,14 @@ def gpu_arm(args):
                          pin_memory=True).numpy()
         t_[...] = v
         return t_
+    # the mesh tables the call uploads (cell nodes and materials, edges,
+    # Dirichlet flags, node coordinates, material flags) pinned too, in the
+    # types the call takes
+    for fld, dt in (("xyz", np.float64), ("nvkat", np.int32), ("nver", np.int32),
+                    ("sigma", np.float64), ("edges", np.int32), ("is_node_bound", np.int32)):
+        setattr(mesh_h, fld, pinned(np.ascontiguousarray(getattr(mesh_h, fld), dtype=dt)))
+    mesh_bytes = (mesh_h.xyz.nbytes + mesh_h.nvkat.nbytes + mesh_h.nver.nbytes +
+                  mesh_h.sigma.nbytes + mesh_h.edges.nbytes + mesh_h.is_node_bound.nbytes)
     host, xpin = {}, {}
     for k, (f, a) in enumerate(systems):
         t = tables[f]
@@ -382,7 +390,7 @@ def gpu_arm(args):
             e2e_solve += st.solve_seconds
             e2e_calls.append(round(st.setup_seconds * 1e3, 2))
             h2d += (s.ig.nbytes + s.jg.nbytes + s.idi.nbytes + s.ijg.nbytes + s.di.nbytes +
-                    s.gg.nbytes + s.pr.nbytes + xh.nbytes)
+                    s.gg.nbytes + s.pr.nbytes + xh.nbytes + mesh_bytes)
             d2h += xh.nbytes
     e2e_s = (time.perf_counter() - t0) / (e2e_steps * S)
     A.close()
@@ -424,7 +432,7 @@ def gpu_arm(args):
                 "setup_seconds_per_solve": e2e_setup / (e2e_steps * S),
                 "solve_seconds_per_solve": e2e_solve / (e2e_steps * S),
                 "setup_ms_per_call": e2e_calls,
-                "path": "mtgpu_pcocr_2x2_folded_ex(double_float=1, stop_on_true_residual=1), pinned host SLAE and x buffers"},
+                "path": "mtgpu_pcocr_2x2_folded_ex(double_float=1, stop_on_true_residual=1), pinned host SLAE, mesh and x buffers"},
         "oracle_parity": oracle_err,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
