@@ -1004,8 +1004,21 @@ __device__ __forceinline__ dfc mf_face_f(const MF &M, const float4 *__restrict__
     return dfc{fr.get(), fi.get()};
 }
 
+// the circulation a + b - c - d in mf_face_f's order
+__device__ __forceinline__ dfc mf_circ(dfc a, dfc b, dfc c, dfc d)
+{
+    acc fr, fi;
+    fr.add(a.re); fr.add(b.re); fr.add(neg(c.re)); fr.add(neg(d.re));
+    fi.add(a.im); fi.add(b.im); fi.add(neg(c.im)); fi.add(neg(d.im));
+    return dfc{fr.get(), fi.get()};
+}
+
 // f = D s: x(e0) + x(e1) - x(e2) - x(e3) around every face (counterclockwise
-// seen from +n: y then z for n = x, z then x for n = y, x then y for n = z)
+// seen from +n: y then z for n = x, z then x for n = y, x then y for n = z).
+// One thread per node and system forms the x-, y- and z-normal faces at the
+// node (those that exist): 9 edge values instead of 12 (the node's own
+// three edges are shared), one position decode instead of three; each sum
+// is mf_face_f's, so f is the same to the last bit.
 template <int SP>
 __global__ void __launch_bounds__(kB)
 k_mf_faces(MF M, const float4 *__restrict__ x, const SysState *sys, int rev)
@@ -1013,13 +1026,28 @@ k_mf_faces(MF M, const float4 *__restrict__ x, const SysState *sys, int rev)
     pdl_wait();
     const int k = threadIdx.x % SP;
     if (sys[k].status != kRun) return;
-    const int nf = (int)(M.nfx + M.nfy + M.nfz);
+    const int nx = M.nx, ny = M.ny, nz = M.nz;
+    const int nn = nx * ny * nz;
     const int rpb = kB / SP;
-    for (int ti = blockIdx.x * rpb + threadIdx.x / SP; ti < nf; ti += gridDim.x * rpb) {
-        const int t = sweep(ti, nf, rev);
-        int n, i, j, kk;
-        mf_face_pos(M, t, n, i, j, kk);
-        M.f[t * SP + k] = to4(mf_face_f<SP>(M, x, n, i, j, kk, k));
+    const dfc zero{df{0.f, 0.f}, df{0.f, 0.f}};
+    for (int ti = blockIdx.x * rpb + threadIdx.x / SP; ti < nn; ti += gridDim.x * rpb) {
+        const int v = sweep(ti, nn, rev);
+        const int r = v / nx, i = v - r * nx;
+        const int kk = r / ny, j = r - kk * ny;
+        // the node's +x, +y, +z edges exist below the last line of their axis
+        const bool hx = i < nx - 1, hy = j < ny - 1, hz = kk < nz - 1;
+        const dfc ex = hx ? mf_x<SP>(M, x, 0, i, j, kk, k) : zero;
+        const dfc ey = hy ? mf_x<SP>(M, x, 1, i, j, kk, k) : zero;
+        const dfc ez = hz ? mf_x<SP>(M, x, 2, i, j, kk, k) : zero;
+        if (hy && hz)
+            M.f[(M.fb[0] + (kk * (ny - 1) + j) * nx + i) * SP + k] =
+                to4(mf_circ(ey, mf_x<SP>(M, x, 2, i, j + 1, kk, k), mf_x<SP>(M, x, 1, i, j, kk + 1, k), ez));
+        if (hx && hz)
+            M.f[(M.fb[1] + (kk * ny + j) * (nx - 1) + i) * SP + k] =
+                to4(mf_circ(ez, mf_x<SP>(M, x, 0, i, j, kk + 1, k), mf_x<SP>(M, x, 2, i + 1, j, kk, k), ex));
+        if (hx && hy)
+            M.f[(M.fb[2] + (kk * (ny - 1) + j) * (nx - 1) + i) * SP + k] =
+                to4(mf_circ(ex, mf_x<SP>(M, x, 1, i + 1, j, kk, k), mf_x<SP>(M, x, 0, i, j + 1, kk, k), ey));
     }
 }
 
@@ -2372,9 +2400,9 @@ struct Impl {
                          : V.ch == 8 ? (const void *)k_spmv<SP, 8> : (const void *)k_spmv<SP, 4>;
         V.g_spmv = g(fs, V.grid_rows);
         if (V.mf.on) {
-            const long long nf = V.mf.nfx + V.mf.nfy + V.mf.nfz;
+            const long long nn = (long long)V.mf.nx * V.mf.ny * V.mf.nz;
             V.g_mff = g((const void *)k_mf_faces<SP>, (int)std::min<long long>(
-                                                          (nf + kB / SP - 1) / (kB / SP), INT_MAX));
+                                                          (nn + kB / SP - 1) / (kB / SP), INT_MAX));
             V.g_mfe = g((const void *)k_mf_edges<SP>, V.grid_rows);
             {
                 const GMarch G = gmarch(V);
